@@ -1,0 +1,192 @@
+"""Generate the golden fixtures under tests/golden/ from the SpecMC reference.
+
+Run once, in a container where the reference package is importable:
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+
+Every fixture is a small ``.npz`` written by the reference's own public API
+(``specmc.api.build_model`` / ``march_adaptive`` / ``model.diagnostics``) or
+by its own transform / operator objects, on seeded inputs built here.  Nothing
+in the test suite imports the reference: the tests read only these files.
+
+Fixtures (sizes chosen so the whole script runs in a few minutes):
+
+* ``transforms_16x12.npz`` -- ``RBC.grid / coeffs / _synth_pad / _trunc_pad``
+  and the basis matrices on a seeded random coefficient field.
+* ``march_<case>.npz`` -- initial state, every step's dt and state, the final
+  diagnostics and the model's counters for one adaptive march per case.
+* ``coupled_ops_16x12.npz`` -- ``eta_of``, ``FreeSchurOperator.matvec``, the
+  assembled Schur matrix and the BFBT preconditioner action for one seeded
+  state (pins the coupled operator, including its partner half).
+"""
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def seeded_noise_theta(model, amp, mmax, nmax, seed, Lx, H=0.0):
+    """Conductive profile (H) plus seeded mirror-symmetric noise, as coeffs.
+
+    noise = sum_{m<=mmax, n<=nmax} a_mn cos(2 pi m x / Lx) sin(n pi z),
+    a_mn ~ U(-1, 1), scaled so max|noise| = amp on the model grid.
+    """
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(-1.0, 1.0, size=(mmax, nmax))
+    X, Z = np.meshgrid(model.x, model.z, indexing='ij')
+    g = np.zeros_like(X)
+    for m in range(1, mmax + 1):
+        for n in range(1, nmax + 1):
+            g += a[m - 1, n - 1] * np.cos(2.0 * np.pi * m * X / Lx) \
+                * np.sin(n * np.pi * Z)
+    g *= amp / np.abs(g).max()
+    g += 0.5 * H * Z * (1.0 - Z)
+    return model.coeffs(g)
+
+
+COUNTER_KEYS = (
+    'n_refresh', 'n_defect', 'n_defect_failed', 'n_defect_double_fail',
+    'n_memo_hits', 'n_stokes', 'n_bfbt_solves', 'n_bfbt_iters',
+    'n_bfbt_rescue', 'n_clip_eta', 'n_smooth_eta', 'n_clip_eta_proj',
+    'n_steps')
+
+
+def counters(m):
+    out = {}
+    for k in COUNTER_KEYS:
+        if hasattr(m, k):
+            out['ctr_' + k] = np.int64(getattr(m, k))
+    th = getattr(m, 'theta', None)
+    if th is not None:
+        out['ctr_theta_n_nonconv'] = np.int64(th.n_nonconv)
+        out['ctr_theta_n_be_fallback'] = np.int64(th.n_be_fallback)
+        out['ctr_theta_last_iters'] = np.int64(th.last_iters)
+    return out
+
+
+def march_case(name, cfg_kw, steps, ic, S):
+    api = S.api
+    cfg = S.ConvectionConfig(**cfg_kw)
+    m = api.build_model(cfg)
+    if ic[0] == 'seed':
+        th0 = m.seed(amp=ic[1], m=ic[2], n=ic[3])
+    else:
+        th0 = seeded_noise_theta(m, amp=ic[1], mmax=ic[2], nmax=ic[3],
+                                 seed=ic[4], Lx=cfg.Lx,
+                                 H=cfg.internal_heating)
+    states, dts = [], []
+    s = np.array(th0, copy=True)
+    t = 0.0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dt = api.production_dt(m, s)
+        s = m.step(s, dt)
+        t += dt
+        states.append(s.copy())
+        dts.append(dt)
+    el = time.perf_counter() - t0
+    d = m.diagnostics(s)
+    rec = dict(that0=th0, states=np.array(states), dts=np.array(dts),
+               t=np.float64(t), wall_s=np.float64(el),
+               **{'diag_' + k: np.float64(v) for k, v in d.items()},
+               **counters(m))
+    for k, v in cfg_kw.items():
+        rec['cfg_' + k] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, 'march_%s.npz' % name), **rec)
+    print('%-14s %3d steps  %.2f s  Nu_top=%.10f urms=%.10f'
+          % (name, steps, el, d['Nu_top'], d['urms']), flush=True)
+
+
+def transforms_case(S):
+    from specmc.core.rbc_galerkin import RBC
+    rng = np.random.default_rng(7)
+    m = RBC(Ra=1e4, Nx=16, Nz=12)
+    cf = rng.standard_normal((m.Nk, m.Nz)) + 1j * rng.standard_normal((m.Nk, m.Nz))
+    g = rng.standard_normal((m.Nx, m.Nz))
+    gp = rng.standard_normal((m.Np, m.Nz))
+    psi, om = m.stokes(cf)
+    ux, uz = m.velocity(psi)
+    np.savez_compressed(
+        os.path.join(HERE, 'transforms_16x12.npz'),
+        cf=cf, g=g, gp=gp, grid=m.grid(cf), coeffs=m.coeffs(g),
+        synth_pad=m._synth_pad(cf), trunc_pad=m._trunc_pad(gp),
+        V=m.V, Vi=m.Vi, D=m.D, z=m.z, x=m.x, kx=m.kx, wq=m.wq,
+        psi=psi, om=om, ux=ux, uz=uz, step=m.step(cf, 1e-4),
+        seed=m.seed(amp=3e-2, m=1, n=1))
+    print('transforms_16x12 written', flush=True)
+
+
+def coupled_ops_case(S):
+    from specmc.models.coupled_model import RBCCoupled
+    from specmc.stokes.lagged_stokes import FreeSchurOperator
+    from specmc.stokes.stokes_coupled import CoupledStokes
+    from specmc.stokes.bfbt import SpectralBFBTPrecond
+    m = RBCCoupled(Nx=16, Nz=12, deta_T=1000.0, eta_drift_tol=0.1,
+                   defect_tol=1e-8)
+    th = seeded_noise_theta(m, amp=0.3, mmax=4, nmax=4, seed=11, Lx=m.Lx)
+    eta = m.eta_of(th)
+    rng = np.random.default_rng(3)
+    n = m.Nk * m.Nz
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    op = CoupledStokes(m, eta)
+    fop = FreeSchurOperator(m, eta, op_template=op)
+    P = SpectralBFBTPrecond(m, eta, profile='harm')
+    G = np.array([op.green(i) for i in range(m.Nk)])
+    psi, om = m.stokes(th)
+    np.savez_compressed(
+        os.path.join(HERE, 'coupled_ops_16x12.npz'),
+        that=th, eta=eta, v=v, Av=fop.matvec(v), A=op.assemble_schur(),
+        b=op.rhs_schur(th), Pv=P.apply(v), G=G, eta_c=fop.eta_c,
+        psi=psi, om=om)
+    print('coupled_ops_16x12 written', flush=True)
+
+
+def main(ref_root):
+    sys.path.insert(0, ref_root)
+    import specmc.api as api
+    from specmc.config import ConvectionConfig
+
+    class S:
+        pass
+    S.api = api
+    S.ConvectionConfig = ConvectionConfig
+
+    transforms_case(S)
+    coupled_ops_case(S)
+    base = dict(Ra=1e4, Nx=32, Nz=24)
+    # configuration 1 of the headline table: isoviscous, march to t = 1e-3
+    march_case('const_32x24', dict(base, viscosity_model='const'), 25,
+               ('seed', 3e-2, 1, 1), S)
+    march_case('etaz_32x24', dict(base, viscosity_model='eta_z',
+                                  deta_T=100.0), 20, ('seed', 3e-2, 1, 1), S)
+    march_case('etaT_32x24', dict(base, viscosity_model='eta_T'), 25,
+               ('seed', 3e-2, 1, 1), S)
+    march_case('etaT_bfbt_32x24', dict(base, viscosity_model='eta_T',
+                                       precond='bfbt'), 12,
+               ('seed', 3e-2, 1, 1), S)
+    # internally heated 2:1 box (Lx = 4 is the mirror-doubled carrier)
+    march_case('heated_2to1_32x24',
+               dict(base, viscosity_model='eta_T', Lx=4.0, Ra=1.25e4,
+                    internal_heating=1.5), 12,
+               ('noise', 1e-2, 8, 8, 1234), S)
+    # Arrhenius + window + dissipation + heating (the large-run physics)
+    march_case('arrhenius_32x24',
+               dict(base, viscosity_model='arrhenius', deta_T=1e3,
+                    arrhenius_Ts=1.0, eta_min=1e-3, eta_max=1.0,
+                    dissipation_number=0.5, internal_heating=1.0),
+               12, ('noise', 1e-2, 8, 8, 99), S)
+    # smooth eta window that is active on this state
+    march_case('smooth_32x24',
+               dict(base, viscosity_model='eta_T', eta_min=3e-3, eta_max=1.0,
+                    eta_smooth=0.5), 10, ('seed', 3e-2, 1, 1), S)
+    # configuration 2 grid, a few steps (the oracle of the bench workload)
+    march_case('etaT_64x96', dict(Ra=1e4, Nx=64, Nz=96,
+                                  viscosity_model='eta_T'), 6,
+               ('seed', 3e-2, 1, 1), S)
+
+
+if __name__ == '__main__':
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')

@@ -1,0 +1,93 @@
+"""The CPU oracle against fixtures written by the SpecMC reference itself.
+
+These pin the oracle (the checker of the GPU path): if it drifts from the
+reference, every GPU parity test downstream would be measuring against the
+wrong thing.
+"""
+import os
+import types
+
+import numpy as np
+import pytest
+
+from oracle import specmc_oracle as O
+
+from conftest import GOLDEN
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def _rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300))
+
+
+def test_basis_and_transforms():
+    g = _load("transforms_16x12.npz")
+    m = O.ConstModel(Ra=1e4, Nx=16, Nz=12)
+    assert np.array_equal(m.D, g["D"])
+    assert np.array_equal(m.V, g["V"])
+    assert _rel(m.Vi, g["Vi"]) < 1e-15
+    assert _rel(m.wq, g["wq"]) < 1e-14
+    assert _rel(m.grid(g["cf"]), g["grid"]) < 1e-14
+    assert _rel(m.coeffs(g["g"]), g["coeffs"]) < 1e-14
+    assert _rel(m.synth_pad(g["cf"]), g["synth_pad"]) < 1e-14
+    assert _rel(m.trunc_pad(g["gp"]), g["trunc_pad"]) < 1e-14
+    psi, om = m.stokes(g["cf"])
+    assert _rel(psi, g["psi"]) < 1e-13 and _rel(om, g["om"]) < 1e-13
+    ux, uz = m.velocity(psi)
+    assert _rel(ux, g["ux"]) < 1e-13 and _rel(uz, g["uz"]) < 1e-13
+    assert _rel(m.step(g["cf"], 1e-4), g["step"]) < 1e-13
+    assert _rel(m.seed(amp=3e-2, m=1, n=1), g["seed"]) < 1e-15
+
+
+def test_coupled_operator():
+    g = _load("coupled_ops_16x12.npz")
+    m = O.CoupledModel(Nx=16, Nz=12, deta_T=1000.0)
+    eta = m.eta_of(g["that"])
+    assert _rel(eta, g["eta"]) < 1e-14
+    assert _rel(np.array(m.G), g["G"]) < 1e-14
+    Ms = m.eta_mats(eta)
+    assert _rel(m.coeffs(eta), g["eta_c"]) < 1e-14
+    assert _rel(m.schur_matvec(Ms, g["v"]), g["Av"]) < 1e-13
+    assert _rel(m.assemble_schur(Ms), g["A"]) < 1e-13
+    assert _rel(m.rhs_schur(g["that"]), g["b"]) < 1e-15
+    lus = m.bfbt_lus(eta)
+    N = m.Nz
+    v = g["v"].copy()
+    Pv = np.concatenate([__import__("scipy.linalg").linalg.lu_solve(
+        lus[i], np.where(np.arange(N) < N - 2, v[i * N:(i + 1) * N], 0.0)) for i in range(m.Nk)])
+    assert _rel(Pv, g["Pv"]) < 1e-12
+    m2 = O.CoupledModel(Nx=16, Nz=12, deta_T=1000.0)
+    psi, om = m2.stokes(g["that"])
+    assert _rel(psi, g["psi"]) < 1e-9 and _rel(om, g["om"]) < 1e-9
+
+
+CASES = ["const_32x24", "etaz_32x24", "etaT_32x24", "etaT_bfbt_32x24",
+         "heated_2to1_32x24", "arrhenius_32x24", "smooth_32x24"]
+
+
+def _cfg_from(g):
+    kw = {k[4:]: g[k].item() for k in g.files if k.startswith("cfg_")}
+    from specmc_gb300.config import ConvectionConfig
+    return ConvectionConfig(**kw)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_march_matches_reference(case):
+    g = _load("march_%s.npz" % case)
+    cfg = _cfg_from(g)
+    m = O.build(cfg)
+    s = np.array(g["that0"], copy=True)
+    worst = 0.0
+    for n in range(len(g["dts"])):
+        dt = O.production_dt(m, s)
+        assert abs(dt - g["dts"][n]) <= 1e-9 * g["dts"][n], (n, dt, g["dts"][n])
+        s = m.step(s, dt)
+        worst = max(worst, _rel(s, g["states"][n]))
+    d = m.diagnostics(s)
+    assert worst < 1e-7, worst
+    for key in ("Nu_top", "urms", "Nu_energy"):
+        ref = g["diag_" + key].item()
+        assert abs(d[key] - ref) <= 1e-9 * abs(ref), (key, d[key], ref)

@@ -1,0 +1,173 @@
+/*
+ * specmc_gb300 -- C ABI of the GB300 time step of SpecMC.
+ *
+ * The reference (SpecMC) is a pure-Python package with no FFI; its public
+ * surface for this path is `ConvectionConfig` + `specmc.api.build_model /
+ * march / march_adaptive / production_dt / describe` and the duck-typed model
+ * object those functions drive (`step`, `cfl_dt`, `diagnostics`, `stokes`,
+ * `grid`, `coeffs`, counters).  Each entry point below replaces one of those
+ * calls; the comment names the reference function (file:line, paths inside
+ * the reference repository) whose behaviour it reproduces.
+ *
+ * Conventions
+ *   - Spectral state `that`: (Nk, Nz) complex128, row-major, interleaved
+ *     (re, im) doubles, Nk = Nx/2 + 1.  Row k is the rfft mode kx = 2 pi k/Lx,
+ *     column n the Chebyshev coefficient of T_n(2z - 1).
+ *   - Grid fields: (Ng, Nz) float64 row-major, x node i, ascending CGL node j.
+ *   - `mem` selects where a caller pointer lives: SMC_HOST (pageable or
+ *     pinned host memory; copies happen inside the call) or SMC_DEVICE
+ *     (device memory of the handle's GPU; no copy).
+ *   - Return value: 0 success; < 0 hard error (the message is available from
+ *     smc_last_error()).  Soft numerical trouble is never an error: it is
+ *     counted in smc_counters, as the reference counts it.
+ *   - A handle owns its device buffers and one CUDA stream; it is not
+ *     re-entrant.  Different handles may be used from different threads.
+ *   - No call reads or writes the caller's input buffers after it returns.
+ */
+#ifndef SPECMC_GB300_H
+#define SPECMC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SMC_ABI_VERSION 1
+
+enum smc_model { SMC_MODEL_CONST = 0, SMC_MODEL_ETA_Z = 1, SMC_MODEL_ETA_T = 2 };
+enum smc_precond { SMC_PRECOND_LEGACY = 0, SMC_PRECOND_BFBT = 1 };
+enum smc_precision { SMC_FP64 = 0, SMC_MIXED = 1 };
+enum smc_mem { SMC_HOST = 0, SMC_DEVICE = 1 };
+enum smc_transform {
+  SMC_GRID = 0,       /* (Nk,Nz) coeffs -> (Nx,Nz) values   rbc_galerkin.py:322 */
+  SMC_COEFFS = 1,     /* (Nx,Nz) values -> (Nk,Nz) coeffs   rbc_galerkin.py:327 */
+  SMC_SYNTH_PAD = 2,  /* (Nk,Nz) coeffs -> (2Nx,Nz) values  rbc_galerkin.py:332 */
+  SMC_TRUNC_PAD = 3   /* (2Nx,Nz) values -> (Nk,Nz) x-modes rbc_galerkin.py:338 */
+};
+
+/* One scenario, already translated from ConvectionConfig by the recipe
+ * modules (specmc/models/{const,eta_z,eta_T}.py kwargs()).  Zero-initialise
+ * and call smc_config_defaults() before filling it. */
+typedef struct smc_config {
+  int abi_version;          /* SMC_ABI_VERSION */
+  int model;                /* enum smc_model (arrhenius = ETA_T with arrhenius_Ts > 0) */
+  int Nx, Nz;
+  double Ra, Lx, deta_T;
+  double internal_heating;  /* H   */
+  double dissipation_number;/* Di  */
+  double eta_min, eta_max, eta_smooth;
+  double arrhenius_Ts;      /* 0 = exponential law */
+  int precond;              /* enum smc_precond */
+  int symmetrize;
+  int lag, K, max_K;
+  double defect_tol;        /* <= 0 selects the fixed-K route */
+  double eta_drift_tol;
+  double stokes_rtol, theta_rtol;
+  int theta_maxiter, theta_restart;
+  int stokes_restart, stokes_maxiter;
+  int precision;            /* enum smc_precision */
+  int device;               /* CUDA ordinal */
+} smc_config;
+
+typedef struct smc_handle smc_handle;
+
+typedef struct smc_diag {   /* RBC.diagnostics, rbc_galerkin.py:439-453 */
+  double Nu_top, Nu_bot, Nu_energy, urms, umax, amp;
+} smc_diag;
+
+typedef struct smc_counters {
+  long long n_steps, n_stokes, n_memo_hits;
+  long long n_refresh, n_defect, n_defect_failed, n_defect_double_fail;
+  long long n_bfbt_solves, n_bfbt_iters, n_bfbt_rescue, n_bfbt_rescue_direct,
+            n_bfbt_rescue_weak;
+  long long n_clip_T, n_T_out_of_range, n_clip_eta, n_smooth_eta,
+            n_clip_eta_proj, n_smooth_eta_proj;
+  long long n_theta_nonconv, n_be_fallback, n_theta_solves, n_theta_iters;
+  long long theta_last_iters, last_K;
+  double max_T_excursion, last_corr, theta_last_res, last_bfbt_true_res,
+         sym_removed;
+  long long n_kernel_launches;       /* kernels this handle has launched */
+} smc_counters;
+
+typedef struct smc_march_info {     /* api.march_adaptive return dict */
+  long long steps;
+  double t, dt;
+} smc_march_info;
+
+/* Fill `cfg` with the production defaults (specmc/_numerics.py:67-148,
+ * specmc/config.py:240-423). */
+void smc_config_defaults(smc_config* cfg);
+
+/* Build a model: api.build_model (specmc/api.py:102-110) -> RBC /
+ * RBCImplicitTheta / RBCCoupled constructors (rbc_galerkin.py:258-315,
+ * implicit_theta.py:557-599, coupled_model.py:128-330). */
+int smc_create(const smc_config* cfg, smc_handle** out);
+int smc_destroy(smc_handle* h);
+
+/* model.step(that, dt) -> new state (rbc_galerkin.py:426, implicit_theta.py:608,
+ * via the coupled model's memoised Stokes solve coupled_model.py:725). */
+int smc_step(smc_handle* h, const double* that_in, double* that_out, int mem, double dt);
+
+/* model.cfl_dt(that, safety, dtmax, dtmin) (rbc_galerkin.py:465-471). */
+int smc_cfl_dt(smc_handle* h, const double* that_in, int mem, double safety,
+               double dtmax, double dtmin, double* dt_out);
+
+/* api.production_dt (api.py:126-133) = cfl_policy.cfl_dt (cfl_policy.py:64-73). */
+int smc_production_dt(smc_handle* h, const double* that_in, int mem,
+                      double safety, double dtmax, double* dt_out);
+
+/* api.march_adaptive (api.py:169-190): CFL-limited march to tstop, the state
+ * staying on the device between steps.  max_steps <= 0 means unbounded. */
+int smc_march_adaptive(smc_handle* h, const double* that_in, double* that_out,
+                       int mem, double tstop, double safety, double dtmax,
+                       long long max_steps, smc_march_info* info);
+
+/* api.march (api.py:147-166): fixed-dt march of nsteps. */
+int smc_march(smc_handle* h, const double* that_in, double* that_out, int mem,
+              double dt, long long nsteps);
+
+/* model.diagnostics(that) (rbc_galerkin.py:439-453). */
+int smc_diagnostics(smc_handle* h, const double* that_in, int mem, smc_diag* out);
+
+/* model.stokes(that) -> (psi, omega) coefficients (rbc_galerkin.py:342,
+ * convection_modes.py:224, coupled_model.py:725). */
+int smc_stokes(smc_handle* h, const double* that_in, int mem, double* psi_out,
+               double* om_out);
+
+/* model.velocity(psi) -> (ux, uz) on the (Nx,Nz) grid (rbc_galerkin.py:355). */
+int smc_velocity(smc_handle* h, const double* psi_in, int mem, double* ux_out,
+                 double* uz_out);
+
+/* RBCVariableViscosity.project_mirror (convection_modes.py:134-153). */
+int smc_project_mirror(smc_handle* h, const double* that_in, double* that_out, int mem);
+
+/* The four transforms of the model (see enum smc_transform). */
+int smc_transform(smc_handle* h, int kind, const double* in, double* out, int mem);
+
+/* RBCCoupled.eta_of (coupled_model.py:401-496): the (Nx,Nz) viscosity the
+ * coupled Stokes operator consumes for `that` (updates the eta counters). */
+int smc_eta_of(smc_handle* h, const double* that_in, int mem, double* eta_out);
+
+/* FreeSchurOperator.matvec (stokes/lagged_stokes.py:202-220) at the viscosity
+ * `eta` (Nx,Nz): out = A(eta) v, v and out (Nk,Nz) complex. */
+int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
+                     double* out, int mem);
+
+/* RBCImplicitTheta.reset_history (implicit_theta.py:601-606). */
+int smc_reset_history(smc_handle* h);
+
+int smc_counters_get(smc_handle* h, smc_counters* out);
+
+/* Sizes of the handle's arrays: Nk, Nx, Nz, Np (= 2 Nx). */
+int smc_shape(smc_handle* h, int* Nk, int* Nx, int* Nz, int* Np);
+
+/* The handle's CUDA stream (cudaStream_t), for callers that order their own
+ * work after the handle's. */
+void* smc_stream(smc_handle* h);
+
+/* Message of the last hard error on the calling thread ("" if none). */
+const char* smc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPECMC_GB300_H */

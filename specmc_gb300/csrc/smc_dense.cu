@@ -1,0 +1,505 @@
+// Dense linear algebra of the FP64 time step.
+//
+//  * Batched small LU (one CTA per matrix, the matrix held in shared memory)
+//    for the per-wavenumber operators of SpecMC: the Chebyshev-tau Helmholtz
+//    operators (rbc_galerkin.py:119-185), the reduced eta(z) Stokes operators
+//    (stokes/vv_stokes.py:298-321) and the BFBT blocks (stokes/bfbt.py:157-191).
+//  * Blocked right-looking complex LU with partial pivoting and the matching
+//    triangular solve for the lagged dense Schur matrix (lagged_stokes.py:
+//    274-300, scipy lu_factor / lu_solve).  The pivot of each column is the
+//    first row of largest |re| + |im|, the choice LAPACK's zgetrf makes.
+//
+// GB300 runs FP64 at a small fraction of its FP32 rate, so every FP64 kernel
+// here spreads its arithmetic over all SMs: the panel factorisation and the
+// triangular solves are single cooperative launches (one CTA per SM) that
+// synchronise the grid between dependent steps, and the trailing update is a
+// tiled GEMM over the whole machine.
+#include <cooperative_groups.h>
+
+#include "smc_internal.cuh"
+#include "smc_schur.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace smc {
+
+// ======================================================== small batched LU
+__global__ void smc_lu_small_kernel(double* __restrict__ A, int* __restrict__ piv,
+                                    int* __restrict__ info, int N) {
+  extern __shared__ double a[];                   // N*N column-major
+  __shared__ double rv[32];
+  __shared__ int ri[32];
+  __shared__ int s_p;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  double* Ag = A + (long long)blockIdx.x * N * N;
+  for (int i = tid; i < N * N; i += nt) a[i] = Ag[i];
+  __syncthreads();
+  int inf = 0;
+  for (int c = 0; c < N; ++c) {
+    // pivot: first row of largest |a[r,c]|, r >= c (idamax)
+    double best = -1.0;
+    int bi = N;
+    for (int r = c + tid; r < N; r += nt) {
+      double v = fabs(a[r + c * N]);
+      if (v > best) { best = v; bi = r; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double ov = __shfl_xor_sync(0xffffffffu, best, o);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    if ((tid & 31) == 0) { rv[tid >> 5] = best; ri[tid >> 5] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      double b = rv[0];
+      int p = ri[0];
+      for (int w = 1; w < (nt >> 5); ++w)
+        if (rv[w] > b || (rv[w] == b && ri[w] < p)) { b = rv[w]; p = ri[w]; }
+      if (p >= N) p = c;
+      s_p = p;
+      piv[(long long)blockIdx.x * N + c] = p;
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p != c)
+      for (int col = tid; col < N; col += nt) {
+        double t = a[c + col * N];
+        a[c + col * N] = a[p + col * N];
+        a[p + col * N] = t;
+      }
+    __syncthreads();
+    const double pv = a[c + c * N];
+    if (pv != 0.0) {
+      const double rinv = 1.0 / pv;
+      for (int r = c + 1 + tid; r < N; r += nt) a[r + c * N] *= rinv;
+    } else if (!inf) {
+      inf = c + 1;
+    }
+    __syncthreads();
+    const int m = N - c - 1;
+    for (int t = tid; t < m * m; t += nt) {
+      int r = c + 1 + t % m, col = c + 1 + t / m;
+      a[r + col * N] -= a[r + c * N] * a[c + col * N];
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < N * N; i += nt) Ag[i] = a[i];
+  if (tid == 0 && info) info[blockIdx.x] = inf;
+}
+
+void lu_small_batched(const Ctx& c, double* A, int* piv, int* info, int N, int count) {
+  size_t smem = (size_t)N * N * sizeof(double);
+  if (smem > 200 * 1024) throw std::runtime_error("lu_small_batched: Nz too large for the shared-memory LU");
+  SMC_CUDA(cudaFuncSetAttribute(smc_lu_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+  smc_lu_small_kernel<<<count, 256, smem, c.s>>>(A, piv, info, N);
+  SMC_LAUNCH_CHECK(c);
+}
+
+// In-place solve of one real LU factor (column-major, LAPACK ipiv) with a
+// complex right-hand side held in shared memory.
+__device__ void lu_real_solve_smem(const double* __restrict__ L, const int* __restrict__ pv,
+                                   double2* xs, int N) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0)
+    for (int i = 0; i < N; ++i) {
+      int p = pv[i];
+      if (p != i) { double2 t = xs[i]; xs[i] = xs[p]; xs[p] = t; }
+    }
+  __syncthreads();
+  for (int c = 0; c < N; ++c) {          // unit lower
+    double2 xc = xs[c];
+    for (int r = c + 1 + tid; r < N; r += nt) {
+      double l = L[r + (long long)c * N];
+      xs[r].x -= l * xc.x;
+      xs[r].y -= l * xc.y;
+    }
+    __syncthreads();
+  }
+  for (int c = N - 1; c >= 0; --c) {     // upper
+    if (tid == 0) {
+      double u = L[c + (long long)c * N];
+      xs[c].x /= u;
+      xs[c].y /= u;
+    }
+    __syncthreads();
+    double2 xc = xs[c];
+    for (int r = tid; r < c; r += nt) {
+      double u = L[r + (long long)c * N];
+      xs[r].x -= u * xc.x;
+      xs[r].y -= u * xc.y;
+    }
+    __syncthreads();
+  }
+}
+
+// x_b = A_b^{-1} (alpha P b_b), complex right-hand side, real LU factor
+__global__ void smc_lu_small_solve_kernel(const double* __restrict__ LU, const int* __restrict__ piv,
+                                          long long lu_stride, const double2* __restrict__ b,
+                                          double2* __restrict__ x, int N, double alpha,
+                                          int zero_tau, const int* __restrict__ skip) {
+  extern __shared__ double2 xs[];
+  const int k = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  double2* xo = x + (long long)k * N;
+  if (skip && skip[k]) {
+    for (int i = tid; i < N; i += nt) xo[i] = make_double2(0.0, 0.0);
+    return;
+  }
+  for (int i = tid; i < N; i += nt) {
+    double2 v = b[(long long)k * N + i];
+    if (zero_tau && i >= N - 2) v = make_double2(0.0, 0.0);
+    xs[i] = make_double2(alpha * v.x, alpha * v.y);
+  }
+  __syncthreads();
+  lu_real_solve_smem(LU + (long long)k * lu_stride, piv + (long long)k * N, xs, N);
+  for (int i = tid; i < N; i += nt) xo[i] = xs[i];
+}
+
+// G_k[:, q] = A_k^{-1} e_q for q < N-2, 0 for the two tau columns
+// (vv_stokes.py:281-296: G = solve(A, P)); one CTA per (k, q)
+__global__ void smc_green_kernel(const double* __restrict__ LU, const int* __restrict__ piv,
+                                 double* __restrict__ G, int N) {
+  extern __shared__ double2 xs[];
+  const int k = blockIdx.x, q = blockIdx.y, tid = threadIdx.x;
+  double* Gk = G + (long long)k * N * N;
+  if (q >= N - 2) {
+    for (int p = tid; p < N; p += blockDim.x) Gk[(long long)p * N + q] = 0.0;
+    return;
+  }
+  for (int i = tid; i < N; i += blockDim.x) xs[i] = make_double2(i == q ? 1.0 : 0.0, 0.0);
+  __syncthreads();
+  lu_real_solve_smem(LU + (long long)k * N * N, piv + (long long)k * N, xs, N);
+  for (int p = tid; p < N; p += blockDim.x) Gk[(long long)p * N + q] = xs[p].x;
+}
+
+void green_from_lu(const Ctx& c, const double* LUcm, const int* piv, double* G, int N, int Nk) {
+  dim3 grd(Nk, N);
+  smc_green_kernel<<<grd, 128, N * sizeof(double2), c.s>>>(LUcm, piv, G, N);
+  SMC_LAUNCH_CHECK(c);
+}
+
+void lu_small_solve(const Ctx& c, const double* LU, const int* piv, long long lu_stride,
+                    const double2* b, double2* x, int N, int count, double alpha, int zero_tau,
+                    const int* skip_mask) {
+  size_t smem = (size_t)N * sizeof(double2);
+  smc_lu_small_solve_kernel<<<count, 128, smem, c.s>>>(LU, piv, lu_stride, b, x, N, alpha,
+                                                       zero_tau, skip_mask);
+  SMC_LAUNCH_CHECK(c);
+}
+
+// ======================================================== dense complex LU
+static constexpr int ZNB = 32;     // panel width
+static constexpr int ZROWCHUNK = 32;
+
+// rows of the column range [r_lo, n) owned by CTA b: chunks of 32 rows dealt
+// round-robin over the grid
+#define SMC_FOR_OWNED_ROWS(r, r_lo, n, b, G)                                   \
+  for (int ch_ = ((r_lo) / ZROWCHUNK + (((b) - ((r_lo) / ZROWCHUNK) % (G)) + (G)) % (G)); \
+       ch_ * ZROWCHUNK < (n); ch_ += (G))                                      \
+    for (int r = max(ch_ * ZROWCHUNK, (r_lo)); r < min((ch_ + 1) * ZROWCHUNK, (n)); ++r)
+
+__device__ __forceinline__ void argmax_merge(double& v, int& i, double ov, int oi) {
+  if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
+}
+
+// Panel factorisation of columns [p0, p0+nbp): cooperative, one CTA per SM.
+__global__ void smc_zlu_panel_kernel(double2* __restrict__ A, int n, int p0, int nbp,
+                                     int* __restrict__ piv, double* __restrict__ part) {
+  cg::grid_group grid = cg::this_grid();
+  const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  __shared__ double rv[32];
+  __shared__ int ri[32];
+  __shared__ int s_p;
+  __shared__ double2 prow[ZNB];
+  for (int c = p0; c < p0 + nbp; ++c) {
+    // A: local argmax of |re|+|im| over owned rows r >= c of column c
+    double best = -1.0;
+    int bi = n;
+    {
+      int t = tid;
+      // flatten owned rows, stride nt
+      int cnt = 0;
+      SMC_FOR_OWNED_ROWS(r, c, n, b, G) {
+        if ((cnt++ % nt) == t) {
+          double v = cabs1(A[r + (long long)c * n]);
+          if (v != v) v = INFINITY;           // NaN wins, like a failed factorisation
+          argmax_merge(best, bi, v, r);
+        }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+      argmax_merge(best, bi, __shfl_xor_sync(0xffffffffu, best, o), __shfl_xor_sync(0xffffffffu, bi, o));
+    if ((tid & 31) == 0) { rv[tid >> 5] = best; ri[tid >> 5] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      double v = rv[0];
+      int i = ri[0];
+      for (int w = 1; w < (nt >> 5); ++w) argmax_merge(v, i, rv[w], ri[w]);
+      part[2 * b] = v;
+      part[2 * b + 1] = (double)i;
+    }
+    grid.sync();
+    // B: global pivot (every CTA), CTA 0 swaps rows c and p inside the panel
+    if (tid == 0) {
+      double v = -1.0;
+      int i = n;
+      for (int g = 0; g < G; ++g) argmax_merge(v, i, part[2 * g], (int)part[2 * g + 1]);
+      if (i >= n) i = c;
+      s_p = i;
+      if (b == 0) piv[c] = i;
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (b == 0 && p != c)
+      for (int col = p0 + tid; col < p0 + nbp; col += nt) {
+        double2 t = A[c + (long long)col * n];
+        A[c + (long long)col * n] = A[p + (long long)col * n];
+        A[p + (long long)col * n] = t;
+      }
+    grid.sync();
+    // C: scale column c below the diagonal, rank-1 update of the panel
+    for (int col = c + tid; col < p0 + nbp; col += nt) prow[col - c] = A[c + (long long)col * n];
+    __syncthreads();
+    const double2 pv = prow[0];
+    const bool nz = (pv.x != 0.0 || pv.y != 0.0);
+    const double2 rinv = nz ? cdiv(make_double2(1.0, 0.0), pv) : make_double2(0.0, 0.0);
+    const int ncols = p0 + nbp - c - 1;
+    int cnt = 0;
+    SMC_FOR_OWNED_ROWS(r, c + 1, n, b, G) {
+      if ((cnt++ % nt) == tid) {
+        double2 l = A[r + (long long)c * n];
+        if (nz) l = cmul(l, rinv);
+        A[r + (long long)c * n] = l;
+        for (int j = 1; j <= ncols; ++j) {
+          double2* e = &A[r + (long long)(c + j) * n];
+          *e = csub(*e, cmul(l, prow[j]));
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// row interchanges of panel [p0, p0+nbp) applied to every column outside it
+__global__ void smc_zlu_laswp_kernel(double2* __restrict__ A, int n, int p0, int nbp,
+                                     const int* __restrict__ piv) {
+  int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= n || (col >= p0 && col < p0 + nbp)) return;
+  double2* Ac = A + (long long)col * n;
+  for (int i = p0; i < p0 + nbp; ++i) {
+    int p = piv[i];
+    if (p != i) { double2 t = Ac[i]; Ac[i] = Ac[p]; Ac[p] = t; }
+  }
+}
+
+// U12 = L11^{-1} A12 (unit lower L11 of the panel), one thread per column
+__global__ void smc_zlu_trsm_kernel(double2* __restrict__ A, int n, int p0, int nbp) {
+  __shared__ double2 L[ZNB * ZNB];
+  for (int t = threadIdx.x; t < nbp * nbp; t += blockDim.x) {
+    int r = t % nbp, c = t / nbp;
+    L[t] = A[(p0 + r) + (long long)(p0 + c) * n];
+  }
+  __syncthreads();
+  int col = p0 + nbp + blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= n) return;
+  double2 x[ZNB];
+  double2* Ac = A + (long long)col * n + p0;
+  for (int i = 0; i < nbp; ++i) x[i] = Ac[i];
+  for (int c = 0; c < nbp; ++c)
+    for (int r = c + 1; r < nbp; ++r) x[r] = csub(x[r], cmul(L[r + c * nbp], x[c]));
+  for (int i = 0; i < nbp; ++i) Ac[i] = x[i];
+}
+
+// A22 -= L21 U12 : 64x64 output tile per CTA, 4x4 complex outputs per thread
+static constexpr int GT = 64;
+__global__ void __launch_bounds__(256) smc_zlu_gemm_kernel(double2* __restrict__ A, int n, int p0, int nbp) {
+  extern __shared__ double2 sm[];
+  double2* Ls = sm;                    // [nbp][GT] : Ls[kk*GT + r]
+  double2* Us = sm + ZNB * GT;         // [nbp][GT] : Us[kk*GT + c]
+  const int r0 = p0 + nbp + blockIdx.y * GT;
+  const int c0 = p0 + nbp + blockIdx.x * GT;
+  const int tid = threadIdx.x;
+  for (int t = tid; t < nbp * GT; t += 256) {
+    int r = t % GT, kk = t / GT;
+    int gr = r0 + r;
+    Ls[kk * GT + r] = (gr < n) ? A[gr + (long long)(p0 + kk) * n] : make_double2(0.0, 0.0);
+  }
+  for (int t = tid; t < nbp * GT; t += 256) {
+    int k2 = t % nbp, cc = t / nbp;
+    int gc = c0 + cc;
+    Us[k2 * GT + cc] = (gc < n) ? A[(p0 + k2) + (long long)gc * n] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  const int tr = (tid % 16) * 4, tc = (tid / 16) * 4;
+  double2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
+  for (int kk = 0; kk < nbp; ++kk) {
+    double2 l[4], u[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) l[i] = Ls[kk * GT + tr + i];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) u[j] = Us[kk * GT + tc + j];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        acc[i][j].x += l[i].x * u[j].x - l[i].y * u[j].y;
+        acc[i][j].y += l[i].x * u[j].y + l[i].y * u[j].x;
+      }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    int gc = c0 + tc + j;
+    if (gc >= n) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int gr = r0 + tr + i;
+      if (gr >= n) continue;
+      double2* e = &A[gr + (long long)gc * n];
+      *e = csub(*e, acc[i][j]);
+    }
+  }
+}
+
+void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work) {
+  const size_t gsm = (size_t)2 * ZNB * GT * sizeof(double2);
+  SMC_CUDA(cudaFuncSetAttribute(smc_zlu_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)gsm));
+  int G = c.num_sms;
+  int maxb = 0;
+  SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, smc_zlu_panel_kernel, 256, 0));
+  if (maxb < 1) throw std::runtime_error("zlu_dense: panel kernel cannot be co-resident");
+  double* part = reinterpret_cast<double*>(work);
+  for (int p0 = 0; p0 < n; p0 += ZNB) {
+    int nbp = std::min(ZNB, n - p0);
+    void* args[] = {&A, &n, &p0, &nbp, &piv, &part};
+    SMC_CUDA(cudaLaunchCooperativeKernel((void*)smc_zlu_panel_kernel, dim3(G), dim3(256), args, 0, c.s));
+    SMC_LAUNCH_CHECK(c);
+    smc_zlu_laswp_kernel<<<ceil_div(n, 128), 128, 0, c.s>>>(A, n, p0, nbp, piv);
+    SMC_LAUNCH_CHECK(c);
+    int rest = n - p0 - nbp;
+    if (rest > 0) {
+      smc_zlu_trsm_kernel<<<ceil_div(rest, 64), 64, 0, c.s>>>(A, n, p0, nbp);
+      SMC_LAUNCH_CHECK(c);
+      dim3 g(ceil_div(rest, GT), ceil_div(rest, GT));
+      smc_zlu_gemm_kernel<<<g, 256, gsm, c.s>>>(A, n, p0, nbp);
+      SMC_LAUNCH_CHECK(c);
+    }
+  }
+}
+
+// ================================================== dense triangular solve
+static constexpr int SB = 64;      // diagonal block of the solve
+
+// x = U^{-1} L^{-1} b[perm]: cooperative, one CTA per SM.  Each CTA solves the
+// current diagonal block redundantly (no grid barrier inside the block) and
+// updates the rows it owns (32-row chunks dealt round-robin).  The forward
+// sweep updates `x` in place and writes solved blocks to `y`; the backward
+// sweep updates `y` in place and writes solved blocks to `x`, so a block is
+// never written while another CTA may still be reading it.
+__device__ __forceinline__ int first_owned_chunk(int row_lo, int b, int G) {
+  int c0 = row_lo / 32;
+  return c0 + ((b - c0 % G) % G + G) % G;
+}
+
+template <bool LOWER>
+__device__ void smc_trsv_block(const double2* __restrict__ LU, double2* __restrict__ work,
+                               double2* __restrict__ dst, int n, int bk, double2* Db, double2* xb,
+                               double2 (*red)[32]) {
+  const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int r0 = bk * SB, r1 = min(n, r0 + SB), m = r1 - r0;
+  for (int t = tid; t < SB * SB; t += 256) {
+    int r = t % SB, cc = t / SB;
+    Db[t] = (r < m && cc < m) ? LU[(r0 + r) + (long long)(r0 + cc) * n]
+                              : make_double2(LOWER ? 0.0 : 1.0, 0.0);
+  }
+  if (tid < SB) xb[tid] = (tid < m) ? work[r0 + tid] : make_double2(0.0, 0.0);
+  __syncthreads();
+  if (warp == 0) {
+    double2 v0 = xb[lane], v1 = xb[lane + 32];
+    if (LOWER) {
+      for (int cc = 0; cc < m; ++cc) {
+        double2 xc = (cc < 32) ? make_double2(__shfl_sync(0xffffffffu, v0.x, cc), __shfl_sync(0xffffffffu, v0.y, cc))
+                               : make_double2(__shfl_sync(0xffffffffu, v1.x, cc - 32), __shfl_sync(0xffffffffu, v1.y, cc - 32));
+        if (lane > cc) v0 = csub(v0, cmul(Db[lane + cc * SB], xc));
+        if (lane + 32 > cc) v1 = csub(v1, cmul(Db[lane + 32 + cc * SB], xc));
+      }
+    } else {
+      for (int cc = m - 1; cc >= 0; --cc) {
+        if (cc < 32) { if (lane == cc) v0 = cdiv(v0, Db[cc + cc * SB]); }
+        else if (lane == cc - 32) v1 = cdiv(v1, Db[cc + cc * SB]);
+        double2 xc = (cc < 32) ? make_double2(__shfl_sync(0xffffffffu, v0.x, cc), __shfl_sync(0xffffffffu, v0.y, cc))
+                               : make_double2(__shfl_sync(0xffffffffu, v1.x, cc - 32), __shfl_sync(0xffffffffu, v1.y, cc - 32));
+        if (lane < cc) v0 = csub(v0, cmul(Db[lane + cc * SB], xc));
+        if (lane + 32 < cc) v1 = csub(v1, cmul(Db[lane + 32 + cc * SB], xc));
+      }
+    }
+    xb[lane] = v0;
+    xb[lane + 32] = v1;
+  }
+  __syncthreads();
+  if (b == bk % G)
+    for (int i = tid; i < m; i += 256) dst[r0 + i] = xb[i];
+  // rows to update: below the block (forward) or above it (backward)
+  const int lo = LOWER ? r1 : 0, hi = LOWER ? n : r0;
+  for (int ch = first_owned_chunk(lo, b, G); ch * 32 < hi; ch += G) {
+    int r = ch * 32 + lane;
+    bool act = (r >= lo && r < hi);
+    double2 acc = make_double2(0.0, 0.0);
+    if (act)
+      for (int cc = warp; cc < m; cc += 8) acc = cadd(acc, cmul(LU[r + (long long)(r0 + cc) * n], xb[cc]));
+    red[warp][lane] = acc;
+    __syncthreads();
+    if (warp == 0 && act) {
+      double2 s = red[0][lane];
+      for (int w = 1; w < 8; ++w) s = cadd(s, red[w][lane]);
+      work[r] = csub(work[r], s);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) smc_zlu_solve_kernel(const double2* __restrict__ LU,
+                                                           const int* __restrict__ perm,
+                                                           const double2* __restrict__ bvec,
+                                                           double2* __restrict__ x,
+                                                           double2* __restrict__ y, int n) {
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ double2 Db[];   // diagonal block (SB x SB, column-major), dynamic
+  __shared__ double2 xb[SB];
+  __shared__ double2 red[8][32];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = bvec[perm[i]];
+  grid.sync();
+  const int nblk = (n + SB - 1) / SB;
+  for (int bk = 0; bk < nblk; ++bk) {
+    smc_trsv_block<true>(LU, x, y, n, bk, Db, xb, red);
+    grid.sync();
+  }
+  for (int bk = nblk - 1; bk >= 0; --bk) {
+    smc_trsv_block<false>(LU, y, x, n, bk, Db, xb, red);
+    grid.sync();
+  }
+}
+
+void zlu_dense_solve(const Ctx& c, const double2* LU, const int* perm, const double2* b,
+                     double2* x, int n, double2* work) {
+  int G = c.num_sms;
+  const size_t dsm = (size_t)SB * SB * sizeof(double2);
+  SMC_CUDA(cudaFuncSetAttribute(smc_zlu_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)dsm));
+  int maxb = 0;
+  SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, smc_zlu_solve_kernel, 256, dsm));
+  if (maxb < 1) throw std::runtime_error("zlu_dense_solve: kernel cannot be co-resident");
+  double2* y = work;
+  void* args[] = {(void*)&LU, (void*)&perm, (void*)&b, (void*)&x, (void*)&y, (void*)&n};
+  SMC_CUDA(cudaLaunchCooperativeKernel((void*)smc_zlu_solve_kernel, dim3(G), dim3(256), args, dsm, c.s));
+  SMC_LAUNCH_CHECK(c);
+}
+
+}  // namespace smc

@@ -1,0 +1,189 @@
+// Internal declarations shared by the translation units of libspecmc_gb300.
+//
+// Layout conventions (device memory):
+//   spectral fields   (Nk, Nz) complex  row-major, double2 / float2 (re, im)
+//   grid fields       (Ng, Nz) real     row-major (x node i, CGL node j)
+//   small operators   (N, N) real       row-major unless a name says "cm"
+//                                       (column-major, used by LU factors)
+//   dense Schur LU    (n, n) complex    column-major, n = Nk * Nz
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+namespace smc {
+
+// ------------------------------------------------------------------ errors
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string& m) : std::runtime_error(m) {}
+};
+
+#define SMC_CUDA(call)                                                        \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess)                                                    \
+      throw ::smc::CudaError(std::string(#call) + ": " +                      \
+                             cudaGetErrorString(e_) + " (" + __FILE__ + ":" + \
+                             std::to_string(__LINE__) + ")");                 \
+  } while (0)
+
+// Launch context: the stream every kernel of a handle goes to, and the
+// launch counter the handle reports.
+struct Ctx {
+  cudaStream_t s = nullptr;
+  long long* nlaunch = nullptr;
+  int num_sms = 152;
+  void count(int n = 1) const { if (nlaunch) *nlaunch += n; }
+};
+
+#define SMC_LAUNCH_CHECK(ctx)                                                 \
+  do {                                                                        \
+    (ctx).count();                                                            \
+    cudaError_t e_ = cudaGetLastError();                                      \
+    if (e_ != cudaSuccess)                                                    \
+      throw ::smc::CudaError(std::string("kernel launch: ") +                 \
+                             cudaGetErrorString(e_) + " (" + __FILE__ + ":" + \
+                             std::to_string(__LINE__) + ")");                 \
+  } while (0)
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// ------------------------------------------------------- complex helpers
+__host__ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ double2 cadd(double2 a, double2 b) {
+  return make_double2(a.x + b.x, a.y + b.y);
+}
+__host__ __device__ __forceinline__ double2 csub(double2 a, double2 b) {
+  return make_double2(a.x - b.x, a.y - b.y);
+}
+__host__ __device__ __forceinline__ double2 cscale(double2 a, double s) {
+  return make_double2(a.x * s, a.y * s);
+}
+__host__ __device__ __forceinline__ double2 cconj(double2 a) {
+  return make_double2(a.x, -a.y);
+}
+// numpy-style complex division (Smith's algorithm is what CPython uses for
+// complex128 true division; the exact formula only matters at roundoff level)
+__host__ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  double ar = fabs(b.x), ai = fabs(b.y);
+  if (ar >= ai) {
+    double r = b.y / b.x, d = b.x + b.y * r;
+    return make_double2((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+  }
+  double r = b.x / b.y, d = b.y + b.x * r;
+  return make_double2((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
+__host__ __device__ __forceinline__ double cabs1(double2 a) {  // |re| + |im|
+  return fabs(a.x) + fabs(a.y);
+}
+
+// per-mode complex factor (cre + i cim) * kx[k]^kpow
+struct KFactor {
+  double cre = 1.0, cim = 0.0;
+  int kpow = 0;
+};
+
+__device__ __forceinline__ double2 kfactor_eval(const KFactor& f, double kx) {
+  double p = 1.0;
+  for (int e = 0; e < f.kpow; ++e) p *= kx;
+  return make_double2(f.cre * p, f.cim * p);
+}
+
+// ============================================================ spectral ops
+// Y_b[k][n] (=|+=) f_b(k) * sum_m Z_b[n][m] X_b[k][m]   (Z real N x N;
+// per-k operator when zstride > 0).  Up to 4 jobs per launch.
+struct ZJob {
+  const double* Z = nullptr;
+  long long zstride = 0;
+  const double2* X = nullptr;
+  double2* Y = nullptr;
+  KFactor f;
+  int accumulate = 0;
+  int x_real = 0;        // use Re(X) only
+  int zero_tau = 0;      // write 0 to columns N-2, N-1 of Y
+};
+void zmat_apply(const Ctx& c, const ZJob* jobs, int njobs, int Nk, int N,
+                const double* kx);
+
+// g_b[i][j] = sum_k w_k Re(X_b[k][j] e^{2 pi i k i / Ng})  (irfft * Ng)
+struct SynthJob {
+  const double2* X = nullptr;
+  double* g = nullptr;
+};
+void synth_x(const Ctx& c, const SynthJob* jobs, int njobs, int Nk, int N,
+             int Ng, const double2* tw);
+
+// A_b[k][j] = scale * sum_i g_b[i][j] e^{-2 pi i k i / Ng},  k < Nk
+struct AnaJob {
+  const double* g = nullptr;
+  double2* A = nullptr;
+};
+void analysis_x(const Ctx& c, const AnaJob* jobs, int njobs, int Nk, int N,
+                int Ng, const double2* tw, double scale);
+
+// elementwise kernels on grids (Ng * N points)
+void grid_explicit_nonlinear(const Ctx& c, const double* ux, const double* uz,
+                             const double* thx, const double* thz, double H,
+                             double* out, long long npts);
+void grid_advect_product(const Ctx& c, const double* ux, const double* uz,
+                         const double* vx, const double* vz, double* out,
+                         long long npts);
+void grid_phi(const Ctx& c, const double* gxx, const double* gzz,
+              const double* gxz, const double* gtr, const double* eta_pad,
+              double coef, double* out_accum, long long npts, int accumulate);
+
+// max|a|, max|b| (nullable b) -> dst[0]
+void reduce_maxabs2(const Ctx& c, const double* a, const double* b, long long n,
+                    double* dst, double* scratch);
+
+// ============================================================ vector ops
+// generic spectral combinations (n complex entries)
+void vec_axpby(const Ctx& c, double2* y, double2 a, const double2* x, double2 b,
+               long long n);                           // y = a x + b y
+void vec_copy(const Ctx& c, double2* y, const double2* x, long long n);
+void vec_zero(const Ctx& c, void* p, long long bytes);
+// out[k][n] = alpha*in[k][n]  with tau columns forced to 0 and row kx==0
+// forced to 0 when zero_k0
+void vec_scaled_modes(const Ctx& c, const double2* in, double2* out, int Nk,
+                      int N, KFactor f, const double* kx, int zero_tau,
+                      int zero_k0);
+// dot / norm reductions (partials in scratch, result at dst)
+void vec_norm2(const Ctx& c, const double2* x, long long n, double* dst,
+               double* scratch);
+// memo signature test of the coupled model: dst = {all_equal, max|X-cX|, max|cX|}
+void memo_compare(const Ctx& c, const double2* that, const double2* cthat,
+                  const double2* X, const double2* cX, long long n, double* dst,
+                  double* scratch);
+
+// ============================================================ dense ops
+// in-place LU with partial pivoting of `count` real N x N matrices
+// (column-major, stride N*N); piv 0-based LAPACK ipiv; info[b] = first zero pivot+1
+void lu_small_batched(const Ctx& c, double* A, int* piv, int* info, int N,
+                      int count);
+// x_b = A_b^{-1} (alpha * P b_b): P zeroes rows N-2, N-1 when zero_tau
+void lu_small_solve(const Ctx& c, const double* LU, const int* piv, long long lu_stride,
+                    const double2* b, double2* x, int N, int count, double alpha,
+                    int zero_tau, const int* skip_mask);
+// dense complex LU (column-major n x n) with partial pivoting (|re|+|im| pivot
+// choice, as LAPACK zgetrf); piv 0-based
+void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work);
+// x = A^{-1} b with a zlu_dense factor; perm = composed row permutation
+void zlu_dense_solve(const Ctx& c, const double2* LU, const int* perm,
+                     const double2* b, double2* x, int n, double2* work);
+
+// ============================================================ Schur ops
+// complex Chebyshev product matrices M_d for d in (-Nk, Nk): Md[(d+Nk-1)] (N x N row-major)
+void build_mult_mats(const Ctx& c, const double2* eta_c, double2* Md, int Nk, int N);
+// out = mult_eta(f) (one-sided convolution + partner half with sign sgn)
+void mult_eta(const Ctx& c, const double2* Md, const double2* f, double2* out,
+              int Nk, int N, double sgn, double2* partial);
+// dense Schur assembly (column-major) from Md, D, D2, G, V
+void assemble_schur(const Ctx& c, const double2* Md, const double* D,
+                    const double* D2, const double* G, const double* V,
+                    const double* kx, double2* A, int Nk, int N, double2* work);
+
+}  // namespace smc

@@ -1,0 +1,1243 @@
+// Native runtime of the GB300 time step: model handles, device buffers, the
+// control flow of the three SpecMC routes and the C ABI of include/specmc_gb300.h.
+//
+// Routes (the recipe each ConvectionConfig is translated into):
+//   const  -> rbc_galerkin.RBC            explicit advection + BE diffusion
+//   eta_z  -> implicit_theta.RBCImplicitTheta   frozen eta(z) Stokes + BDF2 theta
+//   eta_T  -> coupled_model.RBCCoupled    eta(T) coupled Stokes + BDF2 theta
+// Control decisions (FGMRES convergence, defect-correction stopping, refresh
+// triggers, memo hits) are taken on the host from scalars the kernels reduce,
+// exactly where the reference takes them; all vector and matrix work stays
+// on the device, on the handle's stream.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/specmc_gb300.h"
+#include "smc_internal.cuh"
+#include "smc_route.cuh"
+#include "smc_schur.cuh"
+
+namespace smc {
+
+using cplx = std::complex<double>;
+static thread_local std::string g_last_error;
+
+// --------------------------------------------------------------- host basis
+// CGL nodes, Chebyshev Vandermonde (chebvander recurrence), derivative
+// (exact integers), inverse Vandermonde, Clenshaw-Curtis weights
+// (rbc_galerkin.py:63-81, :284-287).
+struct HostBasis {
+  int N = 0;
+  std::vector<double> z, V, Vi, D, D2, wq, VD, VD2, VT;
+
+  static void host_inverse(const std::vector<double>& A, std::vector<double>& Ai, int N) {
+    // Gauss-Jordan with partial pivoting (set-up only)
+    std::vector<double> M(A);
+    Ai.assign((size_t)N * N, 0.0);
+    for (int i = 0; i < N; ++i) Ai[(size_t)i * N + i] = 1.0;
+    for (int c = 0; c < N; ++c) {
+      int p = c;
+      for (int r = c + 1; r < N; ++r)
+        if (std::fabs(M[(size_t)r * N + c]) > std::fabs(M[(size_t)p * N + c])) p = r;
+      if (p != c)
+        for (int q = 0; q < N; ++q) {
+          std::swap(M[(size_t)c * N + q], M[(size_t)p * N + q]);
+          std::swap(Ai[(size_t)c * N + q], Ai[(size_t)p * N + q]);
+        }
+      double piv = M[(size_t)c * N + c];
+      if (piv == 0.0) throw std::runtime_error("singular Chebyshev Vandermonde");
+      for (int q = 0; q < N; ++q) { M[(size_t)c * N + q] /= piv; Ai[(size_t)c * N + q] /= piv; }
+      for (int r = 0; r < N; ++r) {
+        if (r == c) continue;
+        double f = M[(size_t)r * N + c];
+        if (f == 0.0) continue;
+        for (int q = 0; q < N; ++q) {
+          M[(size_t)r * N + q] -= f * M[(size_t)c * N + q];
+          Ai[(size_t)r * N + q] -= f * Ai[(size_t)c * N + q];
+        }
+      }
+    }
+  }
+
+  explicit HostBasis(int N_) : N(N_) {
+    z.resize(N);
+    for (int j = 0; j < N; ++j) z[j] = 0.5 * (1.0 - std::cos(M_PI * j / (N - 1)));
+    V.assign((size_t)N * N, 0.0);
+    for (int j = 0; j < N; ++j) {
+      double x = 2.0 * z[j] - 1.0, x2 = 2.0 * x;
+      V[(size_t)j * N + 0] = 1.0;
+      if (N > 1) V[(size_t)j * N + 1] = x;
+      for (int k = 2; k < N; ++k)
+        V[(size_t)j * N + k] = V[(size_t)j * N + k - 1] * x2 - V[(size_t)j * N + k - 2];
+    }
+    D.assign((size_t)N * N, 0.0);
+    for (int k = 1; k < N; ++k)
+      for (int n = k - 1; n >= 0; n -= 2) D[(size_t)n * N + k] = (n == 0 ? 2.0 : 4.0) * k;
+    auto mm = [&](const std::vector<double>& A, const std::vector<double>& B) {
+      std::vector<double> C((size_t)N * N, 0.0);
+      for (int i = 0; i < N; ++i)
+        for (int k = 0; k < N; ++k) {
+          double a = A[(size_t)i * N + k];
+          if (a == 0.0) continue;
+          for (int j = 0; j < N; ++j) C[(size_t)i * N + j] += a * B[(size_t)k * N + j];
+        }
+      return C;
+    };
+    D2 = mm(D, D);
+    host_inverse(V, Vi, N);
+    std::vector<double> gk(N, 0.0);
+    for (int k = 0; k < N; ++k) gk[k] = (k % 2) ? 0.0 : 1.0 / (1.0 - (double)k * k);
+    gk[0] = 1.0;
+    wq.assign(N, 0.0);
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < N; ++k) wq[j] += Vi[(size_t)k * N + j] * gk[k];
+    VD = mm(V, D);
+    VD2 = mm(V, D2);
+    VT.assign((size_t)N * N, 0.0);
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) VT[(size_t)j * N + i] = V[(size_t)i * N + j];
+  }
+};
+
+// ------------------------------------------------------------ device memory
+struct DevMem {
+  std::vector<void*> ptrs;
+  template <class T>
+  T* alloc(size_t count) {
+    void* p = nullptr;
+    if (count == 0) count = 1;
+    SMC_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    SMC_CUDA(cudaMemset(p, 0, count * sizeof(T)));
+    ptrs.push_back(p);
+    return static_cast<T*>(p);
+  }
+  template <class T>
+  T* upload(const std::vector<T>& h) {
+    T* p = alloc<T>(h.size());
+    SMC_CUDA(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return p;
+  }
+  ~DevMem() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+};
+
+struct LamSlot {
+  double key = 0.0;
+  double* LU = nullptr;
+  int* piv = nullptr;
+  bool used = false;
+};
+
+struct FgmresResult {
+  int info = 1;
+  int iters = 0;
+};
+
+using Op = std::function<void(const double2*, double2*)>;
+
+// =================================================================== Model
+struct Model {
+  smc_config cfg{};
+  int Nx = 0, N = 0, Nk = 0, Np = 0;
+  long long n = 0, NN = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  long long nlaunch = 0;
+  Ctx ctx;
+  DevMem mem;
+  double* hbuf = nullptr;     // pinned scalars
+  smc_counters ctr{};
+
+  std::unique_ptr<HostBasis> hb;
+  std::vector<double> kx_h, x_h;
+  double dzmin = 0.0;
+  // device basis
+  double *dV, *dVi, *dD, *dD2, *dVD, *dVD2, *dVT, *dz, *dkx, *dwq;
+  double2 *dtwNx, *dtwNp;
+  int* dSkipK0;
+  double *dLU0 = nullptr;   // tau lam = 0 (column-major)
+  int* dPiv0 = nullptr;
+  double* dG = nullptr;     // Green operators (row-major)
+  LamSlot lam_slots[4];
+  int lam_next = 0;
+  // reduced operator (eta_z Stokes / BFBT blocks)
+  double *dRedLU = nullptr;
+  int* dRedPiv = nullptr;
+  double *dM0, *dDM0, *dT1, *dT2, *dT3, *dComm, *dCommG, *dPcm;
+  double* dMpLU = nullptr;
+  int* dMpPiv = nullptr;
+  // viscosity
+  EtaLaw law;
+  double *dEta = nullptr, *dEtaLag = nullptr, *dLastEta = nullptr, *dEtaP = nullptr,
+         *dEtaPadZ = nullptr, *dZeroGrid = nullptr;
+  double2 *dEtaC = nullptr, *dMd = nullptr, *dAsmWork = nullptr;
+  double2* dSchur = nullptr;
+  int *dSchurPiv = nullptr, *dSchurPerm = nullptr;
+  bool have_lag = false;
+  int n_since_refresh = 0;
+  bool last_failed = false;
+  // memo
+  double2 *dMemoThat, *dMemoX, *dMemoPsi, *dMemoOm;
+  bool memo_valid = false;
+  // history
+  double2 *dPrev, *dPsiPrev, *dPsiN;
+  bool have_prev = false;
+  double dt_prev = 0.0;
+  double a0 = 1.0, b0 = 1.0, b1 = 0.0;
+  // state and spectral work buffers
+  double2 *dIn, *dOut, *dS0, *dS1, *dTh1, *dTh2, *dPsi, *dOm, *dPsiStar, *dRhs, *dPhi;
+  double2* sp[16];
+  double* gr[10];
+  double *dRed, *dScal;
+  // Krylov
+  int mmax = 0;
+  double2 *dKV, *dKZ, *dKw, *dKx, *dKr, *dKh, *dKy, *dKb;
+  // Schur defect work
+  double2 *dSb, *dSx, *dSr, *dSdx, *dSAx, *dSw, *dSf2, *dSf3, *dSf4, *dSt[4], *dSolveWork;
+  double2 *dBfbtRhs, *dBfbtProfC;
+  double* dBfbtHw;
+
+  // ------------------------------------------------------------ utilities
+  void sync_read(const double* d, int count) {
+    SMC_CUDA(cudaMemcpyAsync(hbuf, d, count * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SMC_CUDA(cudaStreamSynchronize(stream));
+  }
+  double norm(const double2* x) {
+    vec_norm2(ctx, x, n, dScal, dRed);
+    sync_read(dScal, 1);
+    return hbuf[0];
+  }
+
+  // --------------------------------------------------------- transforms
+  // values per mode X = f(k) * Zop @ cf, then x-synthesis on Ng points
+  void synth(const double2* cf, const double* Zop, KFactor f, double* g, int Ng, double2* tmp) {
+    ZJob j;
+    j.Z = Zop; j.X = cf; j.Y = tmp; j.f = f;
+    zmat_apply(ctx, &j, 1, Nk, N, dkx);
+    SynthJob s{tmp, g};
+    synth_x(ctx, &s, 1, Nk, N, Ng, Ng == Np ? dtwNp : dtwNx);
+  }
+  // grid (Ng) -> coefficients: Vi @ (rfft(g)/Ng)[:Nk]
+  void analyze(const double* g, int Ng, double2* out, double2* tmp, KFactor f = KFactor(),
+               int zero_tau = 0) {
+    AnaJob a{g, tmp};
+    analysis_x(ctx, &a, 1, Nk, N, Ng, Ng == Np ? dtwNp : dtwNx, 1.0 / Ng);
+    ZJob j;
+    j.Z = dVi; j.X = tmp; j.Y = out; j.f = f; j.zero_tau = zero_tau;
+    zmat_apply(ctx, &j, 1, Nk, N, dkx);
+  }
+  void zop(const double* Z, long long zs, const double2* X, double2* Y, KFactor f = KFactor(),
+           int x_real = 0, int accumulate = 0) {
+    ZJob j;
+    j.Z = Z; j.zstride = zs; j.X = X; j.Y = Y; j.f = f; j.x_real = x_real; j.accumulate = accumulate;
+    zmat_apply(ctx, &j, 1, Nk, N, dkx);
+  }
+
+  // ------------------------------------------------------- LU lam cache
+  // ChebTau factors keyed by round(lam, 10), at most 4 lam values
+  // (rbc_galerkin.py:102,119-144)
+  LamSlot& lam_lu(double lam) {
+    double key = std::round(lam * 1e10) / 1e10;
+    for (auto& s : lam_slots)
+      if (s.used && s.key == key) return s;
+    int used = 0;
+    for (auto& s : lam_slots) used += s.used;
+    if (used >= 4)
+      for (auto& s : lam_slots) s.used = false;
+    LamSlot* slot = nullptr;
+    for (auto& s : lam_slots)
+      if (!s.used) { slot = &s; break; }
+    tau_ops(ctx, dD2, dkx, lam, slot->LU, N, Nk);
+    lu_small_batched(ctx, slot->LU, slot->piv, nullptr, N, Nk);
+    slot->key = key;
+    slot->used = true;
+    return *slot;
+  }
+
+  // ---------------------------------------------------------------- set-up
+  void setup() {
+    Nx = cfg.Nx; N = cfg.Nz; Nk = Nx / 2 + 1; Np = 2 * Nx;
+    n = (long long)Nk * N; NN = (long long)N * N;
+    SMC_CUDA(cudaSetDevice(cfg.device));
+    device = cfg.device;
+    SMC_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    int sms = 0;
+    SMC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    ctx.s = stream; ctx.nlaunch = &nlaunch; ctx.num_sms = sms;
+    SMC_CUDA(cudaMallocHost(&hbuf, 4096 * sizeof(double)));
+    if (N < 4 || Nx < 4) throw std::runtime_error("Nx and Nz must be >= 4");
+    if ((size_t)N * N * sizeof(double) > 200 * 1024)
+      throw std::runtime_error("Nz > 160 needs the global-memory small LU (not built)");
+
+    hb.reset(new HostBasis(N));
+    kx_h.resize(Nk);
+    // 2 pi * rfftfreq(Nx, d=Lx/Nx) = 2 pi * (k * (1 / (Nx * (Lx/Nx))))
+    const double fval = 1.0 / ((double)Nx * (cfg.Lx / Nx));
+    for (int k = 0; k < Nk; ++k) kx_h[k] = (2.0 * M_PI) * ((double)k * fval);
+    x_h.resize(Nx);
+    for (int i = 0; i < Nx; ++i) x_h[i] = i * cfg.Lx / Nx;
+    dzmin = INFINITY;
+    for (int j = 0; j + 1 < N; ++j) dzmin = std::min(dzmin, hb->z[j + 1] - hb->z[j]);
+
+    dV = mem.upload(hb->V); dVi = mem.upload(hb->Vi); dD = mem.upload(hb->D);
+    dD2 = mem.upload(hb->D2); dVD = mem.upload(hb->VD); dVD2 = mem.upload(hb->VD2);
+    dVT = mem.upload(hb->VT); dz = mem.upload(hb->z); dkx = mem.upload(kx_h);
+    dwq = mem.upload(hb->wq);
+    auto twiddles = [&](int Ng) {
+      std::vector<double2> t(Ng);
+      for (int m = 0; m < Ng; ++m) {
+        long double a = 2.0L * (long double)M_PI * m / Ng;
+        t[m] = make_double2((double)cosl(a), (double)sinl(a));
+      }
+      t[0] = make_double2(1.0, 0.0);
+      if (Ng % 2 == 0) t[Ng / 2] = make_double2(-1.0, 0.0);
+      if (Ng % 4 == 0) { t[Ng / 4] = make_double2(0.0, 1.0); t[3 * Ng / 4] = make_double2(0.0, -1.0); }
+      return t;
+    };
+    dtwNx = mem.upload(twiddles(Nx));
+    dtwNp = mem.upload(twiddles(Np));
+    std::vector<int> skip(Nk, 0);
+    for (int k = 0; k < Nk; ++k) skip[k] = (kx_h[k] == 0.0);
+    dSkipK0 = mem.upload(skip);
+
+    for (auto& s : lam_slots) { s.LU = mem.alloc<double>(Nk * NN); s.piv = mem.alloc<int>(Nk * N); }
+    dLU0 = mem.alloc<double>(Nk * NN);
+    dPiv0 = mem.alloc<int>(Nk * N);
+    dG = mem.alloc<double>(Nk * NN);
+
+    dIn = mem.alloc<double2>(n); dOut = mem.alloc<double2>(n);
+    dS0 = mem.alloc<double2>(n); dS1 = mem.alloc<double2>(n);
+    dTh1 = mem.alloc<double2>(n); dTh2 = mem.alloc<double2>(n);
+    dPsi = mem.alloc<double2>(n); dOm = mem.alloc<double2>(n);
+    dPsiStar = mem.alloc<double2>(n); dRhs = mem.alloc<double2>(n); dPhi = mem.alloc<double2>(n);
+    for (auto& p : sp) p = mem.alloc<double2>(n);
+    for (auto& p : gr) p = mem.alloc<double>((size_t)Np * N);
+    dRed = mem.alloc<double>(4096);
+    dScal = mem.alloc<double>(64);
+    dPrev = mem.alloc<double2>(n); dPsiPrev = mem.alloc<double2>(n); dPsiN = mem.alloc<double2>(n);
+    dMemoThat = mem.alloc<double2>(n); dMemoX = mem.alloc<double2>(n);
+    dMemoPsi = mem.alloc<double2>(n); dMemoOm = mem.alloc<double2>(n);
+    dZeroGrid = mem.alloc<double>((size_t)Np * N);
+
+    // Stokes/Green factors at lam = 0 (every model factorises them at build)
+    tau_ops(ctx, dD2, dkx, 0.0, dLU0, N, Nk);
+    lu_small_batched(ctx, dLU0, dPiv0, nullptr, N, Nk);
+    green_from_lu(ctx, dLU0, dPiv0, dG, N, Nk);
+
+    law.L = std::log(cfg.deta_T);
+    law.Ts = cfg.model == SMC_MODEL_ETA_T ? cfg.arrhenius_Ts : 0.0;
+    law.lo = cfg.eta_min; law.hi = cfg.eta_max;
+    law.lo_eff = cfg.eta_min * (1.0 - 1e-12);
+    law.hi_eff = cfg.eta_max * (1.0 + 1e-12);
+    law.w = cfg.eta_smooth;
+    law.ylo = std::log(cfg.eta_min); law.yhi = std::log(cfg.eta_max);
+
+    if (cfg.model != SMC_MODEL_CONST) {
+      mmax = std::max(cfg.theta_restart, cfg.stokes_restart);
+      dKV = mem.alloc<double2>((size_t)(mmax + 1) * n);
+      dKZ = mem.alloc<double2>((size_t)mmax * n);
+      dKw = mem.alloc<double2>(n); dKx = mem.alloc<double2>(n); dKr = mem.alloc<double2>(n);
+      dKb = mem.alloc<double2>(n);
+      dKh = mem.alloc<double2>(mmax + 2); dKy = mem.alloc<double2>(mmax + 2);
+      dRedLU = mem.alloc<double>(Nk * NN); dRedPiv = mem.alloc<int>(Nk * N);
+      dM0 = mem.alloc<double>(NN); dDM0 = mem.alloc<double>(NN);
+      dT1 = mem.alloc<double>(NN); dT2 = mem.alloc<double>(NN); dT3 = mem.alloc<double>(NN);
+      dComm = mem.alloc<double>(NN); dCommG = mem.alloc<double>(Nk * NN);
+      dPcm = mem.alloc<double>(Nk * NN);
+      // frozen eta(z) of the depth-only base (convection_modes.py:96-107)
+      double* dEz = mem.alloc<double>(N);
+      EtaLaw lz = law;
+      lz.Ts = 0.0;
+      eta_law(ctx, dZeroGrid, dz, N, N, lz, dEz, dScal, dRed);
+      sync_read(dScal, 6);
+      double clip = hbuf[4], band = hbuf[5];
+      if (law.w > 0.0) { ctr.n_clip_eta = (long long)clip; ctr.n_smooth_eta = (long long)band; }
+      else if (clip > 0) { eta_window(ctx, dEz, N, lz, 0, dScal, dRed); ctr.n_clip_eta = (long long)clip; }
+      // tiled (Nx, N) eta(z) and its padded re-synthesis (dissipation source)
+      dEtaPadZ = mem.alloc<double>((size_t)Np * N);
+      {
+        std::vector<double> ez(N);
+        SMC_CUDA(cudaMemcpy(ez.data(), dEz, N * sizeof(double), cudaMemcpyDeviceToHost));
+        std::vector<double> tiled((size_t)Nx * N);
+        for (int i = 0; i < Nx; ++i)
+          for (int j = 0; j < N; ++j) tiled[(size_t)i * N + j] = ez[j];
+        double* dTiled = mem.upload(tiled);
+        eta_pad_from_grid(dTiled, dEtaPadZ);
+      }
+      if (cfg.model == SMC_MODEL_ETA_Z) {
+        // eta_c = Vi @ eta_grid, reduced operator LU per k (vv_stokes.py:240-279)
+        double2* dEzc = mem.alloc<double2>(N);
+        double2* dEzIn = mem.alloc<double2>(N);
+        {
+          std::vector<double> ez(N);
+          SMC_CUDA(cudaMemcpy(ez.data(), dEz, N * sizeof(double), cudaMemcpyDeviceToHost));
+          std::vector<double2> ec(N);
+          for (int j = 0; j < N; ++j) ec[j] = make_double2(ez[j], 0.0);
+          SMC_CUDA(cudaMemcpy(dEzIn, ec.data(), N * sizeof(double2), cudaMemcpyHostToDevice));
+        }
+        ZJob j; j.Z = dVi; j.X = dEzIn; j.Y = dEzc;
+        zmat_apply(ctx, &j, 1, 1, N, dkx);
+        build_reduced_lu(dEzc, dRedLU, dRedPiv);
+      } else {
+        // coupled: eta fields, Schur storage, assembly workspace
+        dEta = mem.alloc<double>((size_t)Nx * N);
+        dEtaLag = mem.alloc<double>((size_t)Nx * N);
+        dLastEta = mem.alloc<double>((size_t)Nx * N);
+        dEtaP = mem.alloc<double>((size_t)Np * N);
+        dEtaC = mem.alloc<double2>(n);
+        dMd = mem.alloc<double2>((size_t)(2 * Nk - 1) * NN);
+        dAsmWork = mem.alloc<double2>((size_t)4 * (2 * Nk - 1) * NN);
+        dSchur = mem.alloc<double2>((size_t)n * n);
+        dSchurPiv = mem.alloc<int>(n);
+        dSchurPerm = mem.alloc<int>(n);
+        dSb = mem.alloc<double2>(n); dSx = mem.alloc<double2>(n); dSr = mem.alloc<double2>(n);
+        dSdx = mem.alloc<double2>(n); dSAx = mem.alloc<double2>(n); dSw = mem.alloc<double2>(n);
+        dSf2 = mem.alloc<double2>(n); dSf3 = mem.alloc<double2>(n); dSf4 = mem.alloc<double2>(n);
+        for (auto& p : dSt) p = mem.alloc<double2>(n);
+        dSolveWork = mem.alloc<double2>(n);
+        dBfbtHw = mem.alloc<double>(2 * N);
+        dBfbtRhs = mem.alloc<double2>(N);
+        dBfbtProfC = mem.alloc<double2>(N);
+        // Galerkin mass matrix V^T W V and its LU (stokes/bfbt.py:74-84)
+        std::vector<double> Mp(NN, 0.0);
+        for (int a = 0; a < N; ++a)
+          for (int b = 0; b < N; ++b) {
+            double s = 0;
+            for (int j = 0; j < N; ++j) s += hb->V[(size_t)j * N + a] * hb->wq[j] * hb->V[(size_t)j * N + b];
+            Mp[(size_t)b * N + a] = s;   // column-major
+          }
+        dMpLU = mem.upload(Mp);
+        dMpPiv = mem.alloc<int>(N);
+        lu_small_batched(ctx, dMpLU, dMpPiv, nullptr, N, 1);
+      }
+    }
+    SMC_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  // reduced operator LU from real Chebyshev coefficients `coef` (complex
+  // storage, imaginary part ignored): P_k = (D2 - k^2) M + 2 k^2 [D,[D,M]] G_k
+  void build_reduced_lu(const double2* coef, double* LU, int* piv) {
+    // extract the real coefficient vector into dT3 (scratch), then M0
+    realpart(coef, dT3, N);
+    cheb_mult_real(ctx, dT3, dM0, N);
+    bgemm(ctx, false, dD2, 0, false, dM0, 0, dDM0, 0, N, 1, 1.0);   // D2 M
+    bgemm(ctx, false, dM0, 0, false, dD, 0, dT1, 0, N, 1, 1.0);     // M D
+    bgemm(ctx, false, dD, 0, false, dT1, 0, dT2, 0, N, 1, 1.0);     // D M D
+    bgemm(ctx, false, dM0, 0, false, dD2, 0, dT3, 0, N, 1, 1.0);    // M D2
+    comm_combine(dDM0, dT2, dT3, dComm, (long long)NN);              // D2M - 2DMD + MD2
+    bgemm(ctx, false, dComm, 0, false, dG, NN, dCommG, NN, N, Nk, 1.0);
+    reduced_blocks(ctx, dDM0, dM0, dCommG, dV, dkx, dPcm, N, Nk);
+    SMC_CUDA(cudaMemcpyAsync(LU, dPcm, sizeof(double) * Nk * NN, cudaMemcpyDeviceToDevice, stream));
+    lu_small_batched(ctx, LU, piv, nullptr, N, Nk);
+  }
+
+  void realpart(const double2* in, double* out, int count);
+  void comm_combine(const double* a, const double* b, const double* c, double* out, long long cnt);
+
+  // padded re-synthesis of a (Nx, N) viscosity grid: G(coeffs(eta))
+  // (physics/dissipation.py:359-362)
+  void eta_pad_from_grid(const double* eta_grid, double* out) {
+    analyze(eta_grid, Nx, sp[14], sp[15]);
+    synth(sp[14], dV, KFactor(), out, Np, sp[15]);
+  }
+
+  // ------------------------------------------------------ stokes routes
+  void stokes_const(const double2* th, double2* psi, double2* om) {
+    KFactor f; f.cre = 0.0; f.cim = -cfg.Ra; f.kpow = 1;      // -i k Ra theta
+    vec_scaled_modes(ctx, th, sp[0], Nk, N, f, dkx, 0, 1);
+    lu_small_solve(ctx, dLU0, dPiv0, NN, sp[0], om, N, Nk, 1.0, 1, dSkipK0);
+    lu_small_solve(ctx, dLU0, dPiv0, NN, om, psi, N, Nk, -1.0, 1, dSkipK0);
+    ctr.n_stokes++;
+  }
+
+  void stokes_etaz(const double2* th, double2* psi, double2* om) {
+    KFactor f; f.cre = 0.0; f.cim = cfg.Ra; f.kpow = 1;       // i k Ra theta
+    vec_scaled_modes(ctx, th, sp[0], Nk, N, f, dkx, 1, 1);
+    lu_small_solve(ctx, dRedLU, dRedPiv, NN, sp[0], sp[1], N, Nk, 1.0, 1, dSkipK0);
+    zop(dG, NN, sp[1], psi);
+    vec_axpby(ctx, om, make_double2(-1.0, 0.0), sp[1], make_double2(0.0, 0.0), n);
+    ctr.n_stokes++;
+  }
+
+  // eta_of (coupled_model.py:401-496) -> dEta (Nx, N)
+  void eta_of(const double2* th) {
+    synth(th, dV, KFactor(), gr[0], Np, sp[0]);              // theta on 2 Nx points
+    eta_law(ctx, gr[0], dz, N, (long long)Np * N, law, dEtaP, dScal, dRed);
+    sync_read(dScal, 6);
+    double tmin = hbuf[0], tmax = hbuf[1];
+    ctr.max_T_excursion = std::max(ctr.max_T_excursion, std::max(std::max(0.0 - tmin, tmax - 1.0), 0.0));
+    ctr.n_T_out_of_range += (long long)hbuf[2];
+    ctr.n_clip_T += (long long)hbuf[3];
+    if (law.w > 0.0) {
+      ctr.n_clip_eta += (long long)hbuf[4];
+      ctr.n_smooth_eta += (long long)hbuf[5];
+    } else if (hbuf[4] > 0.0) {
+      eta_window(ctx, dEtaP, (long long)Np * N, law, 0, dScal + 8, dRed);
+      ctr.n_clip_eta += (long long)hbuf[4];
+    }
+    AnaJob a{dEtaP, sp[1]};
+    analysis_x(ctx, &a, 1, Nk, N, Np, dtwNp, 1.0 / Np);
+    SynthJob s{sp[1], dEta};
+    synth_x(ctx, &s, 1, Nk, N, Nx, dtwNx);
+    min_and_drift(ctx, dEta, nullptr, (long long)Nx * N, dScal, dRed);
+    sync_read(dScal, 1);
+    if (!(hbuf[0] > 0.0)) {
+      // positivity guard (coupled_model.py:451-496)
+      eta_window(ctx, dEta, (long long)Nx * N, law, 1, dScal, dRed);
+      sync_read(dScal, 2);
+      double c = hbuf[0];
+      if (law.w > 0.0) {
+        eta_window(ctx, dEta, (long long)Nx * N, law, 0, dScal, dRed);
+        sync_read(dScal, 2);
+        ctr.n_clip_eta_proj += (long long)c;
+        ctr.n_smooth_eta_proj += (long long)hbuf[1];
+      } else if (c > 0) {
+        eta_window(ctx, dEta, (long long)Nx * N, law, 0, dScal, dRed);
+        ctr.n_clip_eta_proj += (long long)c;
+      }
+    }
+  }
+
+  // Md from the current dEta: eta_c = coeffs(eta)
+  void eta_operator() {
+    analyze(dEta, Nx, dEtaC, sp[2]);
+    build_mult_mats(ctx, dEtaC, dMd, Nk, N);
+  }
+
+  // FreeSchurOperator.matvec at the current Md (lagged_stokes.py:202-220)
+  void schur_matvec(const double2* v, double2* out) {
+    zop(dG, NN, v, dSw);                                   // w = G v
+    KFactor f2; f2.cre = 2.0; f2.kpow = 2;                  // 2 k^2 w
+    vec_scaled_modes(ctx, dSw, dSf2, Nk, N, f2, dkx, 0, 0);
+    zop(dD2, 0, dSw, dSf3);                                // D2 w
+    KFactor f4; f4.kpow = 1;                                // k (D w)
+    zop(dD, 0, dSw, dSf4, f4);
+    smc::mult_eta(ctx, dMd, v, dSt[0], Nk, N, -1.0, nullptr);
+    smc::mult_eta(ctx, dMd, dSf2, dSt[1], Nk, N, -1.0, nullptr);
+    smc::mult_eta(ctx, dMd, dSf3, dSt[2], Nk, N, -1.0, nullptr);
+    smc::mult_eta(ctx, dMd, dSf4, dSt[3], Nk, N, +1.0, nullptr);
+    schur_combine(ctx, dSt[0], dSt[1], dSt[2], dSt[3], v, dD, dD2, dV, dkx, out, Nk, N);
+  }
+
+  void rhs_schur(const double2* th, double2* b) {
+    KFactor f; f.cre = 0.0; f.cim = cfg.Ra; f.kpow = 1;
+    vec_scaled_modes(ctx, th, b, Nk, N, f, dkx, 1, 1);
+  }
+
+  void refresh() {
+    assemble_schur(ctx, dMd, dD, dD2, dG, dV, dkx, dSchur, Nk, N, dAsmWork);
+    zlu_dense(ctx, dSchur, dSchurPiv, (int)n, dAsmWork);
+    std::vector<int> piv(n), perm(n);
+    SMC_CUDA(cudaMemcpyAsync(piv.data(), dSchurPiv, n * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    SMC_CUDA(cudaStreamSynchronize(stream));
+    for (long long i = 0; i < n; ++i) perm[i] = (int)i;
+    for (long long i = 0; i < n; ++i) std::swap(perm[i], perm[piv[i]]);
+    SMC_CUDA(cudaMemcpyAsync(dSchurPerm, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice, stream));
+    SMC_CUDA(cudaMemcpyAsync(dEtaLag, dEta, sizeof(double) * Nx * N, cudaMemcpyDeviceToDevice, stream));
+    SMC_CUDA(cudaStreamSynchronize(stream));
+    have_lag = true;
+    n_since_refresh = 0;
+    ctr.n_refresh++;
+  }
+
+  void lag_solve(const double2* b, double2* x) {
+    zlu_dense_solve(ctx, dSchur, dSchurPerm, b, x, (int)n, dSolveWork);
+  }
+
+  // coupled_model.py:524-573
+  void defect_solve(const double2* th, double2* x) {
+    rhs_schur(th, dSb);
+    lag_solve(dSb, x);
+    double xn = std::max(norm(x), 1e-300);
+    const bool adaptive = cfg.defect_tol > 0.0;
+    const int kmax = adaptive ? cfg.max_K : cfg.K;
+    int kdone = 0;
+    double c = 0.0;
+    for (int it = 0; it < kmax; ++it) {
+      schur_matvec(x, dSAx);
+      vec_axpby(ctx, dSAx, make_double2(1.0, 0.0), dSb, make_double2(-1.0, 0.0), n);  // r = b - Ax
+      lag_solve(dSAx, dSdx);
+      c = norm(dSdx) / xn;
+      vec_axpby(ctx, x, make_double2(1.0, 0.0), dSdx, make_double2(1.0, 0.0), n);     // x += dx
+      ++kdone;
+      if (adaptive && c <= cfg.defect_tol) break;
+    }
+    // final residual of the accepted iterate (reported, as the reference does)
+    schur_matvec(x, dSAx);
+    vec_axpby(ctx, dSAx, make_double2(1.0, 0.0), dSb, make_double2(-1.0, 0.0), n);
+    double bn = std::max(norm(dSb), 1e-300);
+    ctr_last_defect_res = norm(dSAx) / bn;
+    ctr.last_K = kdone;
+    ctr.last_corr = kdone ? c : 0.0;
+    ctr.n_defect++;
+    if (!adaptive) last_failed = false;
+    else {
+      last_failed = !std::isfinite(ctr.last_corr) || ctr.last_corr > cfg.defect_tol;
+      if (last_failed) ctr.n_defect_failed++;
+    }
+  }
+  double ctr_last_defect_res = 0.0;
+
+  void legacy_solve(const double2* th, double2* x) {
+    double drift = INFINITY;
+    if (have_lag) {
+      min_and_drift(ctx, dEta, dEtaLag, (long long)Nx * N, dScal, dRed);
+      sync_read(dScal, 2);
+      drift = hbuf[1];
+    }
+    if (!have_lag || n_since_refresh >= cfg.lag || drift > cfg.eta_drift_tol) refresh();
+    n_since_refresh++;
+    defect_solve(th, x);
+    if (last_failed) {
+      refresh();
+      n_since_refresh++;
+      defect_solve(th, x);
+      if (last_failed) ctr.n_defect_double_fail++;
+    }
+  }
+
+  // spectral BFBT blocks from the harmonic-mean profile (stokes/bfbt.py:111-191)
+  void bfbt_build() {
+    harm_profile_rhs(ctx, dEta, Nx, N, dwq, dBfbtHw);
+    to_complex(dBfbtHw, dBfbtRhs, N);
+    ZJob j; j.Z = dVT; j.X = dBfbtRhs; j.Y = dBfbtProfC;     // V^T (w g)
+    zmat_apply(ctx, &j, 1, 1, N, dkx);
+    lu_small_solve(ctx, dMpLU, dMpPiv, NN, dBfbtProfC, dBfbtRhs, N, 1, 1.0, 0, nullptr);
+    build_reduced_lu(dBfbtRhs, dRedLU, dRedPiv);
+  }
+  void to_complex(const double* in, double2* out, int count);
+
+  double schur_true_res(const double2* b, const double2* x) {
+    schur_matvec(x, dSAx);
+    vec_axpby(ctx, dSAx, make_double2(1.0, 0.0), b, make_double2(-1.0, 0.0), n);
+    double bn = std::max(norm(b), 1e-300);
+    return norm(dSAx) / bn;
+  }
+
+  void bfbt_solve(const double2* th, double2* x) {
+    rhs_schur(th, dSb);
+    bfbt_build();
+    Op A = [&](const double2* v, double2* o) { schur_matvec(v, o); };
+    Op M = [&](const double2* r, double2* z) {
+      lu_small_solve(ctx, dRedLU, dRedPiv, NN, r, z, N, Nk, 1.0, 1, nullptr);
+    };
+    FgmresResult fr = fgmres(A, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
+    ctr.n_bfbt_solves++;
+    ctr.n_bfbt_iters += fr.iters;
+    double res = schur_true_res(dSb, x);
+    ctr.last_bfbt_true_res = res;
+    ctr.last_K = 0;
+    if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
+      // rescue chain (coupled_model.py:613-654)
+      ctr.n_bfbt_rescue++;
+      refresh();
+      defect_solve(th, x);
+      if (last_failed) {
+        refresh();
+        defect_solve(th, x);
+        if (last_failed) ctr.n_defect_double_fail++;
+      }
+      res = schur_true_res(dSb, x);
+      if (!(res <= cfg.stokes_rtol || !std::isfinite(res))) {
+        if ((long long)Nk * N > 4096) ctr.n_bfbt_rescue_weak++;
+        else {
+          // the dense direct solve at this eta: the factor just refreshed
+          // is exactly the LU of the assembled A(eta)
+          lag_solve(dSb, x);
+          ctr.n_bfbt_rescue_direct++;
+        }
+      }
+    }
+  }
+
+  void stokes_coupled(const double2* th, double2* psi, double2* om) {
+    eta_of(th);
+    SMC_CUDA(cudaMemcpyAsync(dLastEta, dEta, sizeof(double) * Nx * N, cudaMemcpyDeviceToDevice, stream));
+    have_last_eta = true;
+    eta_operator();
+    if (cfg.precond == SMC_PRECOND_BFBT) bfbt_solve(th, dSx);
+    else legacy_solve(th, dSx);
+    zop(dG, NN, dSx, psi);
+    vec_axpby(ctx, om, make_double2(-1.0, 0.0), dSx, make_double2(0.0, 0.0), n);
+  }
+  bool have_last_eta = false;
+
+  // memoised Stokes solve of the coupled model (coupled_model.py:725-765)
+  void stokes_memo(const double2* th, double2* psi, double2* om) {
+    zop(dV, 0, th, sp[3]);
+    if (memo_valid) {
+      memo_compare(ctx, th, dMemoThat, sp[3], dMemoX, n, dScal, dRed);
+      sync_read(dScal, 3);
+      bool eq = hbuf[0] != 0.0;
+      double den = std::max(hbuf[2], 1e-300);
+      if (eq || hbuf[1] <= 1e-12 * den) {
+        if (!eq) ctr.n_memo_hits++;
+        vec_copy(ctx, psi, dMemoPsi, n);
+        vec_copy(ctx, om, dMemoOm, n);
+        return;
+      }
+    }
+    stokes_coupled(th, dMemoPsi, dMemoOm);
+    ctr.n_stokes++;
+    vec_copy(ctx, dMemoThat, th, n);
+    vec_copy(ctx, dMemoX, sp[3], n);
+    memo_valid = true;
+    vec_copy(ctx, psi, dMemoPsi, n);
+    vec_copy(ctx, om, dMemoOm, n);
+  }
+
+  void stokes(const double2* th, double2* psi, double2* om) {
+    if (cfg.model == SMC_MODEL_CONST) stokes_const(th, psi, om);
+    else if (cfg.model == SMC_MODEL_ETA_Z) stokes_etaz(th, psi, om);
+    else stokes_memo(th, psi, om);
+  }
+
+  void velocity(const double2* psi, double* ux, double* uz) {
+    synth(psi, dVD, KFactor(), ux, Nx, sp[4]);
+    KFactor f; f.cre = 0.0; f.cim = -1.0; f.kpow = 1;       // -i k psi
+    synth(psi, dV, f, uz, Nx, sp[4]);
+  }
+
+  double cfl_dt(const double2* th, double safety, double dtmax, double dtmin) {
+    stokes(th, dPsi, dOm);
+    velocity(dPsi, gr[0], gr[1]);
+    reduce_maxabs2(ctx, gr[0], gr[1], (long long)Nx * N, dScal, dRed);
+    sync_read(dScal, 1);
+    double vmax = hbuf[0];
+    if (!(vmax >= 1e-12)) vmax = (vmax != vmax) ? vmax : 1e-12;
+    double dt = safety * std::min(cfg.Lx / Nx, dzmin) / vmax;
+    return std::min(std::max(dt, dtmin), dtmax);
+  }
+
+  double production_dt(const double2* th, double safety, double dtmax) {
+    double fac = std::min(std::max(safety, 0.0), 80.0);
+    return std::min(dtmax, cfl_dt(th, fac, dtmax, 1e-10));
+  }
+
+  void project(const double2* in, double2* out) {
+    zop(dV, 0, in, sp[5]);
+    zop(dVi, 0, sp[5], out, KFactor(), 1);
+  }
+
+  // ------------------------------------------------------- Phi source
+  // (Di/Ra) F(Phi) with tau rows zeroed, from psi* and the step's eta
+  // (physics/dissipation.py:313-378, :445-459)
+  void phi_grid(const double2* psi, const double* eta_pad, double coef, double* out, int accumulate) {
+    KFactor fik; fik.cre = 0.0; fik.cim = 1.0; fik.kpow = 1;
+    synth(psi, dVD, fik, gr[6], Np, sp[6]);                 // exx = i k D psi
+    KFactor h; h.cre = 0.5;
+    KFactor hk; hk.cre = 0.5; hk.kpow = 2;
+    zop(dVD2, 0, psi, sp[7], h);                             // V (exz) = 0.5 (V D2 psi + k^2 V psi)
+    zop(dV, 0, psi, sp[7], hk, 0, 1);
+    SynthJob s{sp[7], gr[7]};
+    synth_x(ctx, &s, 1, Nk, N, Np, dtwNp);
+    // ezz = -exx and tr = 0 exactly, so gzz^2 = gxx^2 and gtr = 0
+    grid_phi(ctx, gr[6], gr[6], gr[7], nullptr, eta_pad, coef, out, (long long)Np * N, accumulate);
+  }
+
+  void phi_source(const double2* psi, double2* out) {
+    const double* ep = nullptr;
+    if (cfg.model == SMC_MODEL_ETA_Z) ep = dEtaPadZ;
+    else if (cfg.model == SMC_MODEL_ETA_T) {
+      if (have_last_eta) { eta_pad_from_grid(dLastEta, gr[8]); ep = gr[8]; }
+      else ep = dEtaPadZ;
+    }
+    phi_grid(psi, ep, 1.0, gr[9], 0);
+    KFactor f; f.cre = cfg.dissipation_number / cfg.Ra;
+    analyze(gr[9], Np, out, sp[8], f, 1);
+  }
+
+  // -------------------------------------------------------- const step
+  void step_const(const double2* th, double2* out, double dt) {
+    stokes_const(th, dPsi, dOm);
+    ZJob jobs[4];
+    KFactor ik; ik.cre = 0.0; ik.cim = 1.0; ik.kpow = 1;
+    KFactor mik; mik.cre = 0.0; mik.cim = -1.0; mik.kpow = 1;
+    jobs[0].Z = dV; jobs[0].X = th; jobs[0].Y = sp[0]; jobs[0].f = ik;     // thx
+    jobs[1].Z = dVD; jobs[1].X = th; jobs[1].Y = sp[1];                   // thz
+    jobs[2].Z = dVD; jobs[2].X = dPsi; jobs[2].Y = sp[2];                 // ux
+    jobs[3].Z = dV; jobs[3].X = dPsi; jobs[3].Y = sp[3]; jobs[3].f = mik; // uz
+    zmat_apply(ctx, jobs, 4, Nk, N, dkx);
+    SynthJob sj[4] = {{sp[0], gr[0]}, {sp[1], gr[1]}, {sp[2], gr[2]}, {sp[3], gr[3]}};
+    synth_x(ctx, sj, 4, Nk, N, Np, dtwNp);
+    grid_explicit_nonlinear(ctx, gr[2], gr[3], gr[0], gr[1], cfg.internal_heating, gr[4],
+                            (long long)Np * N);
+    if (cfg.dissipation_number != 0.0)
+      phi_grid(dPsi, nullptr, cfg.dissipation_number / cfg.Ra, gr[4], 1);
+    analyze(gr[4], Np, sp[5], sp[6]);                                      // Nc
+    const_rhs(ctx, th, sp[5], dt, sp[7], n);
+    LamSlot& L = lam_lu(1.0 / dt);
+    lu_small_solve(ctx, L.LU, L.piv, NN, sp[7], out, N, Nk, -1.0, 1, nullptr);
+    ctr.n_steps++;
+  }
+
+  // ---------------------------------------------- implicit theta step
+  void theta_matvec(const double2* v, double2* out) {
+    ZJob jobs[2];
+    KFactor ik; ik.cre = 0.0; ik.cim = 1.0; ik.kpow = 1;
+    jobs[0].Z = dV; jobs[0].X = v; jobs[0].Y = sp[9]; jobs[0].f = ik;
+    jobs[1].Z = dVD; jobs[1].X = v; jobs[1].Y = sp[10];
+    zmat_apply(ctx, jobs, 2, Nk, N, dkx);
+    SynthJob sj[2] = {{sp[9], gr[2]}, {sp[10], gr[3]}};
+    synth_x(ctx, sj, 2, Nk, N, Np, dtwNp);
+    grid_advect_product(ctx, gr[0], gr[1], gr[2], gr[3], gr[4], (long long)Np * N);
+    AnaJob a{gr[4], sp[11]};
+    analysis_x(ctx, &a, 1, Nk, N, Np, dtwNp, 1.0 / Np);
+    theta_combine(ctx, v, sp[11], dD2, dVi, dV, dkx, a0, out, Nk, N);
+  }
+
+  void set_step(double dt, bool have_p, double dtp) {
+    if (!have_p) {
+      a0 = b0 = 1.0 / dt;
+      b1 = 0.0;
+      ctr.n_be_fallback++;
+      return;
+    }
+    double r = dt / dtp;
+    a0 = (1.0 + 2.0 * r) / ((1.0 + r) * dt);
+    b0 = (1.0 + r) / dt;
+    b1 = r * r / ((1.0 + r) * dt);
+  }
+
+  void step_theta(const double2* th_in, double2* out, double dt) {
+    const bool sym = cfg.symmetrize != 0;
+    const double2* th1 = th_in;
+    if (sym) { project(th_in, dTh1); th1 = dTh1; }
+    const double2* th2 = th1;
+    if (sym) { project(th1, dTh2); th2 = dTh2; }
+    stokes(th2, dPsi, dOm);
+    vec_copy(ctx, dPsiN, dPsi, n);
+    const double2* ps = dPsi;
+    if (have_prev) { extrapolate(ctx, dPsi, dPsiPrev, dPsiStar, n); ps = dPsiStar; }
+    // frozen velocity on the padded grid
+    KFactor mik; mik.cre = 0.0; mik.cim = -1.0; mik.kpow = 1;
+    synth(ps, dVD, KFactor(), gr[0], Np, sp[12]);
+    synth(ps, dV, mik, gr[1], Np, sp[12]);
+    const double2* phi = nullptr;
+    if (cfg.dissipation_number != 0.0) { phi_source(ps, dPhi); phi = dPhi; }
+    set_step(dt, have_prev, dt_prev);
+    theta_rhs(ctx, th2, dPrev, ps, phi, dkx, b0, b1, cfg.internal_heating, dKb, Nk, N);
+    Op A = [&](const double2* v, double2* o) { theta_matvec(v, o); };
+    LamSlot* Lp = &lam_lu(a0);
+    double* LU = Lp->LU;
+    int* piv = Lp->piv;
+    Op M = [&](const double2* r, double2* z) {
+      lu_small_solve(ctx, LU, piv, NN, r, z, N, Nk, -1.0, 1, nullptr);
+    };
+    FgmresResult fr = fgmres(A, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
+    // true relative residual of the accepted solution (implicit_theta.py:510-516)
+    theta_matvec(dRhs, sp[13]);
+    vec_axpby(ctx, sp[13], make_double2(1.0, 0.0), dKb, make_double2(-1.0, 0.0), n);
+    double bn = std::max(norm(dKb), 1e-300);
+    ctr.theta_last_res = norm(sp[13]) / bn;
+    ctr.theta_last_iters = fr.iters;
+    ctr.n_theta_iters += fr.iters;
+    ctr.n_theta_solves++;
+    if (fr.info != 0) ctr.n_theta_nonconv++;
+    ctr.n_steps++;
+    if (sym) project(dRhs, out);
+    else vec_copy(ctx, out, dRhs, n);
+    vec_copy(ctx, dPrev, th1, n);
+    vec_copy(ctx, dPsiPrev, dPsiN, n);
+    dt_prev = dt;
+    have_prev = true;
+  }
+
+  void step(const double2* in, double2* out, double dt) {
+    if (cfg.model == SMC_MODEL_CONST) step_const(in, out, dt);
+    else step_theta(in, out, dt);
+  }
+
+  // -------------------------------------------------------------- FGMRES
+  // right-preconditioned, zero initial guess (core/krylov_fgmres.py:60-179)
+  FgmresResult fgmres(const Op& A, const Op& M, const double2* b, double2* x, double rtol,
+                      int restart, int maxiter) {
+    FgmresResult res;
+    const int m = std::max(1, std::min(restart, mmax));
+    vec_zero(ctx, x, n * sizeof(double2));
+    double beta = norm(b);                 // r0 = b - A(0) = b
+    const double tol = rtol * beta;
+    if (beta <= tol) { res.info = 0; res.iters = 0; return res; }
+    vec_copy(ctx, dKr, b, n);
+    int total = 0, info = 1;
+    std::vector<cplx> H((size_t)(m + 1) * m), g(m + 1), sn(m);
+    std::vector<double> cs(m);
+    std::vector<double2> hv(m + 2);
+    auto Hij = [&](int i, int j) -> cplx& { return H[(size_t)i * m + j]; };
+    while (total < maxiter) {
+      std::fill(H.begin(), H.end(), cplx(0, 0));
+      std::fill(g.begin(), g.end(), cplx(0, 0));
+      vec_div(ctx, dKr, beta, dKV, n);
+      g[0] = beta;
+      int k = 0;
+      for (int j = 0; j < m; ++j) {
+        if (total >= maxiter) { info = 1; break; }
+        double2* Vj = dKV + (size_t)j * n;
+        double2* Zj = dKZ + (size_t)j * n;
+        M(Vj, Zj);
+        A(Zj, dKw);
+        mgs(ctx, dKV, j, n, dKw, dKh);
+        SMC_CUDA(cudaMemcpyAsync(hv.data(), dKh, (j + 2) * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+        SMC_CUDA(cudaStreamSynchronize(stream));
+        for (int i = 0; i <= j; ++i) Hij(i, j) = cplx(hv[i].x, hv[i].y);
+        const double hn = hv[j + 1].x;
+        Hij(j + 1, j) = hn;
+        for (int i = 0; i < j; ++i) {
+          cplx t = cs[i] * Hij(i, j) + sn[i] * Hij(i + 1, j);
+          Hij(i + 1, j) = -std::conj(sn[i]) * Hij(i, j) + cs[i] * Hij(i + 1, j);
+          Hij(i, j) = t;
+        }
+        // complex Givens (krylov_fgmres.py:42-57)
+        cplx a = Hij(j, j), bb = Hij(j + 1, j);
+        double aa = std::abs(a), bba = std::abs(bb);
+        double c;
+        cplx s, rjj;
+        if (bba == 0.0) { c = 1.0; s = 0.0; rjj = a; }
+        else if (aa == 0.0) { c = 0.0; s = std::conj(bb) / bba; rjj = bba; }
+        else {
+          double den = std::sqrt(aa * aa + bba * bba);
+          c = aa / den;
+          s = c * std::conj(bb) / std::conj(a);
+          rjj = c * (aa * aa + bba * bba) / std::conj(a);
+        }
+        cs[j] = c; sn[j] = s;
+        Hij(j, j) = rjj;
+        Hij(j + 1, j) = 0.0;
+        cplx t = c * g[j] + s * g[j + 1];
+        g[j + 1] = -std::conj(s) * g[j] + c * g[j + 1];
+        g[j] = t;
+        ++total;
+        k = j + 1;
+        if (std::abs(g[j + 1]) <= tol) { info = 0; break; }
+        if (hn == 0.0) { info = 2; break; }
+        vec_div(ctx, dKw, hn, dKV + (size_t)(j + 1) * n, n);
+      }
+      if (k == 0) break;
+      // back substitution of the triangular H[:k,:k] y = g[:k]
+      std::vector<cplx> y(k);
+      for (int i = k - 1; i >= 0; --i) {
+        cplx s = g[i];
+        for (int q = i + 1; q < k; ++q) s -= Hij(i, q) * y[q];
+        y[i] = s / Hij(i, i);
+      }
+      std::vector<double2> yd(k);
+      for (int i = 0; i < k; ++i) yd[i] = make_double2(y[i].real(), y[i].imag());
+      SMC_CUDA(cudaMemcpyAsync(dKy, yd.data(), k * sizeof(double2), cudaMemcpyHostToDevice, stream));
+      krylov_update(ctx, x, dKZ, dKy, k, n);
+      if (info == 0 || info == 2) break;
+      A(x, dKr);
+      vec_axpby(ctx, dKr, make_double2(1.0, 0.0), b, make_double2(-1.0, 0.0), n);   // r = b - Ax
+      beta = norm(dKr);
+      if (beta <= tol) { info = 0; break; }
+    }
+    res.info = info;
+    res.iters = total;
+    return res;
+  }
+
+  ~Model() {
+    if (stream) { cudaStreamSynchronize(stream); cudaStreamDestroy(stream); }
+    if (hbuf) cudaFreeHost(hbuf);
+  }
+};
+
+// small helper kernels of the runtime
+__global__ void smc_realpart_kernel(const double2* in, double* out, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[i].x;
+}
+__global__ void smc_tocomplex_kernel(const double* in, double2* out, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_double2(in[i], 0.0);
+}
+__global__ void smc_comm_kernel(const double* a, const double* b, const double* c, double* out,
+                                long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (a[i] - 2.0 * b[i]) + c[i];
+}
+void Model::realpart(const double2* in, double* out, int count) {
+  smc_realpart_kernel<<<ceil_div(count, 128), 128, 0, stream>>>(in, out, count);
+  SMC_LAUNCH_CHECK(ctx);
+}
+void Model::to_complex(const double* in, double2* out, int count) {
+  smc_tocomplex_kernel<<<ceil_div(count, 128), 128, 0, stream>>>(in, out, count);
+  SMC_LAUNCH_CHECK(ctx);
+}
+void Model::comm_combine(const double* a, const double* b, const double* c, double* out,
+                         long long cnt) {
+  smc_comm_kernel<<<ceil_div(cnt, 256), 256, 0, stream>>>(a, b, c, out, cnt);
+  SMC_LAUNCH_CHECK(ctx);
+}
+
+}  // namespace smc
+
+// ====================================================================== C ABI
+struct smc_handle {
+  smc::Model m;
+};
+
+using smc::Model;
+
+namespace {
+
+int fail(const std::exception& e) {
+  smc::g_last_error = e.what();
+  return -1;
+}
+
+void copy_in(Model& m, double2* dst, const double* src, int mem, long long count) {
+  auto kind = mem == SMC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  SMC_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double2), kind, m.stream));
+}
+void copy_out(Model& m, double* dst, const void* src, int mem, long long bytes) {
+  auto kind = mem == SMC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  SMC_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, m.stream));
+  SMC_CUDA(cudaStreamSynchronize(m.stream));
+}
+
+void validate(const smc_config* c) {
+  if (!c) throw std::runtime_error("null config");
+  if (c->abi_version != SMC_ABI_VERSION) throw std::runtime_error("smc_config.abi_version mismatch");
+  if (c->model < 0 || c->model > 2) throw std::runtime_error("unknown model");
+  if (c->Nx < 4 || c->Nz < 4) throw std::runtime_error("Nx, Nz must be >= 4");
+  if (c->Nx % 2) throw std::runtime_error("Nx must be even");
+  if (!(c->Ra > 0) || !(c->Lx > 0) || !(c->deta_T > 0)) throw std::runtime_error("Ra, Lx, deta_T must be positive");
+  if (!(c->eta_min > 0) || !(c->eta_max > c->eta_min)) throw std::runtime_error("bad eta window");
+  if (c->lag < 1 || c->max_K < 1 || c->K < 0) throw std::runtime_error("bad defect-correction settings");
+  if (c->theta_restart < 1 || c->stokes_restart < 1) throw std::runtime_error("bad restart");
+  if (c->precision != SMC_FP64) throw std::runtime_error("only SMC_FP64 is built in this library");
+}
+
+}  // namespace
+
+extern "C" {
+
+void smc_config_defaults(smc_config* c) {
+  std::memset(c, 0, sizeof(*c));
+  c->abi_version = SMC_ABI_VERSION;
+  c->model = SMC_MODEL_ETA_T;
+  c->Nx = 64; c->Nz = 96;
+  c->Ra = 1e4; c->Lx = 2.0; c->deta_T = 1000.0;
+  c->eta_min = 1e-3; c->eta_max = 1e3;
+  c->precond = SMC_PRECOND_LEGACY;
+  c->symmetrize = 1;
+  c->lag = 16; c->K = 3; c->max_K = 8;
+  c->defect_tol = 1e-8;
+  c->eta_drift_tol = 0.1;
+  c->stokes_rtol = 1e-8; c->theta_rtol = 1e-10;
+  c->theta_maxiter = 200; c->theta_restart = 40;
+  c->stokes_restart = 80; c->stokes_maxiter = 800;
+  c->precision = SMC_FP64;
+  c->device = 0;
+}
+
+int smc_create(const smc_config* cfg, smc_handle** out) {
+  try {
+    validate(cfg);
+    std::unique_ptr<smc_handle> h(new smc_handle());
+    h->m.cfg = *cfg;
+    h->m.setup();
+    *out = h.release();
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(e);
+  }
+}
+
+int smc_destroy(smc_handle* h) {
+  delete h;
+  return 0;
+}
+
+#define SMC_GUARD(h, ...)                                    \
+  try {                                                      \
+    if (!(h)) throw std::runtime_error("null handle");       \
+    SMC_CUDA(cudaSetDevice((h)->m.device));                  \
+    __VA_ARGS__;                                             \
+    return 0;                                                \
+  } catch (const std::exception& e) {                        \
+    return fail(e);                                          \
+  }
+
+int smc_step(smc_handle* h, const double* in, double* out, int mem, double dt) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_in(m, m.dIn, in, mem, m.n);
+    m.step(m.dIn, m.dOut, dt);
+    copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
+  })
+}
+
+int smc_cfl_dt(smc_handle* h, const double* in, int mem, double safety, double dtmax, double dtmin,
+               double* dt_out) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_in(m, m.dIn, in, mem, m.n);
+    *dt_out = m.cfl_dt(m.dIn, safety, dtmax, dtmin);
+  })
+}
+
+int smc_production_dt(smc_handle* h, const double* in, int mem, double safety, double dtmax,
+                      double* dt_out) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_in(m, m.dIn, in, mem, m.n);
+    *dt_out = m.production_dt(m.dIn, safety, dtmax);
+  })
+}
+
+int smc_march_adaptive(smc_handle* h, const double* in, double* out, int mem, double tstop,
+                       double safety, double dtmax, long long max_steps, smc_march_info* info) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_in(m, m.dS0, in, mem, m.n);
+    double2* cur = m.dS0;
+    double2* nxt = m.dS1;
+    double t = 0.0, dt = NAN;
+    long long steps = 0;
+    while (t < tstop && (max_steps <= 0 || steps < max_steps)) {
+      dt = m.production_dt(cur, safety, dtmax);
+      m.step(cur, nxt, dt);
+      std::swap(cur, nxt);
+      t += dt;
+      ++steps;
+    }
+    copy_out(m, out, cur, mem, m.n * sizeof(double2));
+    if (info) { info->steps = steps; info->t = t; info->dt = dt; }
+  })
+}
+
+int smc_march(smc_handle* h, const double* in, double* out, int mem, double dt, long long nsteps) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_in(m, m.dS0, in, mem, m.n);
+    double2* cur = m.dS0;
+    double2* nxt = m.dS1;
+    for (long long s = 0; s < nsteps; ++s) {
+      m.step(cur, nxt, dt);
+      std::swap(cur, nxt);
+    }
+    copy_out(m, out, cur, mem, m.n * sizeof(double2));
+  })
+}
+
+int smc_diagnostics(smc_handle* h, const double* in, int mem, smc_diag* out) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_in(m, m.dIn, in, mem, m.n);
+    m.stokes(m.dIn, m.dPsi, m.dOm);
+    m.velocity(m.dPsi, m.gr[0], m.gr[1]);
+    m.synth(m.dIn, m.dV, smc::KFactor(), m.gr[2], m.Nx, m.sp[4]);
+    smc::diagnostics_reduce(m.ctx, m.gr[0], m.gr[1], m.gr[2], m.dIn, m.dD, m.dV, m.dwq, m.Nx, m.N, m.dScal);
+    m.sync_read(m.dScal, 6);
+    out->Nu_top = m.hbuf[0]; out->Nu_bot = m.hbuf[1]; out->Nu_energy = m.hbuf[2];
+    out->urms = m.hbuf[3]; out->umax = m.hbuf[4]; out->amp = m.hbuf[5];
+  })
+}
+
+int smc_stokes(smc_handle* h, const double* in, int mem, double* psi_out, double* om_out) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_in(m, m.dIn, in, mem, m.n);
+    m.stokes(m.dIn, m.dPsi, m.dOm);
+    copy_out(m, psi_out, m.dPsi, mem, m.n * sizeof(double2));
+    copy_out(m, om_out, m.dOm, mem, m.n * sizeof(double2));
+  })
+}
+
+int smc_velocity(smc_handle* h, const double* psi, int mem, double* ux, double* uz) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_in(m, m.dIn, psi, mem, m.n);
+    m.velocity(m.dIn, m.gr[0], m.gr[1]);
+    copy_out(m, ux, m.gr[0], mem, sizeof(double) * m.Nx * m.N);
+    copy_out(m, uz, m.gr[1], mem, sizeof(double) * m.Nx * m.N);
+  })
+}
+
+int smc_project_mirror(smc_handle* h, const double* in, double* out, int mem) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_in(m, m.dIn, in, mem, m.n);
+    m.project(m.dIn, m.dOut);
+    copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
+  })
+}
+
+int smc_transform(smc_handle* h, int kind, const double* in, double* out, int mem) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    long long gN = (long long)m.Nx * m.N, gP = (long long)m.Np * m.N;
+    auto kin = mem == SMC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (kind == SMC_GRID || kind == SMC_SYNTH_PAD) {
+      copy_in(m, m.dIn, in, mem, m.n);
+      int Ng = kind == SMC_GRID ? m.Nx : m.Np;
+      m.synth(m.dIn, m.dV, smc::KFactor(), m.gr[0], Ng, m.sp[0]);
+      copy_out(m, out, m.gr[0], mem, sizeof(double) * Ng * m.N);
+    } else if (kind == SMC_COEFFS) {
+      SMC_CUDA(cudaMemcpyAsync(m.gr[0], in, sizeof(double) * gN, kin, m.stream));
+      m.analyze(m.gr[0], m.Nx, m.dOut, m.sp[0]);
+      copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
+    } else if (kind == SMC_TRUNC_PAD) {
+      SMC_CUDA(cudaMemcpyAsync(m.gr[0], in, sizeof(double) * gP, kin, m.stream));
+      smc::AnaJob a{m.gr[0], m.dOut};
+      smc::analysis_x(m.ctx, &a, 1, m.Nk, m.N, m.Np, m.dtwNp, 1.0 / m.Np);
+      copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
+    } else {
+      throw std::runtime_error("unknown transform kind");
+    }
+  })
+}
+
+int smc_eta_of(smc_handle* h, const double* in, int mem, double* eta_out) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    if (m.cfg.model != SMC_MODEL_ETA_T) throw std::runtime_error("eta_of needs the eta_T model");
+    copy_in(m, m.dIn, in, mem, m.n);
+    m.eta_of(m.dIn);
+    copy_out(m, eta_out, m.dEta, mem, sizeof(double) * m.Nx * m.N);
+  })
+}
+
+int smc_schur_matvec(smc_handle* h, const double* eta, const double* v, double* out, int mem) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    if (m.cfg.model != SMC_MODEL_ETA_T) throw std::runtime_error("schur_matvec needs the eta_T model");
+    auto kin = mem == SMC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    SMC_CUDA(cudaMemcpyAsync(m.dEta, eta, sizeof(double) * m.Nx * m.N, kin, m.stream));
+    copy_in(m, m.dIn, v, mem, m.n);
+    m.eta_operator();
+    m.schur_matvec(m.dIn, m.dOut);
+    copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
+  })
+}
+
+int smc_reset_history(smc_handle* h) {
+  SMC_GUARD(h, { h->m.have_prev = false; })
+}
+
+int smc_counters_get(smc_handle* h, smc_counters* out) {
+  SMC_GUARD(h, {
+    *out = h->m.ctr;
+    out->n_kernel_launches = h->m.nlaunch;
+  })
+}
+
+int smc_shape(smc_handle* h, int* Nk, int* Nx, int* Nz, int* Np) {
+  SMC_GUARD(h, {
+    *Nk = h->m.Nk; *Nx = h->m.Nx; *Nz = h->m.N; *Np = h->m.Np;
+  })
+}
+
+void* smc_stream(smc_handle* h) { return h ? (void*)h->m.stream : nullptr; }
+
+const char* smc_last_error(void) { return smc::g_last_error.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,83 @@
+"""The C-ABI boundary without a GPU: the library builds, loads and exports
+every symbol include/specmc_gb300.h declares; the host mirror of the
+reference interface validates like the reference."""
+import os
+import re
+import warnings
+
+import pytest
+
+from conftest import ROOT
+
+
+def test_library_exports_every_declared_symbol():
+    from specmc_gb300 import _lib
+    _lib.build()
+    lib = _lib.load()
+    hdr = open(os.path.join(ROOT, "include", "specmc_gb300.h")).read()
+    declared = set(re.findall(r"^(?:int|void\s*\*?|const char\s*\*)\s*(smc_[a-z_]+)\s*\(",
+                              hdr, flags=re.M))
+    assert declared, "no declarations found"
+    assert declared == set(_lib.EXPORTED)
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def test_config_defaults_roundtrip():
+    import ctypes
+    from specmc_gb300 import _lib
+    lib = _lib.load()
+    c = _lib.SmcConfig()
+    lib.smc_config_defaults(ctypes.byref(c))
+    assert (c.Nx, c.Nz, c.lag, c.K, c.max_K) == (64, 96, 16, 3, 8)
+    assert c.defect_tol == 1e-8 and c.theta_rtol == 1e-10 and c.stokes_rtol == 1e-8
+    assert c.theta_restart == 40 and c.stokes_restart == 80 and c.stokes_maxiter == 800
+
+
+def test_create_reports_errors_not_crashes():
+    """A bad config is a hard error with a message (no GPU needed)."""
+    import ctypes
+    from specmc_gb300 import _lib
+    lib = _lib.load()
+    c = _lib.SmcConfig()
+    lib.smc_config_defaults(ctypes.byref(c))
+    c.Nx = 3
+    h = ctypes.c_void_p()
+    assert lib.smc_create(ctypes.byref(c), ctypes.byref(h)) < 0
+    assert b"Nx" in lib.smc_last_error()
+
+
+def test_config_validation_mirrors_reference():
+    from specmc_gb300.config import ConvectionConfig
+    with pytest.raises(ValueError):
+        ConvectionConfig(viscosity_model="nope")
+    with pytest.raises(NotImplementedError):
+        ConvectionConfig(viscosity_model="eta_Tz")
+    with pytest.raises(ValueError):
+        ConvectionConfig(viscosity_model="eta_T", arrhenius_Ts=1.0)
+    with pytest.raises(ValueError):
+        ConvectionConfig(eta_min=1.0, eta_max=0.5)
+    with pytest.raises(ValueError):
+        ConvectionConfig(precond="ilu")
+    with pytest.raises(ValueError):
+        ConvectionConfig(K=9)
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        ConvectionConfig(symmetrize=False)
+        assert any(issubclass(x.category, UserWarning) for x in w)
+    c = ConvectionConfig(viscosity_model="arrhenius", arrhenius_Ts=1.0)
+    assert c.canonical()["viscosity_model"] == "arrhenius"
+
+
+def test_api_dispatch_table():
+    from specmc_gb300 import api
+    from specmc_gb300.config import ConvectionConfig
+    from specmc_gb300.solver import RBC, RBCCoupled, RBCImplicitTheta
+    assert api.MODEL_CLASSES == {"const": RBC, "eta_z": RBCImplicitTheta,
+                                 "eta_T": RBCCoupled, "arrhenius": RBCCoupled}
+    d = api.describe(ConvectionConfig())
+    assert d["model_class"] == "RBCCoupled" and d["numerics"]["DTMAX"] == 4e-5
+    spec = api.model_spec(ConvectionConfig(defect_tol=0.0, K=3))
+    assert spec["kwargs"]["defect_tol"] is None
+    with pytest.raises(NotImplementedError):
+        api.model_spec(ConvectionConfig(compressibility="tala"))

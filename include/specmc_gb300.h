@@ -125,6 +125,26 @@ int smc_march_adaptive(smc_handle* h, const double* that_in, double* that_out,
 int smc_march(smc_handle* h, const double* that_in, double* that_out, int mem,
               double dt, long long nsteps);
 
+/* Device-resident march (the state the C-ABI keeps between calls, as the
+ * reference's march_adaptive keeps `s` between steps, api.py:179-189):
+ * set_state uploads a state and restarts the march clock t = 0; advance runs
+ * CFL-limited steps (production_dt + step) until t >= tstop or max_steps
+ * (<= 0: unbounded); get_state downloads the current state. */
+int smc_set_state(smc_handle* h, const double* that, int mem);
+int smc_get_state(smc_handle* h, double* that_out, int mem);
+int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety,
+                double dtmax, smc_march_info* info);
+
+/* Kernel-region timing with CUDA events on the handle's stream (no
+ * reference counterpart; the reference keeps wall-clock accumulators
+ * t_stokes/t_refresh, coupled_model.py:329-330).  smc_profile(h, 1) resets
+ * and enables; smc_profile_get returns slot `slot` (name NULL past the last):
+ * total ms, launches, and the algorithmic work counted for those launches
+ * (flops, or bytes when *work_is_bytes). */
+int smc_profile(smc_handle* h, int enable);
+int smc_profile_get(smc_handle* h, int slot, const char** name, double* ms,
+                    long long* launches, double* work, int* work_is_bytes);
+
 /* model.diagnostics(that) (rbc_galerkin.py:439-453). */
 int smc_diagnostics(smc_handle* h, const double* that_in, int mem, smc_diag* out);
 
@@ -151,6 +171,13 @@ int smc_eta_of(smc_handle* h, const double* that_in, int mem, double* eta_out);
  * `eta` (Nx,Nz): out = A(eta) v, v and out (Nk,Nz) complex. */
 int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
                      double* out, int mem);
+
+/* Implementation switches with no reference counterpart (the reference has
+ * one evaluation of each operator).  "dense_mult_eta" (0/1): evaluate
+ * mult_eta with the dense per-shift Chebyshev product blocks
+ * (stokes/lagged_stokes.py:162-193 term by term) instead of the default
+ * pseudo-spectral form of the same linear map; used to cross-check them. */
+int smc_set_option(smc_handle* h, const char* key, double value);
 
 /* RBCImplicitTheta.reset_history (implicit_theta.py:601-606). */
 int smc_reset_history(smc_handle* h);

@@ -54,10 +54,18 @@ def model_kwargs(cfg: ConvectionConfig):
     return dict(model_spec(cfg)["kwargs"])
 
 
-def build_model(cfg: ConvectionConfig):
-    """Build the GPU model for ``cfg`` and check its class (specmc/api.py:102-110)."""
+def build_model(cfg: ConvectionConfig, form="plain", device=0):
+    """Build the GPU model for ``cfg`` and check its class (specmc/api.py:102-110).
+
+    ``form='plain'`` (default) is the FP64 GPU port of the reference algorithm,
+    route for route.  ``form='mixed'`` is the fast form: the coupled Stokes
+    system is solved by spectral-BFBT preconditioned FGMRES (FP64 outer loop
+    and residuals) whatever ``cfg.precond`` says, with the per-wavenumber block
+    preconditioners applied as explicit FP64 inverse operators; it agrees with
+    the plain form to the solver tolerances (1e-8 Stokes, 1e-10 theta).
+    """
     spec = model_spec(cfg)
-    model = MODEL_MODULES[spec["model"]].build(**spec["kwargs"])
+    model = MODEL_MODULES[spec["model"]].build(**spec["kwargs"], form=form, device=device)
     if type(model) is not spec["cls"]:
         raise AssertionError("internal mapping error: viscosity_model=%r built %s, expected %s"
                              % (spec["model"], type(model).__name__, spec["cls"].__name__))

@@ -202,71 +202,83 @@ __device__ __forceinline__ void argmax_merge(double& v, int& i, double ov, int o
   if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
 }
 
-// Panel factorisation of columns [p0, p0+nbp): cooperative, one CTA per SM.
+// Panel factorisation of columns [p0, p0+nbp): cooperative, one CTA per SM,
+// ONE grid barrier per column.  Rows are not swapped during the panel: the
+// pivot row of column c stays at its physical position p and is marked done
+// (excluded from later pivot searches and updates), which removes the race a
+// physical swap would have with the other CTAs' reads.  After the last
+// column the sequence of pivot rows is converted into LAPACK's sequential
+// interchanges ipiv, and laswp applies them to every column (panel included):
+// the elimination arithmetic of each row does not depend on where it sits, so
+// the result is the LAPACK layout.  Candidate pivots are double-buffered
+// (part[(c & 1)]) so a fast CTA never overwrites a slot a slow one is reading.
 __global__ void smc_zlu_panel_kernel(double2* __restrict__ A, int n, int p0, int nbp,
-                                     int* __restrict__ piv, double* __restrict__ part) {
+                                     int* __restrict__ piv, double* __restrict__ part,
+                                     int* __restrict__ done, int* __restrict__ pv) {
   cg::grid_group grid = cg::this_grid();
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
   __shared__ double rv[32];
   __shared__ int ri[32];
   __shared__ int s_p;
   __shared__ double2 prow[ZNB];
-  for (int c = p0; c < p0 + nbp; ++c) {
-    // A: local argmax of |re|+|im| over owned rows r >= c of column c
-    double best = -1.0;
-    int bi = n;
-    {
-      int t = tid;
-      // flatten owned rows, stride nt
-      int cnt = 0;
-      SMC_FOR_OWNED_ROWS(r, c, n, b, G) {
-        if ((cnt++ % nt) == t) {
-          double v = cabs1(A[r + (long long)c * n]);
-          if (v != v) v = INFINITY;           // NaN wins, like a failed factorisation
-          argmax_merge(best, bi, v, r);
-        }
+  // mark owned rows not done; local argmax of the first column
+  double best = -1.0;
+  int bi = n;
+  {
+    int cnt = 0;
+    SMC_FOR_OWNED_ROWS(r, p0, n, b, G) {
+      if ((cnt++ % nt) == tid) {
+        done[r] = 0;
+        double v = cabs1(A[r + (long long)p0 * n]);
+        if (v != v) v = INFINITY;
+        argmax_merge(best, bi, v, r);
       }
     }
+  }
+  for (int t = 0; t < nbp; ++t) {
+    const int c = p0 + t;
+    double* pw = part + (size_t)(t & 1) * 2 * G;
     for (int o = 16; o > 0; o >>= 1)
       argmax_merge(best, bi, __shfl_xor_sync(0xffffffffu, best, o), __shfl_xor_sync(0xffffffffu, bi, o));
-    if ((tid & 31) == 0) { rv[tid >> 5] = best; ri[tid >> 5] = bi; }
+    if (lane == 0) { rv[warp] = best; ri[warp] = bi; }
     __syncthreads();
     if (tid == 0) {
       double v = rv[0];
       int i = ri[0];
       for (int w = 1; w < (nt >> 5); ++w) argmax_merge(v, i, rv[w], ri[w]);
-      part[2 * b] = v;
-      part[2 * b + 1] = (double)i;
+      pw[2 * b] = v;
+      pw[2 * b + 1] = (double)i;
     }
     grid.sync();
-    // B: global pivot (every CTA), CTA 0 swaps rows c and p inside the panel
-    if (tid == 0) {
+    // global pivot, warp-parallel over the G candidates
+    if (warp == 0) {
       double v = -1.0;
       int i = n;
-      for (int g = 0; g < G; ++g) argmax_merge(v, i, part[2 * g], (int)part[2 * g + 1]);
-      if (i >= n) i = c;
-      s_p = i;
-      if (b == 0) piv[c] = i;
+      for (int g = lane; g < G; g += 32) argmax_merge(v, i, pw[2 * g], (int)pw[2 * g + 1]);
+      for (int o = 16; o > 0; o >>= 1)
+        argmax_merge(v, i, __shfl_xor_sync(0xffffffffu, v, o), __shfl_xor_sync(0xffffffffu, i, o));
+      if (lane == 0) {
+        if (i >= n) i = c;          // all-zero or empty column: keep the diagonal
+        s_p = i;
+      }
     }
     __syncthreads();
     const int p = s_p;
-    if (b == 0 && p != c)
-      for (int col = p0 + tid; col < p0 + nbp; col += nt) {
-        double2 t = A[c + (long long)col * n];
-        A[c + (long long)col * n] = A[p + (long long)col * n];
-        A[p + (long long)col * n] = t;
-      }
-    grid.sync();
-    // C: scale column c below the diagonal, rank-1 update of the panel
-    for (int col = c + tid; col < p0 + nbp; col += nt) prow[col - c] = A[c + (long long)col * n];
+    if (b == 0 && tid == 0) pv[t] = p;
+    for (int col = c + tid; col < p0 + nbp; col += nt) prow[col - c] = A[p + (long long)col * n];
     __syncthreads();
-    const double2 pv = prow[0];
-    const bool nz = (pv.x != 0.0 || pv.y != 0.0);
-    const double2 rinv = nz ? cdiv(make_double2(1.0, 0.0), pv) : make_double2(0.0, 0.0);
+    const double2 pivv = prow[0];
+    const bool nz = (pivv.x != 0.0 || pivv.y != 0.0);
+    const double2 rinv = nz ? cdiv(make_double2(1.0, 0.0), pivv) : make_double2(0.0, 0.0);
     const int ncols = p0 + nbp - c - 1;
+    best = -1.0;
+    bi = n;
     int cnt = 0;
-    SMC_FOR_OWNED_ROWS(r, c + 1, n, b, G) {
+    SMC_FOR_OWNED_ROWS(r, p0, n, b, G) {
       if ((cnt++ % nt) == tid) {
+        if (r == p) { done[r] = 1; continue; }
+        if (done[r]) continue;
         double2 l = A[r + (long long)c * n];
         if (nz) l = cmul(l, rinv);
         A[r + (long long)c * n] = l;
@@ -274,17 +286,43 @@ __global__ void smc_zlu_panel_kernel(double2* __restrict__ A, int n, int p0, int
           double2* e = &A[r + (long long)(c + j) * n];
           *e = csub(*e, cmul(l, prow[j]));
         }
+        if (t + 1 < nbp) {
+          double v = cabs1(A[r + (long long)(c + 1) * n]);
+          if (v != v) v = INFINITY;
+          argmax_merge(best, bi, v, r);
+        }
       }
     }
     __syncthreads();
   }
+  // pivot rows (physical, unswapped) -> LAPACK sequential interchanges
+  if (b == 0 && tid == 0) {
+    int rowid[2 * ZNB], posn[2 * ZNB];   // tracked rows and their current positions
+    int nt2 = 0;
+    for (int t = 0; t < nbp; ++t) {
+      const int q = p0 + t, r = pv[t];
+      int pr = r;                    // current position of row r
+      for (int k = 0; k < nt2; ++k) if (rowid[k] == r) { pr = posn[k]; break; }
+      int rq = q;                    // row currently at position q
+      for (int k = 0; k < nt2; ++k) if (posn[k] == q) { rq = rowid[k]; break; }
+      piv[q] = pr;
+      // swap: row r -> q, row rq -> pr
+      bool fr = false, fq = false;
+      for (int k = 0; k < nt2; ++k) {
+        if (rowid[k] == r) { posn[k] = q; fr = true; }
+        else if (rowid[k] == rq) { posn[k] = pr; fq = true; }
+      }
+      if (!fr && nt2 < 2 * ZNB) { rowid[nt2] = r; posn[nt2] = q; ++nt2; }
+      if (!fq && rq != r && nt2 < 2 * ZNB) { rowid[nt2] = rq; posn[nt2] = pr; ++nt2; }
+    }
+  }
 }
 
-// row interchanges of panel [p0, p0+nbp) applied to every column outside it
+// row interchanges of panel [p0, p0+nbp) applied to every column
 __global__ void smc_zlu_laswp_kernel(double2* __restrict__ A, int n, int p0, int nbp,
                                      const int* __restrict__ piv) {
   int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= n || (col >= p0 && col < p0 + nbp)) return;
+  if (col >= n) return;
   double2* Ac = A + (long long)col * n;
   for (int i = p0; i < p0 + nbp; ++i) {
     int p = piv[i];
@@ -372,10 +410,12 @@ void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work) {
   int maxb = 0;
   SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, smc_zlu_panel_kernel, 256, 0));
   if (maxb < 1) throw std::runtime_error("zlu_dense: panel kernel cannot be co-resident");
-  double* part = reinterpret_cast<double*>(work);
+  double* part = reinterpret_cast<double*>(work);                 // 4 G doubles
+  int* done = reinterpret_cast<int*>(part + 4 * G + 64);           // n ints
+  int* pv = done + n + 64;                                          // ZNB ints
   for (int p0 = 0; p0 < n; p0 += ZNB) {
     int nbp = std::min(ZNB, n - p0);
-    void* args[] = {&A, &n, &p0, &nbp, &piv, &part};
+    void* args[] = {&A, &n, &p0, &nbp, &piv, &part, &done, &pv};
     SMC_CUDA(cudaLaunchCooperativeKernel((void*)smc_zlu_panel_kernel, dim3(G), dim3(256), args, 0, c.s));
     SMC_LAUNCH_CHECK(c);
     smc_zlu_laswp_kernel<<<ceil_div(n, 128), 128, 0, c.s>>>(A, n, p0, nbp, piv);
@@ -394,58 +434,85 @@ void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work) {
 // ================================================== dense triangular solve
 static constexpr int SB = 64;      // diagonal block of the solve
 
-// x = U^{-1} L^{-1} b[perm]: cooperative, one CTA per SM.  Each CTA solves the
-// current diagonal block redundantly (no grid barrier inside the block) and
-// updates the rows it owns (32-row chunks dealt round-robin).  The forward
-// sweep updates `x` in place and writes solved blocks to `y`; the backward
-// sweep updates `y` in place and writes solved blocks to `x`, so a block is
-// never written while another CTA may still be reading it.
+// Inverses of the SB x SB diagonal blocks of L (unit lower) and U (upper),
+// column-major, computed once per factorisation: blockIdx.x = block,
+// blockIdx.y = 0 (L) / 1 (U).  Thread c forms column c of the inverse.
+__global__ void smc_zlu_diag_inv_kernel(const double2* __restrict__ LU, int n,
+                                        double2* __restrict__ invL, double2* __restrict__ invU) {
+  extern __shared__ double2 sm[];
+  double2* Bk = sm;               // SB*SB block
+  double2* X = sm + SB * SB;      // SB*SB inverse
+  const int bk = blockIdx.x, upper = blockIdx.y;
+  const int r0 = bk * SB, m = min(SB, n - r0);
+  for (int t = threadIdx.x; t < SB * SB; t += blockDim.x) {
+    int r = t % SB, c = t / SB;
+    Bk[t] = (r < m && c < m) ? LU[(r0 + r) + (long long)(r0 + c) * n]
+                             : make_double2((r == c) ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  const int c = threadIdx.x;
+  if (c < SB) {
+    double2* x = X + c * SB;
+    if (!upper) {
+      for (int r = 0; r < SB; ++r) x[r] = make_double2(r == c ? 1.0 : 0.0, 0.0);
+      for (int r = c + 1; r < SB; ++r) {
+        double2 acc = x[r];
+        for (int j = c; j < r; ++j) acc = csub(acc, cmul(Bk[r + j * SB], x[j]));
+        x[r] = acc;
+      }
+    } else {
+      for (int r = 0; r < SB; ++r) x[r] = make_double2(0.0, 0.0);
+      for (int r = c; r >= 0; --r) {
+        double2 acc = make_double2(r == c ? 1.0 : 0.0, 0.0);
+        for (int j = r + 1; j <= c; ++j) acc = csub(acc, cmul(Bk[r + j * SB], x[j]));
+        x[r] = cdiv(acc, Bk[r + r * SB]);
+      }
+    }
+  }
+  __syncthreads();
+  double2* dst = (upper ? invU : invL) + (long long)bk * SB * SB;
+  for (int t = threadIdx.x; t < SB * SB; t += blockDim.x) dst[t] = X[t];
+}
+
 __device__ __forceinline__ int first_owned_chunk(int row_lo, int b, int G) {
   int c0 = row_lo / 32;
   return c0 + ((b - c0 % G) % G + G) % G;
 }
 
+// One block step of the solve.  Every CTA forms x_blk = inv(D_bk) w[r0:r1]
+// (a 64 x 64 GEMV, redundant across CTAs so no barrier is needed inside the
+// step); the block's owner writes x_blk to `dst`; each CTA then updates the
+// rows it owns (32-row chunks dealt round-robin) below (forward) or above
+// (backward) the block.  The forward sweep updates `x` in place and writes
+// solved blocks to `y`, the backward sweep updates `y` and writes to `x`,
+// so a block is never written while another CTA may still be reading it.
 template <bool LOWER>
-__device__ void smc_trsv_block(const double2* __restrict__ LU, double2* __restrict__ work,
-                               double2* __restrict__ dst, int n, int bk, double2* Db, double2* xb,
-                               double2 (*red)[32]) {
+__device__ void smc_trsv_block(const double2* __restrict__ LU, const double2* __restrict__ inv,
+                               double2* __restrict__ work, double2* __restrict__ dst, int n,
+                               int bk, double2* win, double2* xb, double2 (*red)[32]) {
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int r0 = bk * SB, r1 = min(n, r0 + SB), m = r1 - r0;
-  for (int t = tid; t < SB * SB; t += 256) {
-    int r = t % SB, cc = t / SB;
-    Db[t] = (r < m && cc < m) ? LU[(r0 + r) + (long long)(r0 + cc) * n]
-                              : make_double2(LOWER ? 0.0 : 1.0, 0.0);
-  }
-  if (tid < SB) xb[tid] = (tid < m) ? work[r0 + tid] : make_double2(0.0, 0.0);
-  __syncthreads();
-  if (warp == 0) {
-    double2 v0 = xb[lane], v1 = xb[lane + 32];
-    if (LOWER) {
-      for (int cc = 0; cc < m; ++cc) {
-        double2 xc = (cc < 32) ? make_double2(__shfl_sync(0xffffffffu, v0.x, cc), __shfl_sync(0xffffffffu, v0.y, cc))
-                               : make_double2(__shfl_sync(0xffffffffu, v1.x, cc - 32), __shfl_sync(0xffffffffu, v1.y, cc - 32));
-        if (lane > cc) v0 = csub(v0, cmul(Db[lane + cc * SB], xc));
-        if (lane + 32 > cc) v1 = csub(v1, cmul(Db[lane + 32 + cc * SB], xc));
-      }
-    } else {
-      for (int cc = m - 1; cc >= 0; --cc) {
-        if (cc < 32) { if (lane == cc) v0 = cdiv(v0, Db[cc + cc * SB]); }
-        else if (lane == cc - 32) v1 = cdiv(v1, Db[cc + cc * SB]);
-        double2 xc = (cc < 32) ? make_double2(__shfl_sync(0xffffffffu, v0.x, cc), __shfl_sync(0xffffffffu, v0.y, cc))
-                               : make_double2(__shfl_sync(0xffffffffu, v1.x, cc - 32), __shfl_sync(0xffffffffu, v1.y, cc - 32));
-        if (lane < cc) v0 = csub(v0, cmul(Db[lane + cc * SB], xc));
-        if (lane + 32 < cc) v1 = csub(v1, cmul(Db[lane + 32 + cc * SB], xc));
-      }
-    }
-    xb[lane] = v0;
-    xb[lane + 32] = v1;
-  }
-  __syncthreads();
-  if (b == bk % G)
-    for (int i = tid; i < m; i += 256) dst[r0 + i] = xb[i];
-  // rows to update: below the block (forward) or above it (backward)
   const int lo = LOWER ? r1 : 0, hi = LOWER ? n : r0;
+  const bool owner = (b == bk % G);
+  const bool has_rows = first_owned_chunk(lo, b, G) * 32 < hi;
+  if (!owner && !has_rows) return;
+  if (tid < SB) win[tid] = (tid < m) ? work[r0 + tid] : make_double2(0.0, 0.0);
+  __syncthreads();
+  {
+    // xb[i] = sum_j inv[i + j*SB] win[j]: 4 threads per row, 16 terms each
+    const int i = tid & 63, qd = tid >> 6;
+    const double2* Ib = inv + (long long)bk * SB * SB;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int j = qd * 16; j < qd * 16 + 16; ++j) acc = cadd(acc, cmul(Ib[i + j * SB], win[j]));
+    double2* rf = &red[0][0];          // viewed as [4][64]
+    rf[qd * 64 + i] = acc;
+    __syncthreads();
+    if (tid < 64) xb[tid] = cadd(cadd(rf[tid], rf[64 + tid]), cadd(rf[128 + tid], rf[192 + tid]));
+    __syncthreads();
+  }
+  if (owner)
+    for (int i = tid; i < m; i += 256) dst[r0 + i] = xb[i];
   for (int ch = first_owned_chunk(lo, b, G); ch * 32 < hi; ch += G) {
     int r = ch * 32 + lane;
     bool act = (r >= lo && r < hi);
@@ -464,12 +531,14 @@ __device__ void smc_trsv_block(const double2* __restrict__ LU, double2* __restri
 }
 
 __global__ void __launch_bounds__(256) smc_zlu_solve_kernel(const double2* __restrict__ LU,
+                                                           const double2* __restrict__ invL,
+                                                           const double2* __restrict__ invU,
                                                            const int* __restrict__ perm,
                                                            const double2* __restrict__ bvec,
                                                            double2* __restrict__ x,
                                                            double2* __restrict__ y, int n) {
   cg::grid_group grid = cg::this_grid();
-  extern __shared__ double2 Db[];   // diagonal block (SB x SB, column-major), dynamic
+  __shared__ double2 win[SB];
   __shared__ double2 xb[SB];
   __shared__ double2 red[8][32];
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -478,27 +547,34 @@ __global__ void __launch_bounds__(256) smc_zlu_solve_kernel(const double2* __res
   grid.sync();
   const int nblk = (n + SB - 1) / SB;
   for (int bk = 0; bk < nblk; ++bk) {
-    smc_trsv_block<true>(LU, x, y, n, bk, Db, xb, red);
+    smc_trsv_block<true>(LU, invL, x, y, n, bk, win, xb, red);
     grid.sync();
   }
   for (int bk = nblk - 1; bk >= 0; --bk) {
-    smc_trsv_block<false>(LU, y, x, n, bk, Db, xb, red);
+    smc_trsv_block<false>(LU, invU, y, x, n, bk, win, xb, red);
     grid.sync();
   }
 }
 
-void zlu_dense_solve(const Ctx& c, const double2* LU, const int* perm, const double2* b,
-                     double2* x, int n, double2* work) {
+void zlu_diag_inverses(const Ctx& c, const double2* LU, int n, double2* invL, double2* invU) {
+  const int nblk = (n + SB - 1) / SB;
+  const size_t sm = (size_t)2 * SB * SB * sizeof(double2);
+  SMC_CUDA(cudaFuncSetAttribute(smc_zlu_diag_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sm));
+  smc_zlu_diag_inv_kernel<<<dim3(nblk, 2), 64, sm, c.s>>>(LU, n, invL, invU);
+  SMC_LAUNCH_CHECK(c);
+}
+
+void zlu_dense_solve(const Ctx& c, const double2* LU, const double2* invL, const double2* invU,
+                     const int* perm, const double2* b, double2* x, int n, double2* work) {
   int G = c.num_sms;
-  const size_t dsm = (size_t)SB * SB * sizeof(double2);
-  SMC_CUDA(cudaFuncSetAttribute(smc_zlu_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)dsm));
   int maxb = 0;
-  SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, smc_zlu_solve_kernel, 256, dsm));
+  SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, smc_zlu_solve_kernel, 256, 0));
   if (maxb < 1) throw std::runtime_error("zlu_dense_solve: kernel cannot be co-resident");
   double2* y = work;
-  void* args[] = {(void*)&LU, (void*)&perm, (void*)&b, (void*)&x, (void*)&y, (void*)&n};
-  SMC_CUDA(cudaLaunchCooperativeKernel((void*)smc_zlu_solve_kernel, dim3(G), dim3(256), args, dsm, c.s));
+  void* args[] = {(void*)&LU, (void*)&invL, (void*)&invU, (void*)&perm, (void*)&b,
+                  (void*)&x, (void*)&y, (void*)&n};
+  SMC_CUDA(cudaLaunchCooperativeKernel((void*)smc_zlu_solve_kernel, dim3(G), dim3(256), args, 0, c.s));
   SMC_LAUNCH_CHECK(c);
 }
 

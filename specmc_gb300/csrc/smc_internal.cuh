@@ -29,13 +29,57 @@ struct CudaError : std::runtime_error {
                              std::to_string(__LINE__) + ")");                 \
   } while (0)
 
-// Launch context: the stream every kernel of a handle goes to, and the
-// launch counter the handle reports.
+// Optional per-tag event timer: when enabled, the launch helpers bracket
+// the kernels of a tag with CUDA events on the handle's stream; elapsed
+// times are resolved (and the events recycled) by Profiler::resolve.
+struct Profiler {
+  static constexpr int MAXTAG = 24;
+  bool enabled = false;
+  const char* names[MAXTAG] = {nullptr};
+  double ms[MAXTAG] = {0};
+  long long launches[MAXTAG] = {0};
+  double work[MAXTAG] = {0};      // algorithmic flops or bytes, as tagged
+  int work_is_bytes[MAXTAG] = {0};
+  struct Pending { int tag; cudaEvent_t a, b; };
+  Pending* pend = nullptr;
+  int npend = 0, cap = 0;
+  cudaEvent_t* pool = nullptr;
+  int npool = 0;
+  int tag_of(const char* name);
+  void begin(cudaStream_t s, int tag, cudaEvent_t* a);
+  void end(cudaStream_t s, int tag, cudaEvent_t a, double work_amount, int is_bytes);
+  void resolve();
+  void reset();
+  ~Profiler();
+};
+
+// Launch context: the stream every kernel of a handle goes to, the launch
+// counter the handle reports, and the optional profiler.
 struct Ctx {
   cudaStream_t s = nullptr;
   long long* nlaunch = nullptr;
   int num_sms = 152;
+  Profiler* prof = nullptr;
   void count(int n = 1) const { if (nlaunch) *nlaunch += n; }
+};
+
+// RAII bracket of one tagged launch region
+struct ProfScope {
+  const Ctx& c;
+  int tag = -1;
+  cudaEvent_t a = nullptr;
+  double work;
+  int is_bytes;
+  ProfScope(const Ctx& c_, const char* name, double work_ = 0.0, int is_bytes_ = 0)
+      : c(c_), work(work_), is_bytes(is_bytes_) {
+    if (c.prof && c.prof->enabled) {
+      tag = c.prof->tag_of(name);
+      c.prof->begin(c.s, tag, &a);
+    }
+  }
+  ~ProfScope() {
+    if (tag >= 0) c.prof->end(c.s, tag, a, work, is_bytes);
+  }
 };
 
 #define SMC_LAUNCH_CHECK(ctx)                                                 \
@@ -171,9 +215,12 @@ void lu_small_solve(const Ctx& c, const double* LU, const int* piv, long long lu
 // dense complex LU (column-major n x n) with partial pivoting (|re|+|im| pivot
 // choice, as LAPACK zgetrf); piv 0-based
 void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work);
-// x = A^{-1} b with a zlu_dense factor; perm = composed row permutation
-void zlu_dense_solve(const Ctx& c, const double2* LU, const int* perm,
-                     const double2* b, double2* x, int n, double2* work);
+// inverses of the 64 x 64 diagonal blocks of L and U (column-major blocks)
+void zlu_diag_inverses(const Ctx& c, const double2* LU, int n, double2* invL, double2* invU);
+// x = A^{-1} b with a zlu_dense factor; perm = composed row permutation;
+// work: n complex
+void zlu_dense_solve(const Ctx& c, const double2* LU, const double2* invL, const double2* invU,
+                     const int* perm, const double2* b, double2* x, int n, double2* work);
 
 // ============================================================ Schur ops
 // complex Chebyshev product matrices M_d for d in (-Nk, Nk): Md[(d+Nk-1)] (N x N row-major)

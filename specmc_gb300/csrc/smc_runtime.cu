@@ -22,6 +22,7 @@
 #include "smc_internal.cuh"
 #include "smc_route.cuh"
 #include "smc_schur.cuh"
+#include "smc_pseudo.cuh"
 
 namespace smc {
 
@@ -132,6 +133,7 @@ struct LamSlot {
   double key = 0.0;
   double* LU = nullptr;
   int* piv = nullptr;
+  double* Ginv = nullptr;   // A^{-1} P (tau columns zero): the solve as one GEMV
   bool used = false;
 };
 
@@ -142,6 +144,64 @@ struct FgmresResult {
 
 using Op = std::function<void(const double2*, double2*)>;
 
+// ---------------------------------------------------------------- profiler
+int Profiler::tag_of(const char* name) {
+  for (int t = 0; t < MAXTAG; ++t) {
+    if (names[t] == nullptr) { names[t] = name; return t; }
+    if (std::strcmp(names[t], name) == 0) return t;
+  }
+  return MAXTAG - 1;
+}
+void Profiler::begin(cudaStream_t s, int tag, cudaEvent_t* a) {
+  if (npool == 0) { SMC_CUDA(cudaEventCreate(a)); }
+  else *a = pool[--npool];
+  SMC_CUDA(cudaEventRecord(*a, s));
+  (void)tag;
+}
+void Profiler::end(cudaStream_t s, int tag, cudaEvent_t a, double w, int is_bytes) {
+  cudaEvent_t b;
+  if (npool == 0) { SMC_CUDA(cudaEventCreate(&b)); }
+  else b = pool[--npool];
+  SMC_CUDA(cudaEventRecord(b, s));
+  if (npend == cap) {
+    int nc = cap ? 2 * cap : 1024;
+    Pending* np = new Pending[nc];
+    for (int i = 0; i < npend; ++i) np[i] = pend[i];
+    delete[] pend;
+    pend = np;
+    cap = nc;
+    cudaEvent_t* pp = new cudaEvent_t[2 * nc];
+    for (int i = 0; i < npool; ++i) pp[i] = pool[i];
+    delete[] pool;
+    pool = pp;
+  }
+  pend[npend++] = Pending{tag, a, b};
+  launches[tag]++;
+  work[tag] += w;
+  work_is_bytes[tag] = is_bytes;
+}
+void Profiler::resolve() {
+  for (int i = 0; i < npend; ++i) {
+    SMC_CUDA(cudaEventSynchronize(pend[i].b));
+    float e = 0.f;
+    SMC_CUDA(cudaEventElapsedTime(&e, pend[i].a, pend[i].b));
+    ms[pend[i].tag] += e;
+    pool[npool++] = pend[i].a;
+    pool[npool++] = pend[i].b;
+  }
+  npend = 0;
+}
+void Profiler::reset() {
+  resolve();
+  for (int t = 0; t < MAXTAG; ++t) { ms[t] = 0; launches[t] = 0; work[t] = 0; }
+}
+Profiler::~Profiler() {
+  for (int i = 0; i < npend; ++i) { cudaEventDestroy(pend[i].a); cudaEventDestroy(pend[i].b); }
+  for (int i = 0; i < npool; ++i) cudaEventDestroy(pool[i]);
+  delete[] pend;
+  delete[] pool;
+}
+
 // =================================================================== Model
 struct Model {
   smc_config cfg{};
@@ -151,6 +211,10 @@ struct Model {
   cudaStream_t stream = nullptr;
   long long nlaunch = 0;
   Ctx ctx;
+  Profiler prof;
+  // resident state of smc_set_state / smc_advance
+  double t_resident = 0.0;
+  bool resident_cur0 = true;
   DevMem mem;
   double* hbuf = nullptr;     // pinned scalars
   smc_counters ctr{};
@@ -180,6 +244,7 @@ struct Model {
   double2 *dEtaC = nullptr, *dMd = nullptr, *dAsmWork = nullptr;
   double2* dSchur = nullptr;
   int *dSchurPiv = nullptr, *dSchurPerm = nullptr;
+  double2 *dSchurInvL = nullptr, *dSchurInvU = nullptr;
   bool have_lag = false;
   int n_since_refresh = 0;
   bool last_failed = false;
@@ -203,6 +268,15 @@ struct Model {
   double2 *dSb, *dSx, *dSr, *dSdx, *dSAx, *dSw, *dSf2, *dSf3, *dSf4, *dSt[4], *dSolveWork;
   double2 *dBfbtRhs, *dBfbtProfC;
   double* dBfbtHw;
+  // pseudo-spectral mult_eta
+  PsPlan psplan;
+  double* dPsE = nullptr;
+  double2 *dPsFv = nullptr, *dPsHv = nullptr;
+  bool use_dense_mult = false;
+  // fast (mixed) form: BFBT-preconditioned FGMRES for the coupled Stokes
+  // solve and explicit per-k inverse operators for the block preconditioners
+  bool fast = false;
+  double* dRedG = nullptr;
 
   // ------------------------------------------------------------ utilities
   void sync_read(const double* d, int count) {
@@ -256,6 +330,7 @@ struct Model {
       if (!s.used) { slot = &s; break; }
     tau_ops(ctx, dD2, dkx, lam, slot->LU, N, Nk);
     lu_small_batched(ctx, slot->LU, slot->piv, nullptr, N, Nk);
+    if (fast) green_from_lu(ctx, slot->LU, slot->piv, slot->Ginv, N, Nk);
     slot->key = key;
     slot->used = true;
     return *slot;
@@ -270,7 +345,7 @@ struct Model {
     SMC_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     int sms = 0;
     SMC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    ctx.s = stream; ctx.nlaunch = &nlaunch; ctx.num_sms = sms;
+    ctx.s = stream; ctx.nlaunch = &nlaunch; ctx.num_sms = sms; ctx.prof = &prof;
     SMC_CUDA(cudaMallocHost(&hbuf, 4096 * sizeof(double)));
     if (N < 4 || Nx < 4) throw std::runtime_error("Nx and Nz must be >= 4");
     if ((size_t)N * N * sizeof(double) > 200 * 1024)
@@ -307,7 +382,12 @@ struct Model {
     for (int k = 0; k < Nk; ++k) skip[k] = (kx_h[k] == 0.0);
     dSkipK0 = mem.upload(skip);
 
-    for (auto& s : lam_slots) { s.LU = mem.alloc<double>(Nk * NN); s.piv = mem.alloc<int>(Nk * N); }
+    fast = cfg.precision == SMC_MIXED;
+    for (auto& s : lam_slots) {
+      s.LU = mem.alloc<double>(Nk * NN);
+      s.piv = mem.alloc<int>(Nk * N);
+      if (fast) s.Ginv = mem.alloc<double>(Nk * NN);
+    }
     dLU0 = mem.alloc<double>(Nk * NN);
     dPiv0 = mem.alloc<int>(Nk * N);
     dG = mem.alloc<double>(Nk * NN);
@@ -347,6 +427,7 @@ struct Model {
       dKb = mem.alloc<double2>(n);
       dKh = mem.alloc<double2>(mmax + 2); dKy = mem.alloc<double2>(mmax + 2);
       dRedLU = mem.alloc<double>(Nk * NN); dRedPiv = mem.alloc<int>(Nk * N);
+      dRedG = mem.alloc<double>(Nk * NN);
       dM0 = mem.alloc<double>(NN); dDM0 = mem.alloc<double>(NN);
       dT1 = mem.alloc<double>(NN); dT2 = mem.alloc<double>(NN); dT3 = mem.alloc<double>(NN);
       dComm = mem.alloc<double>(NN); dCommG = mem.alloc<double>(Nk * NN);
@@ -397,12 +478,53 @@ struct Model {
         dSchur = mem.alloc<double2>((size_t)n * n);
         dSchurPiv = mem.alloc<int>(n);
         dSchurPerm = mem.alloc<int>(n);
+        {
+          long long nblk = (n + 63) / 64;
+          dSchurInvL = mem.alloc<double2>((size_t)nblk * 64 * 64);
+          dSchurInvU = mem.alloc<double2>((size_t)nblk * 64 * 64);
+        }
         dSb = mem.alloc<double2>(n); dSx = mem.alloc<double2>(n); dSr = mem.alloc<double2>(n);
         dSdx = mem.alloc<double2>(n); dSAx = mem.alloc<double2>(n); dSw = mem.alloc<double2>(n);
         dSf2 = mem.alloc<double2>(n); dSf3 = mem.alloc<double2>(n); dSf4 = mem.alloc<double2>(n);
         for (auto& p : dSt) p = mem.alloc<double2>(n);
         dSolveWork = mem.alloc<double2>(n);
         dBfbtHw = mem.alloc<double>(2 * N);
+        // pseudo-spectral plan: L >= 3 Nk - 2 x-points, Mz = 2N - 1 CGL points
+        psplan.Nk = Nk; psplan.N = N; psplan.Mz = 2 * N - 1; psplan.L = 3 * Nk - 2;
+        {
+          const int Mz = psplan.Mz, L = psplan.L;
+          std::vector<double> Zf((size_t)Mz * N), Zi((size_t)N * Mz);
+          const long double PI = 3.14159265358979323846264338327950288L;
+          for (int sI = 0; sI < Mz; ++sI)
+            for (int q = 0; q < N; ++q) {
+              // T_q(-cos(pi s/(Mz-1))) = (-1)^q cos(pi q s/(Mz-1))
+              long long r = ((long long)q * sI) % (2LL * (Mz - 1));
+              long double v = cosl(PI * (long double)r / (Mz - 1));
+              if (q & 1) v = -v;
+              Zf[(size_t)sI * N + q] = (double)v;
+            }
+          for (int pI = 0; pI < N; ++pI)
+            for (int sI = 0; sI < Mz; ++sI) {
+              long double w = (sI == 0 || sI == Mz - 1) ? 0.5L : 1.0L;
+              long double g = (pI == 0 || pI == Mz - 1) ? 2.0L : 1.0L;
+              long long r = ((long long)pI * sI) % (2LL * (Mz - 1));
+              long double t = cosl(PI * (long double)r / (Mz - 1));
+              if (pI & 1) t = -t;
+              Zi[(size_t)pI * Mz + sI] = (double)(2.0L / (Mz - 1) / g * w * t);
+            }
+          std::vector<double2> tw(L);
+          for (int m = 0; m < L; ++m) {
+            long double a = 2.0L * PI * m / L;
+            tw[m] = make_double2((double)cosl(a), (double)sinl(a));
+          }
+          tw[0] = make_double2(1.0, 0.0);
+          psplan.Zf = mem.upload(Zf);
+          psplan.Zi = mem.upload(Zi);
+          psplan.tw = mem.upload(tw);
+          dPsE = mem.alloc<double>((size_t)L * Mz);
+          dPsFv = mem.alloc<double2>((size_t)4 * Nk * Mz);
+          dPsHv = mem.alloc<double2>((size_t)4 * Nk * Mz);
+        }
         dBfbtRhs = mem.alloc<double2>(N);
         dBfbtProfC = mem.alloc<double2>(N);
         // Galerkin mass matrix V^T W V and its LU (stokes/bfbt.py:74-84)
@@ -468,6 +590,7 @@ struct Model {
 
   // eta_of (coupled_model.py:401-496) -> dEta (Nx, N)
   void eta_of(const double2* th) {
+    ProfScope ps(ctx, "eta_of");
     synth(th, dV, KFactor(), gr[0], Np, sp[0]);              // theta on 2 Nx points
     eta_law(ctx, gr[0], dz, N, (long long)Np * N, law, dEtaP, dScal, dRed);
     sync_read(dScal, 6);
@@ -505,24 +628,38 @@ struct Model {
     }
   }
 
-  // Md from the current dEta: eta_c = coeffs(eta)
+  // Md (dense blocks, for the Schur assembly) and the pseudo-spectral eta
+  // grid from the current dEta: eta_c = coeffs(eta)
   void eta_operator() {
     analyze(dEta, Nx, dEtaC, sp[2]);
     build_mult_mats(ctx, dEtaC, dMd, Nk, N);
+    ps_eta_grid(ctx, psplan, dEtaC, dPsFv, dPsE);
   }
 
   // FreeSchurOperator.matvec at the current Md (lagged_stokes.py:202-220)
   void schur_matvec(const double2* v, double2* out) {
+    // algorithmic work of the dense form: 4 mult_eta x (Nk^2 + Nk(Nk-1)/2) N^2
+    // complex MACs (8 flops each)
+    ProfScope ps(ctx, "schur_matvec", 4.0 * 8.0 * ((double)Nk * Nk + 0.5 * Nk * (Nk - 1)) * NN, 0);
     zop(dG, NN, v, dSw);                                   // w = G v
     KFactor f2; f2.cre = 2.0; f2.kpow = 2;                  // 2 k^2 w
     vec_scaled_modes(ctx, dSw, dSf2, Nk, N, f2, dkx, 0, 0);
     zop(dD2, 0, dSw, dSf3);                                // D2 w
     KFactor f4; f4.kpow = 1;                                // k (D w)
     zop(dD, 0, dSw, dSf4, f4);
-    smc::mult_eta(ctx, dMd, v, dSt[0], Nk, N, -1.0, nullptr);
-    smc::mult_eta(ctx, dMd, dSf2, dSt[1], Nk, N, -1.0, nullptr);
-    smc::mult_eta(ctx, dMd, dSf3, dSt[2], Nk, N, -1.0, nullptr);
-    smc::mult_eta(ctx, dMd, dSf4, dSt[3], Nk, N, +1.0, nullptr);
+    if (use_dense_mult) {
+      smc::mult_eta(ctx, dMd, v, dSt[0], Nk, N, -1.0, nullptr);
+      smc::mult_eta(ctx, dMd, dSf2, dSt[1], Nk, N, -1.0, nullptr);
+      smc::mult_eta(ctx, dMd, dSf3, dSt[2], Nk, N, -1.0, nullptr);
+      smc::mult_eta(ctx, dMd, dSf4, dSt[3], Nk, N, +1.0, nullptr);
+    } else {
+      PsJobs j;
+      j.f[0] = v; j.f[1] = dSf2; j.f[2] = dSf3; j.f[3] = dSf4;
+      for (int q = 0; q < 4; ++q) j.out[q] = dSt[q];
+      j.sgn[0] = j.sgn[1] = j.sgn[2] = -1.0;   // partner_sign
+      j.sgn[3] = +1.0;                          // cross term: flipped
+      ps_mult_eta(ctx, psplan, dPsE, j, 4, dPsFv, dPsHv);
+    }
     schur_combine(ctx, dSt[0], dSt[1], dSt[2], dSt[3], v, dD, dD2, dV, dkx, out, Nk, N);
   }
 
@@ -532,8 +669,16 @@ struct Model {
   }
 
   void refresh() {
-    assemble_schur(ctx, dMd, dD, dD2, dG, dV, dkx, dSchur, Nk, N, dAsmWork);
-    zlu_dense(ctx, dSchur, dSchurPiv, (int)n, dAsmWork);
+    {
+      ProfScope ps(ctx, "schur_assembly");
+      assemble_schur(ctx, dMd, dD, dD2, dG, dV, dkx, dSchur, Nk, N, dAsmWork);
+    }
+    {
+      // algorithmic work: complex LU, 8/3 n^3 real flops
+      ProfScope ps(ctx, "schur_lu", 8.0 / 3.0 * (double)n * n * n, 0);
+      zlu_dense(ctx, dSchur, dSchurPiv, (int)n, dAsmWork);
+      zlu_diag_inverses(ctx, dSchur, (int)n, dSchurInvL, dSchurInvU);
+    }
     std::vector<int> piv(n), perm(n);
     SMC_CUDA(cudaMemcpyAsync(piv.data(), dSchurPiv, n * sizeof(int), cudaMemcpyDeviceToHost, stream));
     SMC_CUDA(cudaStreamSynchronize(stream));
@@ -548,7 +693,9 @@ struct Model {
   }
 
   void lag_solve(const double2* b, double2* x) {
-    zlu_dense_solve(ctx, dSchur, dSchurPerm, b, x, (int)n, dSolveWork);
+    // algorithmic bytes: the n^2 complex factor is read once per solve
+    ProfScope ps(ctx, "schur_lu_solve", 16.0 * (double)n * n, 1);
+    zlu_dense_solve(ctx, dSchur, dSchurInvL, dSchurInvU, dSchurPerm, b, x, (int)n, dSolveWork);
   }
 
   // coupled_model.py:524-573
@@ -611,6 +758,7 @@ struct Model {
     zmat_apply(ctx, &j, 1, 1, N, dkx);
     lu_small_solve(ctx, dMpLU, dMpPiv, NN, dBfbtProfC, dBfbtRhs, N, 1, 1.0, 0, nullptr);
     build_reduced_lu(dBfbtRhs, dRedLU, dRedPiv);
+    if (fast) green_from_lu(ctx, dRedLU, dRedPiv, dRedG, N, Nk);
   }
   void to_complex(const double* in, double2* out, int count);
 
@@ -626,7 +774,9 @@ struct Model {
     bfbt_build();
     Op A = [&](const double2* v, double2* o) { schur_matvec(v, o); };
     Op M = [&](const double2* r, double2* z) {
-      lu_small_solve(ctx, dRedLU, dRedPiv, NN, r, z, N, Nk, 1.0, 1, nullptr);
+      ProfScope ps(ctx, "bfbt_precond");
+      if (fast) zop(dRedG, NN, r, z);      // (P_k^{-1} P) r
+      else lu_small_solve(ctx, dRedLU, dRedPiv, NN, r, z, N, Nk, 1.0, 1, nullptr);
     };
     FgmresResult fr = fgmres(A, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
     ctr.n_bfbt_solves++;
@@ -662,7 +812,7 @@ struct Model {
     SMC_CUDA(cudaMemcpyAsync(dLastEta, dEta, sizeof(double) * Nx * N, cudaMemcpyDeviceToDevice, stream));
     have_last_eta = true;
     eta_operator();
-    if (cfg.precond == SMC_PRECOND_BFBT) bfbt_solve(th, dSx);
+    if (cfg.precond == SMC_PRECOND_BFBT || fast) bfbt_solve(th, dSx);
     else legacy_solve(th, dSx);
     zop(dG, NN, dSx, psi);
     vec_axpby(ctx, om, make_double2(-1.0, 0.0), dSx, make_double2(0.0, 0.0), n);
@@ -780,6 +930,7 @@ struct Model {
 
   // ---------------------------------------------- implicit theta step
   void theta_matvec(const double2* v, double2* out) {
+    ProfScope ps(ctx, "theta_matvec");
     ZJob jobs[2];
     KFactor ik; ik.cre = 0.0; ik.cim = 1.0; ik.kpow = 1;
     jobs[0].Z = dV; jobs[0].X = v; jobs[0].Y = sp[9]; jobs[0].f = ik;
@@ -828,8 +979,15 @@ struct Model {
     LamSlot* Lp = &lam_lu(a0);
     double* LU = Lp->LU;
     int* piv = Lp->piv;
+    double* Gi = Lp->Ginv;
     Op M = [&](const double2* r, double2* z) {
-      lu_small_solve(ctx, LU, piv, NN, r, z, N, Nk, -1.0, 1, nullptr);
+      ProfScope ps(ctx, "theta_precond");
+      if (fast) {
+        KFactor mf; mf.cre = -1.0;
+        zop(Gi, NN, r, z, mf);               // -(A^{-1} P) r
+      } else {
+        lu_small_solve(ctx, LU, piv, NN, r, z, N, Nk, -1.0, 1, nullptr);
+      }
     };
     FgmresResult fr = fgmres(A, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
     // true relative residual of the accepted solution (implicit_theta.py:510-516)
@@ -883,7 +1041,10 @@ struct Model {
         double2* Zj = dKZ + (size_t)j * n;
         M(Vj, Zj);
         A(Zj, dKw);
-        mgs(ctx, dKV, j, n, dKw, dKh);
+        {
+          ProfScope ps(ctx, "fgmres_mgs");
+          mgs(ctx, dKV, j, n, dKw, dKh);
+        }
         SMC_CUDA(cudaMemcpyAsync(hv.data(), dKh, (j + 2) * sizeof(double2), cudaMemcpyDeviceToHost, stream));
         SMC_CUDA(cudaStreamSynchronize(stream));
         for (int i = 0; i <= j; ++i) Hij(i, j) = cplx(hv[i].x, hv[i].y);
@@ -1012,7 +1173,7 @@ void validate(const smc_config* c) {
   if (!(c->eta_min > 0) || !(c->eta_max > c->eta_min)) throw std::runtime_error("bad eta window");
   if (c->lag < 1 || c->max_K < 1 || c->K < 0) throw std::runtime_error("bad defect-correction settings");
   if (c->theta_restart < 1 || c->stokes_restart < 1) throw std::runtime_error("bad restart");
-  if (c->precision != SMC_FP64) throw std::runtime_error("only SMC_FP64 is built in this library");
+  if (c->precision != SMC_FP64 && c->precision != SMC_MIXED) throw std::runtime_error("unknown precision");
 }
 
 }  // namespace
@@ -1111,6 +1272,67 @@ int smc_march_adaptive(smc_handle* h, const double* in, double* out, int mem, do
     }
     copy_out(m, out, cur, mem, m.n * sizeof(double2));
     if (info) { info->steps = steps; info->t = t; info->dt = dt; }
+  })
+}
+
+int smc_set_state(smc_handle* h, const double* that, int mem) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_in(m, m.dS0, that, mem, m.n);
+    SMC_CUDA(cudaStreamSynchronize(m.stream));
+    m.resident_cur0 = true;
+    m.t_resident = 0.0;
+  })
+}
+
+int smc_get_state(smc_handle* h, double* out, int mem) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    copy_out(m, out, m.resident_cur0 ? m.dS0 : m.dS1, mem, m.n * sizeof(double2));
+  })
+}
+
+int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety, double dtmax,
+                smc_march_info* info) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    double2* cur = m.resident_cur0 ? m.dS0 : m.dS1;
+    double2* nxt = m.resident_cur0 ? m.dS1 : m.dS0;
+    double dt = NAN;
+    long long steps = 0;
+    while (m.t_resident < tstop && (max_steps <= 0 || steps < max_steps)) {
+      dt = m.production_dt(cur, safety, dtmax);
+      m.step(cur, nxt, dt);
+      std::swap(cur, nxt);
+      m.resident_cur0 = !m.resident_cur0;
+      m.t_resident += dt;
+      ++steps;
+    }
+    if (info) { info->steps = steps; info->t = m.t_resident; info->dt = dt; }
+  })
+}
+
+int smc_profile(smc_handle* h, int enable) {
+  SMC_GUARD(h, {
+    h->m.prof.reset();
+    h->m.prof.enabled = enable != 0;
+  })
+}
+
+int smc_profile_get(smc_handle* h, int slot, const char** name, double* ms, long long* launches,
+                    double* work, int* work_is_bytes) {
+  SMC_GUARD(h, {
+    smc::Profiler& p = h->m.prof;
+    p.resolve();
+    if (slot < 0 || slot >= smc::Profiler::MAXTAG || p.names[slot] == nullptr) {
+      *name = nullptr;
+    } else {
+      *name = p.names[slot];
+      *ms = p.ms[slot];
+      *launches = p.launches[slot];
+      *work = p.work[slot];
+      *work_is_bytes = p.work_is_bytes[slot];
+    }
   })
 }
 
@@ -1216,6 +1438,14 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v, double* 
     m.eta_operator();
     m.schur_matvec(m.dIn, m.dOut);
     copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
+  })
+}
+
+int smc_set_option(smc_handle* h, const char* key, double value) {
+  SMC_GUARD(h, {
+    std::string k(key ? key : "");
+    if (k == "dense_mult_eta") h->m.use_dense_mult = value != 0.0;
+    else throw std::runtime_error("unknown option " + k);
   })
 }
 

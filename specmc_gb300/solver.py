@@ -39,7 +39,7 @@ class GpuModel:
                  symmetrize=True, lag=16, K=3, defect_tol=1e-8, max_K=8,
                  eta_drift_tol=0.1, stokes_rtol=1e-8, theta_rtol=1e-10,
                  theta_maxiter=200, theta_restart=40, stokes_restart=80,
-                 stokes_maxiter=800, device=0, **_ignored):
+                 stokes_maxiter=800, device=0, form="plain", **_ignored):
         lib = _lib.load()
         c = _lib.SmcConfig()
         lib.smc_config_defaults(ctypes.byref(c))
@@ -60,6 +60,12 @@ class GpuModel:
         c.theta_maxiter, c.theta_restart = int(theta_maxiter), int(theta_restart)
         c.stokes_restart, c.stokes_maxiter = int(stokes_restart), int(stokes_maxiter)
         c.device = int(device)
+        form = str(form).lower()
+        if form not in ("plain", "mixed"):
+            raise ValueError("form must be 'plain' (FP64, the reference algorithm) or "
+                             "'mixed' (the fast form), got %r" % (form,))
+        c.precision = _lib.SMC_MIXED if form == "mixed" else _lib.SMC_FP64
+        self.form = form
         self._cfg = c
         self._lib = lib
         h = ctypes.c_void_p()
@@ -261,7 +267,7 @@ class GpuModel:
         raise AttributeError(name)
 
     def describe(self):
-        d = dict(mode=type(self).__name__, backend="gb300-fp64", Nx=self.Nx, Nz=self.Nz,
+        d = dict(mode=type(self).__name__, backend="gb300", form=self.form, Nx=self.Nx, Nz=self.Nz,
                  Ra=self.Ra, Lx=self.Lx, deta_T=self.deta_T,
                  internal_heating=self.internal_heating,
                  dissipation_number=self.dissipation_number)

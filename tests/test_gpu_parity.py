@@ -145,3 +145,47 @@ def test_oracle_parity_64x96_coupled(gb):
     d = m.diagnostics(s)
     assert abs(d["Nu_top"] - g["diag_Nu_top"].item()) <= 1e-8 * abs(g["diag_Nu_top"].item())
     assert abs(d["urms"] - g["diag_urms"].item()) <= 1e-8 * abs(g["diag_urms"].item())
+
+
+def test_pseudo_spectral_mult_eta_equals_dense(gb):
+    """The default pseudo-spectral mult_eta evaluates the same linear map as the
+    dense per-shift blocks of the reference (lagged_stokes.py:162-193)."""
+    import ctypes
+    from specmc_gb300 import _lib
+    api, CC = gb
+    rng = np.random.default_rng(5)
+    cfg = CC(viscosity_model="eta_T", Nx=64, Nz=96)
+    m_ps, m_dn = api.build_model(cfg), api.build_model(cfg)
+    _lib.check(m_dn._lib.smc_set_option(m_dn._h, b"dense_mult_eta", 1.0))
+    th = m_ps.seed(amp=0.3, m=1, n=1) + 0.05 * m_ps.seed(amp=1.0, m=3, n=2)
+    eta = np.empty((64, 96))
+    thc = np.ascontiguousarray(th)
+    _lib.check(m_ps._lib.smc_eta_of(m_ps._h, thc.ctypes.data_as(ctypes.c_void_p), 0,
+                                    eta.ctypes.data_as(ctypes.c_void_p)))
+    v = np.ascontiguousarray(rng.standard_normal((m_ps.Nk, 96)) + 1j * rng.standard_normal((m_ps.Nk, 96)))
+    outs = []
+    for m in (m_ps, m_dn):
+        o = np.empty_like(v)
+        _lib.check(m._lib.smc_schur_matvec(m._h, eta.ctypes.data_as(ctypes.c_void_p),
+                                           v.ctypes.data_as(ctypes.c_void_p),
+                                           o.ctypes.data_as(ctypes.c_void_p), 0))
+        outs.append(o)
+    assert _rel(outs[0], outs[1]) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["etaT_32x24", "heated_2to1_32x24", "arrhenius_32x24"])
+def test_mixed_form_matches_reference(gb, case):
+    """The fast form reproduces the reference's Nu and Vrms to 1e-6 relative."""
+    api, CC = gb
+    g = _load("march_%s.npz" % case)
+    m = api.build_model(CC(**_cfg_kw(g)), form="mixed")
+    s = np.array(g["that0"], copy=True)
+    for n in range(len(g["dts"])):
+        dt = api.production_dt(m, s)
+        assert abs(dt - g["dts"][n]) <= 1e-6 * g["dts"][n]
+        s = m.step(s, dt)
+    assert _rel(s, g["states"][-1]) < 1e-6
+    d = m.diagnostics(s)
+    for key in ("Nu_top", "urms", "Nu_energy"):
+        ref = g["diag_" + key].item()
+        assert abs(d[key] - ref) <= 1e-6 * abs(ref), (key, d[key], ref)

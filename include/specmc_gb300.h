@@ -191,6 +191,26 @@ int smc_shape(smc_handle* h, int* Nk, int* Nx, int* Nz, int* Np);
  * work after the handle's. */
 void* smc_stream(smc_handle* h);
 
+/* Grid synthesis that allocates nothing (no counterpart in the reference,
+ * which has no device memory at all).  For callers that cannot allocate
+ * device memory -- code whose memory is owned by a fixed arena that forbids
+ * foreign cudaMalloc calls, or time loops that cannot afford the device-wide
+ * synchronisation cudaMalloc/cudaFree may cause -- and therefore cannot hold a
+ * model handle.  Turns (Nx/2+1, Nz) complex coefficients `that_dev` (device
+ * memory) into grid values `grid_dev` (device memory, (Nx, Nz) or, with
+ * `padded` != 0, (2Nx, Nz) float64), exactly what smc_transform does for
+ * SMC_GRID / SMC_SYNTH_PAD.  The intermediate per-mode values live in one
+ * fixed library-wide device array of SMC_NOALLOC_MAX_MODES complex entries
+ * (8 MiB, held by every GPU that loads the library until exit); requests with
+ * (Nx/2+1)*Nz above that limit are rejected with an error.  Asynchronous on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream).  The first call
+ * on a device looks the array's address up (no allocation); make that first
+ * call before capturing a stream.  All calls share the array: calls that
+ * overlap on the GPU race; order them on one stream. */
+#define SMC_NOALLOC_MAX_MODES 524288
+int smc_grid_noalloc(const double* that_dev, double* grid_dev, int Nx, int Nz,
+                     int padded, void* stream);
+
 /* Message of the last hard error on the calling thread ("" if none). */
 const char* smc_last_error(void);
 

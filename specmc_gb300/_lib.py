@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libspecmc_gb300.so")
 SOURCES = ("smc_spectral.cu", "smc_dense.cu", "smc_schur.cu", "smc_krylov.cu",
-           "smc_pseudo.cu", "smc_runtime.cu")
+           "smc_pseudo.cu", "smc_noalloc.cu", "smc_runtime.cu")
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
               "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "-I", os.path.join(ROOT, "include")]
@@ -125,7 +125,8 @@ EXPORTED = ("smc_config_defaults", "smc_create", "smc_destroy", "smc_step", "smc
             "smc_stokes", "smc_velocity", "smc_project_mirror", "smc_transform",
             "smc_eta_of", "smc_schur_matvec", "smc_reset_history", "smc_counters_get",
             "smc_shape", "smc_stream", "smc_last_error", "smc_set_state", "smc_get_state",
-            "smc_advance", "smc_profile", "smc_profile_get", "smc_set_option")
+            "smc_advance", "smc_profile", "smc_profile_get", "smc_set_option",
+            "smc_grid_noalloc")
 
 _LIB = None
 
@@ -169,6 +170,7 @@ def load(path=None):
         "smc_advance": (i, [vp, d, ll, d, d, P(SmcMarchInfo)]),
         "smc_profile": (i, [vp, i]),
         "smc_set_option": (i, [vp, ctypes.c_char_p, d]),
+        "smc_grid_noalloc": (i, [vp, vp, i, i, i, vp]),
         "smc_profile_get": (i, [vp, i, P(ctypes.c_char_p), dp, P(ll), dp, P(i)]),
     }
     for name, (res, args) in sig.items():

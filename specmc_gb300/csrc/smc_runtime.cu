@@ -28,6 +28,7 @@ namespace smc {
 
 using cplx = std::complex<double>;
 static thread_local std::string g_last_error;
+void set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
 
 // --------------------------------------------------------------- host basis
 // CGL nodes, Chebyshev Vandermonde (chebvander recurrence), derivative

@@ -176,7 +176,13 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
  * one evaluation of each operator).  "dense_mult_eta" (0/1): evaluate
  * mult_eta with the dense per-shift Chebyshev product blocks
  * (stokes/lagged_stokes.py:162-193 term by term) instead of the default
- * pseudo-spectral form of the same linear map; used to cross-check them. */
+ * pseudo-spectral form of the same linear map; used to cross-check them.
+ * "schur_matvec_variant" (0/1/2, SMC_MIXED handles): which operator
+ * smc_schur_matvec applies -- 0 the plain one, 1 the fused FP64 operator of
+ * the fast form, 2 its FP32 inner-iteration operator.
+ * "inner_fp32" (0/1, SMC_MIXED handles, default 1): run the fast form's
+ * Krylov solves as FP32-operator inner FGMRES inside an FP64 refinement loop
+ * (1) or as plain FP64 FGMRES on the fused operators (0). */
 int smc_set_option(smc_handle* h, const char* key, double value);
 
 /* RBCImplicitTheta.reset_history (implicit_theta.py:601-606). */

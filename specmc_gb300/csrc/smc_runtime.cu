@@ -16,6 +16,7 @@
 #include <functional>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/specmc_gb300.h"
@@ -23,6 +24,7 @@
 #include "smc_route.cuh"
 #include "smc_schur.cuh"
 #include "smc_pseudo.cuh"
+#include "smc_fastops.cuh"
 
 namespace smc {
 
@@ -278,6 +280,16 @@ struct Model {
   // solve and explicit per-k inverse operators for the block preconditioners
   bool fast = false;
   double* dRedG = nullptr;
+  FusedSchur<double> fs64;
+  FusedSchur<float> fs32;
+  FusedTheta<double> ft64;
+  FusedTheta<float> ft32;
+  float *dE32 = nullptr, *dUx32 = nullptr, *dUz32 = nullptr;
+  double2 *dFsFv = nullptr, *dFsHv = nullptr, *dFtX = nullptr, *dFtA = nullptr;
+  double2 *dCgsPart = nullptr, *dRefR = nullptr, *dRefE = nullptr;
+  long long n_outer = 0;
+  int matvec_variant = 0;   // smc_schur_matvec: 0 plain, 1 fused FP64, 2 fused FP32
+  bool inner_fp32 = true;   // fast form: FP32 inner Krylov operators + FP64 refinement
 
   // ------------------------------------------------------------ utilities
   void sync_read(const double* d, int count) {
@@ -427,6 +439,12 @@ struct Model {
       dKw = mem.alloc<double2>(n); dKx = mem.alloc<double2>(n); dKr = mem.alloc<double2>(n);
       dKb = mem.alloc<double2>(n);
       dKh = mem.alloc<double2>(mmax + 2); dKy = mem.alloc<double2>(mmax + 2);
+      if (fast) {
+        dCgsPart = mem.alloc<double2>((size_t)2 * sms * (mmax + 2) + sms + 64);
+        dRefR = mem.alloc<double2>(n);
+        dRefE = mem.alloc<double2>(n);
+        setup_fused_theta();
+      }
       dRedLU = mem.alloc<double>(Nk * NN); dRedPiv = mem.alloc<int>(Nk * N);
       dRedG = mem.alloc<double>(Nk * NN);
       dM0 = mem.alloc<double>(NN); dDM0 = mem.alloc<double>(NN);
@@ -526,6 +544,7 @@ struct Model {
           dPsFv = mem.alloc<double2>((size_t)4 * Nk * Mz);
           dPsHv = mem.alloc<double2>((size_t)4 * Nk * Mz);
         }
+        if (fast) setup_fused_schur();
         dBfbtRhs = mem.alloc<double2>(N);
         dBfbtProfC = mem.alloc<double2>(N);
         // Galerkin mass matrix V^T W V and its LU (stokes/bfbt.py:74-84)
@@ -569,6 +588,131 @@ struct Model {
   void eta_pad_from_grid(const double* eta_grid, double* out) {
     analyze(eta_grid, Nx, sp[14], sp[15]);
     synth(sp[14], dV, KFactor(), out, Np, sp[15]);
+  }
+
+  // ------------------------------------------------ fast-form operators
+  template <class T>
+  T* dev_copy_as(const double* src, long long count) {
+    if (std::is_same<T, double>::value) {
+      T* p = mem.alloc<T>(count);
+      SMC_CUDA(cudaMemcpyAsync(p, src, count * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+      return p;
+    }
+    float* p = mem.alloc<float>(count);
+    to_float(ctx, src, p, count);
+    return reinterpret_cast<T*>(p);
+  }
+
+  void setup_fused_theta() {
+    for (int prec = 0; prec < 2; ++prec) {
+      if (prec == 0) {
+        ft64.Nk = Nk; ft64.N = N; ft64.Np = Np; ft64.kx = dkx; ft64.V64 = dV;
+        ft64.V = dV; ft64.VD = dVD; ft64.D2 = dD2; ft64.Vi = dVi; ft64.tw = dtwNp;
+      } else {
+        ft32.Nk = Nk; ft32.N = N; ft32.Np = Np; ft32.kx = dkx; ft32.V64 = dV;
+        ft32.V = dev_copy_as<float>(dV, NN); ft32.VD = dev_copy_as<float>(dVD, NN);
+        ft32.D2 = dev_copy_as<float>(dD2, NN); ft32.Vi = dev_copy_as<float>(dVi, NN);
+        ft32.tw = dev_copy_as<float>(reinterpret_cast<const double*>(dtwNp), 2LL * Np);
+      }
+    }
+    dUx32 = mem.alloc<float>((size_t)Np * N);
+    dUz32 = mem.alloc<float>((size_t)Np * N);
+    dFtX = mem.alloc<double2>((size_t)2 * n);
+    dFtA = mem.alloc<double2>(n);
+  }
+
+  void setup_fused_schur() {
+    const int Mz = psplan.Mz, L = psplan.L;
+    const long long MN = (long long)Mz * N;
+    double* D2G = mem.alloc<double>(Nk * NN);
+    double* DG = mem.alloc<double>(Nk * NN);
+    bgemm(ctx, false, dD2, 0, false, dG, NN, D2G, NN, N, Nk, 1.0);
+    bgemm(ctx, false, dD, 0, false, dG, NN, DG, NN, N, Nk, 1.0);
+    double* Z1 = mem.alloc<double>(Nk * MN);
+    double* Z2 = mem.alloc<double>(Nk * MN);
+    double* Z3 = mem.alloc<double>(Nk * MN);
+    rgemm_batched(ctx, psplan.Zf, 0, dG, NN, Z1, MN, Mz, N, N, Nk);
+    rgemm_batched(ctx, psplan.Zf, 0, D2G, NN, Z2, MN, Mz, N, N, Nk);
+    rgemm_batched(ctx, psplan.Zf, 0, DG, NN, Z3, MN, Mz, N, N, Nk);
+    double* D2Zi = mem.alloc<double>(MN);
+    double* DZi = mem.alloc<double>(MN);
+    rgemm_batched(ctx, dD2, 0, psplan.Zi, 0, D2Zi, 0, N, N, Mz, 1);
+    rgemm_batched(ctx, dD, 0, psplan.Zi, 0, DZi, 0, N, N, Mz, 1);
+    fs64.Nk = Nk; fs64.N = N; fs64.Mz = Mz; fs64.L = L; fs64.kx = dkx; fs64.V = dV;
+    fs64.Zf = psplan.Zf; fs64.Z1 = Z1; fs64.Z2 = Z2; fs64.Z3 = Z3;
+    fs64.Zi = psplan.Zi; fs64.D2Zi = D2Zi; fs64.DZi = DZi; fs64.tw = psplan.tw;
+    fs32.Nk = Nk; fs32.N = N; fs32.Mz = Mz; fs32.L = L; fs32.kx = dkx; fs32.V = dV;
+    fs32.Zf = dev_copy_as<float>(psplan.Zf, MN);
+    fs32.Z1 = dev_copy_as<float>(Z1, Nk * MN);
+    fs32.Z2 = dev_copy_as<float>(Z2, Nk * MN);
+    fs32.Z3 = dev_copy_as<float>(Z3, Nk * MN);
+    fs32.Zi = dev_copy_as<float>(psplan.Zi, MN);
+    fs32.D2Zi = dev_copy_as<float>(D2Zi, MN);
+    fs32.DZi = dev_copy_as<float>(DZi, MN);
+    fs32.tw = dev_copy_as<float>(reinterpret_cast<const double*>(psplan.tw), 2LL * L);
+    dE32 = mem.alloc<float>((size_t)L * Mz);
+    dFsFv = mem.alloc<double2>((size_t)4 * Nk * Mz);
+    dFsHv = mem.alloc<double2>((size_t)4 * Nk * Mz);
+  }
+
+  void schur_matvec_fast(const double2* v, double2* out, bool fp32) {
+    if (fp32) {
+      ProfScope ps(ctx, "schur_matvec_f32", schur_ps_flops(), 0);
+      fused_schur_matvec(ctx, fs32, dE32, v, out, dFsFv, dFsHv);
+    } else {
+      ProfScope ps(ctx, "schur_matvec_f64", schur_ps_flops(), 0);
+      fused_schur_matvec(ctx, fs64, dPsE, v, out, dFsFv, dFsHv);
+    }
+  }
+
+  // algorithmic flops of one fused pseudo-spectral Schur matvec
+  double schur_ps_flops() const {
+    const double Mz = psplan.Mz, L = psplan.L, nk = Nk, nz = N;
+    double per_field = 4.0 * nk * Mz * nz + 8.0 * L * Mz * (nk - 1) + 2.0 * L * Mz +
+                       8.0 * nk * L * Mz;
+    return 4.0 * per_field + 3.0 * 4.0 * nk * nz * Mz;
+  }
+
+  void theta_matvec_fast(const double2* v, double2* out, bool fp32) {
+    if (fp32) {
+      ProfScope ps(ctx, "theta_matvec_f32");
+      fused_theta_matvec(ctx, ft32, dUx32, dUz32, a0, v, out, dFtX, dFtA);
+    } else {
+      ProfScope ps(ctx, "theta_matvec_f64");
+      fused_theta_matvec(ctx, ft64, gr[0], gr[1], a0, v, out, dFtX, dFtA);
+    }
+  }
+
+  // FGMRES as iterative refinement: inner FGMRES on the FP32 operator, outer
+  // residual r = b - A x in FP64; stops when ||r|| <= rtol ||b||.  Returns
+  // (info, inner iterations) and the final true relative residual.
+  FgmresResult fgmres_refined(const Op& A64, const Op& A32, const Op& M, const double2* b,
+                              double2* x, double rtol, int restart, int maxiter, double* true_res) {
+    FgmresResult res;
+    vec_zero(ctx, x, n * sizeof(double2));
+    const double bn = norm(b);
+    const double tol = rtol * bn;
+    vec_copy(ctx, dRefR, b, n);
+    double beta = bn;
+    int total = 0;
+    res.info = 1;
+    for (int outer = 0; outer < 12; ++outer) {
+      if (beta <= tol) { res.info = 0; break; }
+      if (total >= maxiter) break;
+      const double inner_rtol = std::max(0.3 * tol / beta, 2e-6);
+      FgmresResult fr = fgmres(A32, M, dRefR, dRefE, inner_rtol, restart, maxiter - total);
+      total += fr.iters;
+      vec_axpby(ctx, x, make_double2(1.0, 0.0), dRefE, make_double2(1.0, 0.0), n);
+      A64(x, dRefR);
+      vec_axpby(ctx, dRefR, make_double2(1.0, 0.0), b, make_double2(-1.0, 0.0), n);
+      beta = norm(dRefR);
+      n_outer++;
+      if (fr.iters == 0 && beta > tol) break;     // no progress possible
+    }
+    if (beta <= tol) res.info = 0;
+    res.iters = total;
+    if (true_res) *true_res = beta / std::max(bn, 1e-300);
+    return res;
   }
 
   // ------------------------------------------------------ stokes routes
@@ -635,6 +779,7 @@ struct Model {
     analyze(dEta, Nx, dEtaC, sp[2]);
     build_mult_mats(ctx, dEtaC, dMd, Nk, N);
     ps_eta_grid(ctx, psplan, dEtaC, dPsFv, dPsE);
+    if (fast) to_float(ctx, dPsE, dE32, (long long)psplan.L * psplan.Mz);
   }
 
   // FreeSchurOperator.matvec at the current Md (lagged_stokes.py:202-220)
@@ -776,13 +921,29 @@ struct Model {
     Op A = [&](const double2* v, double2* o) { schur_matvec(v, o); };
     Op M = [&](const double2* r, double2* z) {
       ProfScope ps(ctx, "bfbt_precond");
-      if (fast) zop(dRedG, NN, r, z);      // (P_k^{-1} P) r
+      if (fast) kgemv(ctx, dRedG, r, z, Nk, N, 1.0);      // (P_k^{-1} P) r
       else lu_small_solve(ctx, dRedLU, dRedPiv, NN, r, z, N, Nk, 1.0, 1, nullptr);
     };
-    FgmresResult fr = fgmres(A, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
+    FgmresResult fr;
+    double res;
+    if (fast) {
+      Op A64 = [&](const double2* v, double2* o) { schur_matvec_fast(v, o, false); };
+      Op A32 = [&](const double2* v, double2* o) { schur_matvec_fast(v, o, true); };
+      if (inner_fp32) {
+        fr = fgmres_refined(A64, A32, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart,
+                            cfg.stokes_maxiter, &res);
+      } else {
+        fr = fgmres(A64, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
+        schur_matvec_fast(x, dSAx, false);
+        vec_axpby(ctx, dSAx, make_double2(1.0, 0.0), dSb, make_double2(-1.0, 0.0), n);
+        res = norm(dSAx) / std::max(norm(dSb), 1e-300);
+      }
+    } else {
+      fr = fgmres(A, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
+      res = schur_true_res(dSb, x);
+    }
     ctr.n_bfbt_solves++;
     ctr.n_bfbt_iters += fr.iters;
-    double res = schur_true_res(dSb, x);
     ctr.last_bfbt_true_res = res;
     ctr.last_K = 0;
     if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
@@ -984,18 +1145,36 @@ struct Model {
     Op M = [&](const double2* r, double2* z) {
       ProfScope ps(ctx, "theta_precond");
       if (fast) {
-        KFactor mf; mf.cre = -1.0;
-        zop(Gi, NN, r, z, mf);               // -(A^{-1} P) r
+        kgemv(ctx, Gi, r, z, Nk, N, -1.0);   // -(A^{-1} P) r
       } else {
         lu_small_solve(ctx, LU, piv, NN, r, z, N, Nk, -1.0, 1, nullptr);
       }
     };
-    FgmresResult fr = fgmres(A, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
-    // true relative residual of the accepted solution (implicit_theta.py:510-516)
-    theta_matvec(dRhs, sp[13]);
-    vec_axpby(ctx, sp[13], make_double2(1.0, 0.0), dKb, make_double2(-1.0, 0.0), n);
-    double bn = std::max(norm(dKb), 1e-300);
-    ctr.theta_last_res = norm(sp[13]) / bn;
+    FgmresResult fr;
+    if (fast) {
+      to_float(ctx, gr[0], dUx32, (long long)Np * N);
+      to_float(ctx, gr[1], dUz32, (long long)Np * N);
+      Op A64 = [&](const double2* v, double2* o) { theta_matvec_fast(v, o, false); };
+      Op A32 = [&](const double2* v, double2* o) { theta_matvec_fast(v, o, true); };
+      double tr = 0.0;
+      if (inner_fp32) {
+        fr = fgmres_refined(A64, A32, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart,
+                            cfg.theta_maxiter, &tr);
+      } else {
+        fr = fgmres(A64, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
+        theta_matvec_fast(dRhs, sp[13], false);
+        vec_axpby(ctx, sp[13], make_double2(1.0, 0.0), dKb, make_double2(-1.0, 0.0), n);
+        tr = norm(sp[13]) / std::max(norm(dKb), 1e-300);
+      }
+      ctr.theta_last_res = tr;
+    } else {
+      fr = fgmres(A, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
+      // true relative residual of the accepted solution (implicit_theta.py:510-516)
+      theta_matvec(dRhs, sp[13]);
+      vec_axpby(ctx, sp[13], make_double2(1.0, 0.0), dKb, make_double2(-1.0, 0.0), n);
+      double bn = std::max(norm(dKb), 1e-300);
+      ctr.theta_last_res = norm(sp[13]) / bn;
+    }
     ctr.theta_last_iters = fr.iters;
     ctr.n_theta_iters += fr.iters;
     ctr.n_theta_solves++;
@@ -1042,7 +1221,10 @@ struct Model {
         double2* Zj = dKZ + (size_t)j * n;
         M(Vj, Zj);
         A(Zj, dKw);
-        {
+        if (fast) {
+          ProfScope ps(ctx, "fgmres_cgs2");
+          cgs2(ctx, dKV, j, n, dKw, dKh, dCgsPart);
+        } else {
           ProfScope ps(ctx, "fgmres_mgs");
           mgs(ctx, dKV, j, n, dKw, dKh);
         }
@@ -1437,7 +1619,8 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v, double* 
     SMC_CUDA(cudaMemcpyAsync(m.dEta, eta, sizeof(double) * m.Nx * m.N, kin, m.stream));
     copy_in(m, m.dIn, v, mem, m.n);
     m.eta_operator();
-    m.schur_matvec(m.dIn, m.dOut);
+    if (m.matvec_variant == 0) m.schur_matvec(m.dIn, m.dOut);
+    else m.schur_matvec_fast(m.dIn, m.dOut, m.matvec_variant == 2);
     copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
   })
 }
@@ -1446,7 +1629,14 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
   SMC_GUARD(h, {
     std::string k(key ? key : "");
     if (k == "dense_mult_eta") h->m.use_dense_mult = value != 0.0;
-    else throw std::runtime_error("unknown option " + k);
+    else if (k == "schur_matvec_variant") {
+      int v = (int)value;
+      if (v < 0 || v > 2) throw std::runtime_error("schur_matvec_variant must be 0, 1 or 2");
+      if (v > 0 && !h->m.fast) throw std::runtime_error("fused variants need a SMC_MIXED handle");
+      h->m.matvec_variant = v;
+    } else if (k == "inner_fp32") {
+      h->m.inner_fp32 = value != 0.0;
+    } else throw std::runtime_error("unknown option " + k);
   })
 }
 

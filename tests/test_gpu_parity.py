@@ -189,3 +189,30 @@ def test_mixed_form_matches_reference(gb, case):
     for key in ("Nu_top", "urms", "Nu_energy"):
         ref = g["diag_" + key].item()
         assert abs(d[key] - ref) <= 1e-6 * abs(ref), (key, d[key], ref)
+
+
+def test_fused_schur_matvec_variants(gb):
+    """The fast form's fused FP64 operator equals the plain Schur matvec to
+    roundoff; its FP32 inner-iteration operator to FP32 accuracy."""
+    import ctypes
+    from specmc_gb300 import _lib
+    api, CC = gb
+    rng = np.random.default_rng(9)
+    cfg = CC(viscosity_model="eta_T", Nx=64, Nz=96)
+    m = api.build_model(cfg, form="mixed")
+    th = m.seed(amp=0.3, m=1, n=1) + 0.05 * m.seed(amp=1.0, m=3, n=2)
+    eta = np.empty((64, 96))
+    thc = np.ascontiguousarray(th)
+    _lib.check(m._lib.smc_eta_of(m._h, thc.ctypes.data_as(ctypes.c_void_p), 0,
+                                 eta.ctypes.data_as(ctypes.c_void_p)))
+    v = np.ascontiguousarray(rng.standard_normal((m.Nk, 96)) + 1j * rng.standard_normal((m.Nk, 96)))
+    outs = []
+    for variant in (0, 1, 2):
+        _lib.check(m._lib.smc_set_option(m._h, b"schur_matvec_variant", float(variant)))
+        o = np.empty_like(v)
+        _lib.check(m._lib.smc_schur_matvec(m._h, eta.ctypes.data_as(ctypes.c_void_p),
+                                           v.ctypes.data_as(ctypes.c_void_p),
+                                           o.ctypes.data_as(ctypes.c_void_p), 0))
+        outs.append(o)
+    assert _rel(outs[1], outs[0]) < 1e-11
+    assert _rel(outs[2], outs[0]) < 1e-4

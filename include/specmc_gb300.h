@@ -182,7 +182,10 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
  * the fast form, 2 its FP32 inner-iteration operator.
  * "inner_fp32" (0/1, SMC_MIXED handles, default 1): run the fast form's
  * Krylov solves as FP32-operator inner FGMRES inside an FP64 refinement loop
- * (1) or as plain FP64 FGMRES on the fused operators (0). */
+ * (1) or as plain FP64 FGMRES on the fused operators (0).
+ * "krylov_engine" (0/1, SMC_MIXED handles, default 1): run each of those
+ * FGMRES solves in one persistent cooperative kernel on the device (1) or
+ * with host-side control per iteration (0). */
 int smc_set_option(smc_handle* h, const char* key, double value);
 
 /* RBCImplicitTheta.reset_history (implicit_theta.py:601-606). */

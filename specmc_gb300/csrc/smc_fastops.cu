@@ -16,6 +16,8 @@
 // double2.
 #include <cooperative_groups.h>
 
+#include <type_traits>
+
 #include "smc_internal.cuh"
 #include "smc_fastops.cuh"
 
@@ -32,7 +34,7 @@ template <> struct C2<float> { using type = float2; };
 //   b=0: Zf (shared), c=1 ; b=1: Z1_k, c=2k^2 ; b=2: Z2_k, c=1 ; b=3: Z3_k, c=k
 // one warp per output (b, k, s); lanes split q (coalesced rows of Z)
 template <class T>
-__global__ void smc_fs_fwd_kernel(const double2* __restrict__ v, const T* __restrict__ Zf,
+__global__ void smc_fs_fwd_kernel(const typename C2<T>::type* __restrict__ v, const T* __restrict__ Zf,
                                   const T* __restrict__ Z1, const T* __restrict__ Z2,
                                   const T* __restrict__ Z3, const double* __restrict__ kx, int Nk,
                                   int N, int Mz, typename C2<T>::type* __restrict__ Fv) {
@@ -46,13 +48,13 @@ __global__ void smc_fs_fwd_kernel(const double2* __restrict__ v, const T* __rest
   const long long MN = (long long)Mz * N;
   const T* Z = (b == 0) ? Zf : ((b == 1 ? Z1 : (b == 2 ? Z2 : Z3)) + (long long)k * MN);
   const T* zr = Z + (long long)s * N;
-  const double2* vk = v + (long long)k * N;
+  const typename C2<T>::type* vk = v + (long long)k * N;
   T sr = 0, si = 0;
   for (int q = lane; q < N; q += 32) {
     const T w = zr[q];
-    const double2 x = vk[q];
-    sr += w * (T)x.x;
-    si += w * (T)x.y;
+    const typename C2<T>::type x = vk[q];
+    sr += w * x.x;
+    si += w * x.y;
   }
   for (int d = 16; d > 0; d >>= 1) {
     sr += __shfl_xor_sync(0xffffffffu, sr, d);
@@ -102,21 +104,32 @@ __global__ void smc_fs_x_kernel(const typename C2<T>::type* __restrict__ Fv, con
   }
   __syncthreads();
   const T invL = (T)1 / (T)L;
-  for (int i = tid; i < Nk; i += nt) {
+  // 4 consecutive lanes per output mode i, each summing every 4th point
+  for (int base = 0; base < Nk; base += nt / 4) {
+    const int i = base + tid / 4, part = tid & 3;
     T hr = 0, hi = 0;
-    int idx = 0;
-    for (int l = 0; l < L; ++l) {
-      const CT t = W[idx];
-      const CT p = P[l];
-      hr += p.x * t.x + p.y * t.y;
-      hi += p.y * t.x - p.x * t.y;
-      idx += i;
-      if (idx >= L) idx -= L;
+    if (i < Nk) {
+      int idx = (int)(((long long)i * part) % L);
+      const int step = (int)(((long long)i * 4) % L);
+      for (int l = part; l < L; l += 4) {
+        const CT t = W[idx];
+        const CT p = P[l];
+        hr += p.x * t.x + p.y * t.y;
+        hi += p.y * t.x - p.x * t.y;
+        idx += step;
+        if (idx >= L) idx -= L;
+      }
     }
-    CT o;
-    o.x = hr * invL;
-    o.y = hi * invL;
-    Hv[((long long)b * Nk + i) * Mz + s] = o;
+    hr += __shfl_xor_sync(0xffffffffu, hr, 1);
+    hi += __shfl_xor_sync(0xffffffffu, hi, 1);
+    hr += __shfl_xor_sync(0xffffffffu, hr, 2);
+    hi += __shfl_xor_sync(0xffffffffu, hi, 2);
+    if (i < Nk && part == 0) {
+      CT o;
+      o.x = hr * invL;
+      o.y = hi * invL;
+      Hv[((long long)b * Nk + i) * Mz + s] = o;
+    }
   }
 }
 
@@ -180,12 +193,30 @@ __global__ void smc_fs_out_kernel(const typename C2<T>::type* __restrict__ Hv, c
   }
 }
 
+__global__ void smc_to_float2_kernel(const double2* __restrict__ in, float2* __restrict__ out,
+                                     long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+
 template <class T>
 void fused_schur_matvec_t(const Ctx& c, const FusedSchur<T>& op, const T* E, const double2* v,
                           double2* out, void* Fv, void* Hv) {
   using CT = typename C2<T>::type;
   const long long nf = 4LL * op.Nk * op.Mz;
-  smc_fs_fwd_kernel<T><<<ceil_div(nf, 8), 256, 0, c.s>>>(v, op.Zf, op.Z1, op.Z2, op.Z3, op.kx, op.Nk,
+  const CT* vin;
+  if (std::is_same<T, float>::value) {
+    // one FP64 -> FP32 conversion of the Krylov vector (the FP64 pipe
+    // issues conversions; doing it once keeps the operator on FP32 units)
+    float2* v32 = reinterpret_cast<float2*>(op.vbuf);
+    const long long nv = (long long)op.Nk * op.N;
+    smc_to_float2_kernel<<<ceil_div(nv, 256), 256, 0, c.s>>>(v, v32, nv);
+    SMC_LAUNCH_CHECK(c);
+    vin = reinterpret_cast<const CT*>(v32);
+  } else {
+    vin = reinterpret_cast<const CT*>(v);
+  }
+  smc_fs_fwd_kernel<T><<<ceil_div(nf, 8), 256, 0, c.s>>>(vin, op.Zf, op.Z1, op.Z2, op.Z3, op.kx, op.Nk,
                                                         op.N, op.Mz, (CT*)Fv);
   SMC_LAUNCH_CHECK(c);
   dim3 g2(op.Mz, 4);

@@ -13,6 +13,7 @@ struct FusedSchur {
   const void* tw = nullptr;      // L twiddles, complex T
   const double* kx = nullptr;
   const double* V = nullptr;     // FP64 basis (tau rows)
+  void* vbuf = nullptr;          // Nk*N complex T scratch (FP32 copy of the input)
 };
 
 // temperature matvec (T = double or float)

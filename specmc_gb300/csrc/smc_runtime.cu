@@ -25,6 +25,7 @@
 #include "smc_schur.cuh"
 #include "smc_pseudo.cuh"
 #include "smc_fastops.cuh"
+#include "smc_engine.cuh"
 
 namespace smc {
 
@@ -290,6 +291,11 @@ struct Model {
   long long n_outer = 0;
   int matvec_variant = 0;   // smc_schur_matvec: 0 plain, 1 fused FP64, 2 fused FP32
   bool inner_fp32 = true;   // fast form: FP32 inner Krylov operators + FP64 refinement
+  bool use_engine = true;   // fast form: Krylov solves in the persistent on-device engine
+  EngineIO eio;
+  float* dKx32 = nullptr;
+  float2* dTheta32 = nullptr;
+  int* dEngInt = nullptr;
 
   // ------------------------------------------------------------ utilities
   void sync_read(const double* d, int count) {
@@ -444,6 +450,23 @@ struct Model {
         dRefR = mem.alloc<double2>(n);
         dRefE = mem.alloc<double2>(n);
         setup_fused_theta();
+        // persistent-engine workspace
+        const int mr = mmax + 1, gmax = 2 * sms;
+        eio.max_grid = gmax;
+        eio.H = mem.alloc<double2>((size_t)mr * mr);
+        eio.g = mem.alloc<double2>(mr + 1);
+        eio.sn = mem.alloc<double2>(mr + 1);
+        eio.y = mem.alloc<double2>(mr + 1);
+        eio.cs = mem.alloc<double>(mr + 1);
+        eio.part = mem.alloc<double2>((size_t)2 * gmax * (mr + 1));
+        eio.npart = mem.alloc<double>(gmax);
+        dEngInt = mem.alloc<int>(8);
+        eio.flag = dEngInt;
+        eio.result = dEngInt + 4;
+        eio.V = dKV; eio.Z = dKZ; eio.w = dKw; eio.r = dKr;
+        dKx32 = mem.alloc<float>(Nk);
+        to_float(ctx, dkx, dKx32, Nk);
+        dTheta32 = mem.alloc<float2>(n);
       }
       dRedLU = mem.alloc<double>(Nk * NN); dRedPiv = mem.alloc<int>(Nk * N);
       dRedG = mem.alloc<double>(Nk * NN);
@@ -650,6 +673,7 @@ struct Model {
     fs32.D2Zi = dev_copy_as<float>(D2Zi, MN);
     fs32.DZi = dev_copy_as<float>(DZi, MN);
     fs32.tw = dev_copy_as<float>(reinterpret_cast<const double*>(psplan.tw), 2LL * L);
+    fs32.vbuf = mem.alloc<float2>(n);
     dE32 = mem.alloc<float>((size_t)L * Mz);
     dFsFv = mem.alloc<double2>((size_t)4 * Nk * Mz);
     dFsHv = mem.alloc<double2>((size_t)4 * Nk * Mz);
@@ -683,11 +707,56 @@ struct Model {
     }
   }
 
+  // one FGMRES solve in the persistent engine; kind 0 = Schur, 1 = theta
+  FgmresResult engine_solve(int kind, bool fp32, const double2* b, double2* x, double rtol,
+                            int restart, int maxiter, const double* Gp, double palpha) {
+    ProfScope ps(ctx, kind == 0 ? "engine_stokes" : "engine_theta");
+    EngineOps op;
+    op.kind = kind; op.Nk = Nk; op.N = N; op.kx = dkx; op.V64 = dV;
+    op.Gp = Gp; op.palpha = palpha;
+    op.kxT = fp32 ? (const void*)dKx32 : (const void*)dkx;
+    if (kind == 0) {
+      op.Mz = psplan.Mz; op.L = psplan.L;
+      if (fp32) {
+        op.Zf = fs32.Zf; op.Z1 = fs32.Z1; op.Z2 = fs32.Z2; op.Z3 = fs32.Z3;
+        op.Zi = fs32.Zi; op.D2Zi = fs32.D2Zi; op.DZi = fs32.DZi; op.E = dE32; op.twS = fs32.tw;
+        op.vT = fs32.vbuf;
+      } else {
+        op.Zf = fs64.Zf; op.Z1 = fs64.Z1; op.Z2 = fs64.Z2; op.Z3 = fs64.Z3;
+        op.Zi = fs64.Zi; op.D2Zi = fs64.D2Zi; op.DZi = fs64.DZi; op.E = dPsE; op.twS = fs64.tw;
+      }
+      op.Fv = dFsFv; op.Hv = dFsHv;
+    } else {
+      op.Np = Np; op.a0 = a0;
+      if (fp32) {
+        op.tV = ft32.V; op.tVD = ft32.VD; op.tD2 = ft32.D2; op.tVi = ft32.Vi; op.twT = ft32.tw;
+        op.ux = dUx32; op.uz = dUz32; op.vT = dTheta32;
+      } else {
+        op.tV = ft64.V; op.tVD = ft64.VD; op.tD2 = ft64.D2; op.tVi = ft64.Vi; op.twT = ft64.tw;
+        op.ux = gr[0]; op.uz = gr[1];
+      }
+      op.X = dFtX; op.A = dFtA;
+    }
+    EngineIO io = eio;
+    io.b = b; io.x = x; io.rtol = rtol; io.n = n;
+    io.restart = std::max(1, std::min(restart, mmax));
+    io.maxiter = maxiter;
+    fgmres_engine(ctx, op, io, fp32);
+    int res[2];
+    SMC_CUDA(cudaMemcpyAsync(res, eio.result, sizeof(res), cudaMemcpyDeviceToHost, stream));
+    SMC_CUDA(cudaStreamSynchronize(stream));
+    FgmresResult fr;
+    fr.info = res[0];
+    fr.iters = res[1];
+    return fr;
+  }
+
   // FGMRES as iterative refinement: inner FGMRES on the FP32 operator, outer
   // residual r = b - A x in FP64; stops when ||r|| <= rtol ||b||.  Returns
   // (info, inner iterations) and the final true relative residual.
-  FgmresResult fgmres_refined(const Op& A64, const Op& A32, const Op& M, const double2* b,
-                              double2* x, double rtol, int restart, int maxiter, double* true_res) {
+  using InnerSolve = std::function<FgmresResult(const double2*, double2*, double, int)>;
+  FgmresResult fgmres_refined(const Op& A64, const InnerSolve& inner, const double2* b,
+                              double2* x, double rtol, int maxiter, double* true_res) {
     FgmresResult res;
     vec_zero(ctx, x, n * sizeof(double2));
     const double bn = norm(b);
@@ -700,7 +769,7 @@ struct Model {
       if (beta <= tol) { res.info = 0; break; }
       if (total >= maxiter) break;
       const double inner_rtol = std::max(0.3 * tol / beta, 2e-6);
-      FgmresResult fr = fgmres(A32, M, dRefR, dRefE, inner_rtol, restart, maxiter - total);
+      FgmresResult fr = inner(dRefR, dRefE, inner_rtol, maxiter - total);
       total += fr.iters;
       vec_axpby(ctx, x, make_double2(1.0, 0.0), dRefE, make_double2(1.0, 0.0), n);
       A64(x, dRefR);
@@ -896,13 +965,38 @@ struct Model {
     }
   }
 
-  // spectral BFBT blocks from the harmonic-mean profile (stokes/bfbt.py:111-191)
+  // spectral BFBT blocks from the harmonic-mean profile (stokes/bfbt.py:111-191).
+  // The fast form keeps the blocks while the Galerkin profile stays within
+  // 2% (max-norm, relative) of the one they were built from and for at most
+  // 16 solves: the blocks only precondition, so the solution is unchanged.
+  std::vector<double> bfbt_prof_h, bfbt_prof_new;
+  int bfbt_age = 1 << 30;
+  long long n_bfbt_builds = 0;
   void bfbt_build() {
     harm_profile_rhs(ctx, dEta, Nx, N, dwq, dBfbtHw);
     to_complex(dBfbtHw, dBfbtRhs, N);
     ZJob j; j.Z = dVT; j.X = dBfbtRhs; j.Y = dBfbtProfC;     // V^T (w g)
     zmat_apply(ctx, &j, 1, 1, N, dkx);
     lu_small_solve(ctx, dMpLU, dMpPiv, NN, dBfbtProfC, dBfbtRhs, N, 1, 1.0, 0, nullptr);
+    if (fast) {
+      bfbt_prof_new.resize(2 * N);
+      SMC_CUDA(cudaMemcpyAsync(bfbt_prof_new.data(), dBfbtRhs, N * sizeof(double2),
+                               cudaMemcpyDeviceToHost, stream));
+      SMC_CUDA(cudaStreamSynchronize(stream));
+      bool reuse = !bfbt_prof_h.empty() && bfbt_age < 16;
+      if (reuse) {
+        double mx = 0.0, md = 0.0;
+        for (int q = 0; q < N; ++q) {
+          mx = std::max(mx, std::fabs(bfbt_prof_h[2 * q]));
+          md = std::max(md, std::fabs(bfbt_prof_new[2 * q] - bfbt_prof_h[2 * q]));
+        }
+        reuse = std::isfinite(md) && md <= 0.02 * mx;
+      }
+      if (reuse) { ++bfbt_age; return; }
+      bfbt_prof_h = bfbt_prof_new;
+      bfbt_age = 1;
+    }
+    ++n_bfbt_builds;
     build_reduced_lu(dBfbtRhs, dRedLU, dRedPiv);
     if (fast) green_from_lu(ctx, dRedLU, dRedPiv, dRedG, N, Nk);
   }
@@ -930,10 +1024,18 @@ struct Model {
       Op A64 = [&](const double2* v, double2* o) { schur_matvec_fast(v, o, false); };
       Op A32 = [&](const double2* v, double2* o) { schur_matvec_fast(v, o, true); };
       if (inner_fp32) {
-        fr = fgmres_refined(A64, A32, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart,
-                            cfg.stokes_maxiter, &res);
+        InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
+          if (use_engine)
+            return engine_solve(0, true, r, e, tol, cfg.stokes_restart, mi, dRedG, 1.0);
+          return fgmres(A32, M, r, e, tol, cfg.stokes_restart, mi);
+        };
+        fr = fgmres_refined(A64, inner, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, &res);
       } else {
-        fr = fgmres(A64, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
+        if (use_engine)
+          fr = engine_solve(0, false, dSb, x, cfg.stokes_rtol, cfg.stokes_restart,
+                            cfg.stokes_maxiter, dRedG, 1.0);
+        else
+          fr = fgmres(A64, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
         schur_matvec_fast(x, dSAx, false);
         vec_axpby(ctx, dSAx, make_double2(1.0, 0.0), dSb, make_double2(-1.0, 0.0), n);
         res = norm(dSAx) / std::max(norm(dSb), 1e-300);
@@ -1158,10 +1260,18 @@ struct Model {
       Op A32 = [&](const double2* v, double2* o) { theta_matvec_fast(v, o, true); };
       double tr = 0.0;
       if (inner_fp32) {
-        fr = fgmres_refined(A64, A32, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart,
-                            cfg.theta_maxiter, &tr);
+        InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
+          if (use_engine)
+            return engine_solve(1, true, r, e, tol, cfg.theta_restart, mi, Gi, -1.0);
+          return fgmres(A32, M, r, e, tol, cfg.theta_restart, mi);
+        };
+        fr = fgmres_refined(A64, inner, dKb, dRhs, cfg.theta_rtol, cfg.theta_maxiter, &tr);
       } else {
-        fr = fgmres(A64, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
+        if (use_engine)
+          fr = engine_solve(1, false, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart,
+                            cfg.theta_maxiter, Gi, -1.0);
+        else
+          fr = fgmres(A64, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
         theta_matvec_fast(dRhs, sp[13], false);
         vec_axpby(ctx, sp[13], make_double2(1.0, 0.0), dKb, make_double2(-1.0, 0.0), n);
         tr = norm(sp[13]) / std::max(norm(dKb), 1e-300);
@@ -1636,6 +1746,8 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
       h->m.matvec_variant = v;
     } else if (k == "inner_fp32") {
       h->m.inner_fp32 = value != 0.0;
+    } else if (k == "krylov_engine") {
+      h->m.use_engine = value != 0.0;
     } else throw std::runtime_error("unknown option " + k);
   })
 }

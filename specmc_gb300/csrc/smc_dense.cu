@@ -192,11 +192,17 @@ static constexpr int ZNB = 32;     // panel width
 static constexpr int ZROWCHUNK = 32;
 
 // rows of the column range [r_lo, n) owned by CTA b: chunks of 32 rows dealt
-// round-robin over the grid
-#define SMC_FOR_OWNED_ROWS(r, r_lo, n, b, G)                                   \
-  for (int ch_ = ((r_lo) / ZROWCHUNK + (((b) - ((r_lo) / ZROWCHUNK) % (G)) + (G)) % (G)); \
-       ch_ * ZROWCHUNK < (n); ch_ += (G))                                      \
-    for (int r = max(ch_ * ZROWCHUNK, (r_lo)); r < min((ch_ + 1) * ZROWCHUNK, (n)); ++r)
+// round-robin over the grid (chunk ch belongs to CTA ch mod G).  Inside the
+// CTA, warp w takes the CTA's chunks w, w + nwarps, ...; lane l handles row
+// 32 ch + l, so a warp's loads of one column are one coalesced 512-byte line
+// and a given row is always handled by the same thread during a panel.
+// The body runs once per (chunk, lane); `continue` skips that row.
+#define SMC_FOR_OWNED_ROW(r, r_lo, n, b, G, warp, nwarps, lane)                          \
+  for (int ch_ = ((r_lo) / ZROWCHUNK + (((b) - ((r_lo) / ZROWCHUNK) % (G)) + (G)) % (G)) + \
+                 (warp) * (G);                                                           \
+       ch_ * ZROWCHUNK < (n); ch_ += (G) * (nwarps))                                     \
+    for (int r = ch_ * ZROWCHUNK + (lane), once_ = 1; once_; once_ = 0)                  \
+      if (r >= (r_lo) && r < (n))
 
 __device__ __forceinline__ void argmax_merge(double& v, int& i, double ov, int oi) {
   if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
@@ -225,16 +231,12 @@ __global__ void smc_zlu_panel_kernel(double2* __restrict__ A, int n, int p0, int
   // mark owned rows not done; local argmax of the first column
   double best = -1.0;
   int bi = n;
-  {
-    int cnt = 0;
-    SMC_FOR_OWNED_ROWS(r, p0, n, b, G) {
-      if ((cnt++ % nt) == tid) {
-        done[r] = 0;
-        double v = cabs1(A[r + (long long)p0 * n]);
-        if (v != v) v = INFINITY;
-        argmax_merge(best, bi, v, r);
-      }
-    }
+  const int nwarps = nt >> 5;
+  SMC_FOR_OWNED_ROW(r, p0, n, b, G, warp, nwarps, lane) {
+    done[r] = 0;
+    double v = cabs1(A[r + (long long)p0 * n]);
+    if (v != v) v = INFINITY;
+    argmax_merge(best, bi, v, r);
   }
   for (int t = 0; t < nbp; ++t) {
     const int c = p0 + t;
@@ -274,23 +276,38 @@ __global__ void smc_zlu_panel_kernel(double2* __restrict__ A, int n, int p0, int
     const int ncols = p0 + nbp - c - 1;
     best = -1.0;
     bi = n;
-    int cnt = 0;
-    SMC_FOR_OWNED_ROWS(r, p0, n, b, G) {
-      if ((cnt++ % nt) == tid) {
-        if (r == p) { done[r] = 1; continue; }
-        if (done[r]) continue;
-        double2 l = A[r + (long long)c * n];
-        if (nz) l = cmul(l, rinv);
-        A[r + (long long)c * n] = l;
-        for (int j = 1; j <= ncols; ++j) {
-          double2* e = &A[r + (long long)(c + j) * n];
-          *e = csub(*e, cmul(l, prow[j]));
+    SMC_FOR_OWNED_ROW(r, p0, n, b, G, warp, nwarps, lane) {
+      if (r == p) { done[r] = 1; continue; }
+      if (done[r]) continue;
+      double2* Ar = A + r + (long long)c * n;
+      double2 l = Ar[0];
+      if (nz) l = cmul(l, rinv);
+      Ar[0] = l;
+      // the row's remaining panel entries, eight loads in flight before their
+      // stores (a store could alias a later load as far as the compiler
+      // knows, which would otherwise serialise the loop on memory latency)
+      double2 next = make_double2(0.0, 0.0);   // updated entry of column c+1
+      int j = 1;
+      for (; j + 7 <= ncols; j += 8) {
+        double2 e[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) e[q] = Ar[(long long)(j + q) * n];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          e[q] = csub(e[q], cmul(l, prow[j + q]));
+          Ar[(long long)(j + q) * n] = e[q];
         }
-        if (t + 1 < nbp) {
-          double v = cabs1(A[r + (long long)(c + 1) * n]);
-          if (v != v) v = INFINITY;
-          argmax_merge(best, bi, v, r);
-        }
+        if (j == 1) next = e[0];
+      }
+      for (; j <= ncols; ++j) {
+        double2 e = csub(Ar[(long long)j * n], cmul(l, prow[j]));
+        Ar[(long long)j * n] = e;
+        if (j == 1) next = e;
+      }
+      if (t + 1 < nbp) {
+        double v = cabs1(next);
+        if (v != v) v = INFINITY;
+        argmax_merge(best, bi, v, r);
       }
     }
     __syncthreads();
@@ -315,37 +332,67 @@ __global__ void smc_zlu_panel_kernel(double2* __restrict__ A, int n, int p0, int
       if (!fr && nt2 < 2 * ZNB) { rowid[nt2] = r; posn[nt2] = q; ++nt2; }
       if (!fq && rq != r && nt2 < 2 * ZNB) { rowid[nt2] = rq; posn[nt2] = pr; ++nt2; }
     }
+    // the same interchanges as one gather: position posn[k] receives the
+    // original row rowid[k] (rows that did not move are left out)
+    int* gl = pv + ZNB;
+    int m = 0;
+    for (int k = 0; k < nt2; ++k)
+      if (rowid[k] != posn[k]) { gl[1 + m] = rowid[k]; gl[1 + 2 * ZNB + m] = posn[k]; ++m; }
+    gl[0] = m;
   }
 }
 
-// row interchanges of panel [p0, p0+nbp) applied to every column
-__global__ void smc_zlu_laswp_kernel(double2* __restrict__ A, int n, int p0, int nbp,
-                                     const int* __restrict__ piv) {
-  int col = blockIdx.x * blockDim.x + threadIdx.x;
+// row interchanges of panel [p0, p0+nbp) applied to every column, as the
+// gather the panel kernel left in gl = {m, src[2 ZNB], dst[2 ZNB]}: one warp
+// per column, each lane moving up to two rows; all loads of a column precede
+// its stores.
+static constexpr int LASWP_WARPS = 8;
+__global__ void __launch_bounds__(32 * LASWP_WARPS) smc_zlu_laswp_kernel(double2* __restrict__ A, int n,
+                                                                         const int* __restrict__ gl) {
+  __shared__ int s_src[2 * ZNB], s_dst[2 * ZNB];
+  __shared__ int s_m;
+  if (threadIdx.x == 0) s_m = min(gl[0], 2 * ZNB);
+  __syncthreads();
+  const int m = s_m;
+  for (int t = threadIdx.x; t < m; t += blockDim.x) { s_src[t] = gl[1 + t]; s_dst[t] = gl[1 + 2 * ZNB + t]; }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int col = blockIdx.x * LASWP_WARPS + (threadIdx.x >> 5);
   if (col >= n) return;
   double2* Ac = A + (long long)col * n;
-  for (int i = p0; i < p0 + nbp; ++i) {
-    int p = piv[i];
-    if (p != i) { double2 t = Ac[i]; Ac[i] = Ac[p]; Ac[p] = t; }
-  }
+  double2 v0 = make_double2(0.0, 0.0), v1 = v0;
+  if (lane < m) v0 = Ac[s_src[lane]];
+  if (lane + 32 < m) v1 = Ac[s_src[lane + 32]];
+  __syncwarp();
+  if (lane < m) Ac[s_dst[lane]] = v0;
+  if (lane + 32 < m) Ac[s_dst[lane + 32]] = v1;
 }
 
-// U12 = L11^{-1} A12 (unit lower L11 of the panel), one thread per column
-__global__ void smc_zlu_trsm_kernel(double2* __restrict__ A, int n, int p0, int nbp) {
-  __shared__ double2 L[ZNB * ZNB];
+// U12 = L11^{-1} A12 (unit lower L11 of the panel), one warp per column:
+// lane i holds entry i of the column; forward substitution broadcasts the
+// finished entry c with a shuffle and every lane below it subtracts its
+// multiple.  Loads and stores of a column are one coalesced line.
+static constexpr int TRSM_WARPS = 8;
+__global__ void __launch_bounds__(32 * TRSM_WARPS) smc_zlu_trsm_kernel(double2* __restrict__ A, int n,
+                                                                       int p0, int nbp) {
+  __shared__ double2 L[ZNB * ZNB];     // L[r + c*ZNB]
   for (int t = threadIdx.x; t < nbp * nbp; t += blockDim.x) {
     int r = t % nbp, c = t / nbp;
-    L[t] = A[(p0 + r) + (long long)(p0 + c) * n];
+    L[r + c * ZNB] = A[(p0 + r) + (long long)(p0 + c) * n];
   }
   __syncthreads();
-  int col = p0 + nbp + blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= n) return;
-  double2 x[ZNB];
+  const int lane = threadIdx.x & 31;
+  const int col = p0 + nbp + blockIdx.x * TRSM_WARPS + (threadIdx.x >> 5);
+  if (col >= n) return;              // uniform per warp
   double2* Ac = A + (long long)col * n + p0;
-  for (int i = 0; i < nbp; ++i) x[i] = Ac[i];
-  for (int c = 0; c < nbp; ++c)
-    for (int r = c + 1; r < nbp; ++r) x[r] = csub(x[r], cmul(L[r + c * nbp], x[c]));
-  for (int i = 0; i < nbp; ++i) Ac[i] = x[i];
+  double2 x = lane < nbp ? Ac[lane] : make_double2(0.0, 0.0);
+  for (int c = 0; c + 1 < nbp; ++c) {
+    double2 xc;
+    xc.x = __shfl_sync(0xffffffffu, x.x, c);
+    xc.y = __shfl_sync(0xffffffffu, x.y, c);
+    if (lane > c && lane < nbp) x = csub(x, cmul(L[lane + c * ZNB], xc));
+  }
+  if (lane < nbp) Ac[lane] = x;
 }
 
 // A22 -= L21 U12 : 64x64 output tile per CTA, 4x4 complex outputs per thread
@@ -412,17 +459,17 @@ void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work) {
   if (maxb < 1) throw std::runtime_error("zlu_dense: panel kernel cannot be co-resident");
   double* part = reinterpret_cast<double*>(work);                 // 4 G doubles
   int* done = reinterpret_cast<int*>(part + 4 * G + 64);           // n ints
-  int* pv = done + n + 64;                                          // ZNB ints
+  int* pv = done + n + 64;        // ZNB pivot rows, then the gather list (1 + 4 ZNB ints)
   for (int p0 = 0; p0 < n; p0 += ZNB) {
     int nbp = std::min(ZNB, n - p0);
     void* args[] = {&A, &n, &p0, &nbp, &piv, &part, &done, &pv};
     SMC_CUDA(cudaLaunchCooperativeKernel((void*)smc_zlu_panel_kernel, dim3(G), dim3(256), args, 0, c.s));
     SMC_LAUNCH_CHECK(c);
-    smc_zlu_laswp_kernel<<<ceil_div(n, 128), 128, 0, c.s>>>(A, n, p0, nbp, piv);
+    smc_zlu_laswp_kernel<<<ceil_div(n, LASWP_WARPS), 32 * LASWP_WARPS, 0, c.s>>>(A, n, pv + ZNB);
     SMC_LAUNCH_CHECK(c);
     int rest = n - p0 - nbp;
     if (rest > 0) {
-      smc_zlu_trsm_kernel<<<ceil_div(rest, 64), 64, 0, c.s>>>(A, n, p0, nbp);
+      smc_zlu_trsm_kernel<<<ceil_div(rest, TRSM_WARPS), 32 * TRSM_WARPS, 0, c.s>>>(A, n, p0, nbp);
       SMC_LAUNCH_CHECK(c);
       dim3 g(ceil_div(rest, GT), ceil_div(rest, GT));
       smc_zlu_gemm_kernel<<<g, 256, gsm, c.s>>>(A, n, p0, nbp);

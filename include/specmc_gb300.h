@@ -185,7 +185,11 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
  * (1) or as plain FP64 FGMRES on the fused operators (0).
  * "krylov_engine" (0/1, SMC_MIXED handles, default 1): run each of those
  * FGMRES solves in one persistent cooperative kernel on the device (1) or
- * with host-side control per iteration (0). */
+ * with host-side control per iteration (0).
+ * "engine_phase_profile" (0/1, default 0): while the profiler is on, add the
+ * engine's time between grid barriers, per phase, as profile regions named
+ * "engine_stokes.<phase>" / "engine_theta.<phase>" (SM cycles of one CTA at
+ * the peak clock, so a lower bound on wall time). */
 int smc_set_option(smc_handle* h, const char* key, double value);
 
 /* RBCImplicitTheta.reset_history (implicit_theta.py:601-606). */

@@ -1,19 +1,37 @@
 // Persistent Krylov engine of the fast form: one cooperative launch runs a
 // whole right-preconditioned FGMRES solve (core/krylov_fgmres.py:60-179) on
-// the device -- preconditioner, operator, Arnoldi (CGS2) and the Givens
-// least-squares update -- with grid barriers between dependent phases and no
-// host round trip per iteration.
+// the device -- preconditioner, operator, CGS2 Arnoldi and the Givens
+// least-squares update -- with no host round trip per iteration.
 //
 // Operators: the fused Schur matvec (stokes/lagged_stokes.py:202-220) or the
 // fused temperature matvec (implicit_theta.py:354-383), in working precision
 // T (float: the inner solves of the mixed form; double: FP64).  Krylov
 // vectors, the Hessenberg matrix and the Givens data stay FP64.
 //
+// Work decomposition.  Both operators have the shape
+//     per-k z-contraction -> per-z-point x-convolution -> per-k z-epilogue,
+// and the block preconditioner acts on one Fourier row k at a time.  The grid
+// is split into Nk groups of R = G / Nk CTAs; the CTAs of group k each build
+// the whole row k of the next basis vector and of its preconditioned vector
+// (redundantly -- a row is N values), then each contracts its own slice of
+// output rows.  So one Arnoldi step is four phases separated by grid
+// barriers:
+//   NEXT   v_{j} = (w' - V h2) / h, z_j = M v_j, z-contraction      (per k)
+//   XCONV  x-direction convolution                          (per z-point)
+//   POST   w = z-epilogue, first-pass dots V^H w            (per k, rows)
+//   UPDATE w' = w - V h1, second-pass dots V^H w', ||w'||^2 (per k, rows)
+// The norm of w'' = w' - V h2 follows from ||w''||^2 = ||w'||^2 - ||h2||^2
+// (h2 is orthogonal-projection data, so this is exact up to rounding); when
+// that difference loses more than four digits an exact norm is taken with
+// one extra barrier.  Every CTA reduces the per-CTA dot partials in the same
+// order and runs the Givens update itself, so all CTAs hold identical
+// coefficients and take identical branches.
+//
 // Uniform control: every branch that decides how many grid barriers a CTA
-// executes depends only on data every CTA reads after the same barrier
-// (values reduced in the same order by every CTA, or a flag written by CTA 0
-// before a barrier), and every loop is bounded by the restart length and the
-// iteration budget, so all CTAs execute the same sequence of barriers.
+// executes depends only on values every CTA computes identically from the
+// same data after the same barrier, and every loop is bounded by the restart
+// length and the iteration budget, so all CTAs execute the same sequence of
+// barriers.
 #include <cooperative_groups.h>
 
 #include <type_traits>
@@ -29,8 +47,37 @@ template <class T> struct CT2;
 template <> struct CT2<double> { using type = double2; };
 template <> struct CT2<float> { using type = float2; };
 
+static constexpr int ENG_THREADS = 256;
+static constexpr int ENG_WARPS = ENG_THREADS / 32;
+static constexpr int ENG_MAXM = 100;     // restart + 1
+static constexpr int RCH = 64;           // output rows per GEMV chunk
+
 struct EngCtx {
   int G, b, tid, lane, warp, gw, nw;   // grid size, block, thread, lane, warp, global warp, #warps
+  int R, ntask;                        // CTAs per Fourier row, row tasks
+};
+
+const char* const engine_phase_names[2][ENGINE_PHASES] = {
+    {"engine_stokes.start", "engine_stokes.xconv", "engine_stokes.post", "engine_stokes.update",
+     "engine_stokes.exact_norm", "engine_stokes.next", "engine_stokes.lsq", "engine_stokes.resid"},
+    {"engine_theta.start", "engine_theta.xconv", "engine_theta.post", "engine_theta.update",
+     "engine_theta.exact_norm", "engine_theta.next", "engine_theta.lsq", "engine_theta.resid"}};
+
+// phase timer of CTA 0 / thread 0: cycles since the previous mark go to slot
+struct PhaseClock {
+  long long* acc;
+  long long last;
+  __device__ void init(long long* a, const EngCtx& e) {
+    acc = (a && e.b == 0 && e.tid == 0) ? a : nullptr;
+    last = clock64();
+  }
+  __device__ void mark(int slot) {
+    if (acc) {
+      const long long t = clock64();
+      acc[slot] += t - last;
+      last = t;
+    }
+  }
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -42,81 +89,244 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-// ---------------------------------------------------------------- phases
-// out[k][n] = alpha sum_m Gp[k][n][m] in[k][m]       (warp per output)
-__device__ void ph_precond(const EngineOps& op, const double2* in, double2* out, const EngCtx& e) {
-  const long long no = (long long)op.Nk * op.N;
-  for (long long o = e.gw; o < no; o += e.nw) {
-    const int k = (int)(o / op.N), n = (int)(o % op.N);
-    const double* g = op.Gp + ((long long)k * op.N + n) * op.N;
-    const double2* r = in + (long long)k * op.N;
-    double sr = 0.0, si = 0.0;
-    for (int m = e.lane; m < op.N; m += 32) {
-      sr += g[m] * r[m].x;
-      si += g[m] * r[m].y;
-    }
-    sr = warp_sum(sr);
-    si = warp_sum(si);
-    if (e.lane == 0) out[o] = make_double2(op.palpha * sr, op.palpha * si);
-  }
+template <class T>
+__device__ __forceinline__ typename CT2<T>::type mk2(T a, T b) {
+  typename CT2<T>::type r;
+  r.x = a;
+  r.y = b;
+  return r;
 }
 
+// per-CTA shared-memory rows of the per-k phases (carved from dynamic smem;
+// the x-convolution phases reuse the same bytes from offset 0)
 template <class T>
-__device__ void ph_convert(const EngineOps& op, const double2* in, typename CT2<T>::type* out,
-                           long long n, const EngCtx& e) {
-  for (long long t = (long long)e.b * blockDim.x + e.tid; t < n; t += (long long)e.G * blockDim.x) {
-    typename CT2<T>::type v;
-    v.x = (T)in[t].x;
-    v.y = (T)in[t].y;
-    out[t] = v;
-  }
-}
-
-// Schur forward: Fv[b][k][s] = c_b(k) sum_q Z_b(k)[s][q] v[k][q]; one warp
-// per (k, s) forms all four fields from one read of v_k (4 independent sums)
-template <class T>
-__device__ void ph_schur_fwd(const EngineOps& op, const typename CT2<T>::type* v, const EngCtx& e) {
+struct EngSmem {
   using C = typename CT2<T>::type;
-  const long long total = (long long)op.Nk * op.Mz;
-  const long long MN = (long long)op.Mz * op.N;
-  C* Fv = (C*)op.Fv;
-  for (long long o = e.gw; o < total; o += e.nw) {
-    const int s = (int)(o % op.Mz);
-    const int k = (int)(o / op.Mz);
-    const T* z0 = (const T*)op.Zf + (long long)s * op.N;
-    const T* z1 = (const T*)op.Z1 + (long long)k * MN + (long long)s * op.N;
-    const T* z2 = (const T*)op.Z2 + (long long)k * MN + (long long)s * op.N;
-    const T* z3 = (const T*)op.Z3 + (long long)k * MN + (long long)s * op.N;
-    const C* vk = v + (long long)k * op.N;
-    T a0 = 0, b0 = 0, a1 = 0, b1 = 0, a2 = 0, b2 = 0, a3 = 0, b3 = 0;
-    for (int q = e.lane; q < op.N; q += 32) {
-      const C x = vk[q];
-      const T w0 = z0[q], w1 = z1[q], w2 = z2[q], w3 = z3[q];
-      a0 += w0 * x.x; b0 += w0 * x.y;
-      a1 += w1 * x.x; b1 += w1 * x.y;
-      a2 += w2 * x.x; b2 += w2 * x.y;
-      a3 += w3 * x.x; b3 += w3 * x.y;
+  double2* v;     // N   FP64 row (basis row / epilogue input)
+  double2* w;     // N   FP64 epilogue outputs of the owned rows
+  C* vt;          // N   row in T (preconditioner input; the high part for T = float)
+  C* vlo;         // N   low part of the row (T = float: v - (double) vt)
+  C* z;           // N   preconditioned row in T (contraction input)
+  C* aux;         // max(3 Mz, N) epilogue vectors
+  C* out;         // 4 RCH GEMV results
+  void* red;      // ENG_WARPS * max(4 RCH sizeof(C), RCH sizeof(double2)) partials
+};
+
+__host__ __device__ inline size_t eng_align(size_t b) { return (b + 255) & ~(size_t)255; }
+
+template <class T>
+__host__ __device__ inline size_t eng_rows_bytes(int N, int Mz) {
+  using C = typename CT2<T>::type;
+  const size_t NN = (size_t)N;
+  const size_t aux = (size_t)(3 * Mz > N ? 3 * Mz : N);
+  const size_t redc = (size_t)ENG_WARPS * 4 * RCH * sizeof(C);
+  const size_t redd = (size_t)ENG_WARPS * RCH * sizeof(double2);
+  return eng_align(NN * sizeof(double2)) * 2 + eng_align(NN * sizeof(C)) * 3 +
+         eng_align(aux * sizeof(C)) + eng_align(4 * RCH * sizeof(C)) +
+         eng_align(redc > redd ? redc : redd);
+}
+
+template <class T>
+__device__ EngSmem<T> eng_carve(unsigned char* base, int N, int Mz) {
+  using C = typename CT2<T>::type;
+  EngSmem<T> S;
+  size_t o = 0;
+  const int aux = 3 * Mz > N ? 3 * Mz : N;
+  S.v = reinterpret_cast<double2*>(base + o); o += eng_align((size_t)N * sizeof(double2));
+  S.w = reinterpret_cast<double2*>(base + o); o += eng_align((size_t)N * sizeof(double2));
+  S.vt = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
+  S.vlo = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
+  S.z = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
+  S.aux = reinterpret_cast<C*>(base + o); o += eng_align((size_t)aux * sizeof(C));
+  S.out = reinterpret_cast<C*>(base + o); o += eng_align(4 * RCH * sizeof(C));
+  S.red = base + o;
+  return S;
+}
+
+// ----------------------------------------------------------- row helpers
+// out[m][r] = sum_c At[m][c ld + r0 + r] x[m][c] for r < nr <= RCH, m < NM:
+// lanes over output rows (coalesced in the transposed layout), warps over
+// columns, warp partials summed in a fixed order.  Ends with __syncthreads.
+template <class T, int NM>
+struct GemvArgs {
+  const T* a[NM];
+  const typename CT2<T>::type* x[NM];
+};
+
+template <class T, int NM>
+__device__ void tgemv_chunk(const GemvArgs<T, NM>& g, long long ld, int r0, int nr, int ncol,
+                            EngSmem<T>& S, const EngCtx& e) {
+  using C = typename CT2<T>::type;
+  C* red = reinterpret_cast<C*>(S.red);
+  for (int rc = 0; rc < nr; rc += 32) {
+    const int r = rc + e.lane;
+    T ar[NM], ai[NM];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) { ar[m] = (T)0; ai[m] = (T)0; }
+    if (r < nr) {
+#pragma unroll 4
+      for (int c = e.warp; c < ncol; c += ENG_WARPS) {
+#pragma unroll
+        for (int m = 0; m < NM; ++m) {
+          const T a = g.a[m][(long long)c * ld + r0 + r];
+          const C x = g.x[m][c];
+          ar[m] += a * x.x;
+          ai[m] += a * x.y;
+        }
+      }
     }
-    for (int d = 16; d > 0; d >>= 1) {
-      a0 += __shfl_xor_sync(0xffffffffu, a0, d); b0 += __shfl_xor_sync(0xffffffffu, b0, d);
-      a1 += __shfl_xor_sync(0xffffffffu, a1, d); b1 += __shfl_xor_sync(0xffffffffu, b1, d);
-      a2 += __shfl_xor_sync(0xffffffffu, a2, d); b2 += __shfl_xor_sync(0xffffffffu, b2, d);
-      a3 += __shfl_xor_sync(0xffffffffu, a3, d); b3 += __shfl_xor_sync(0xffffffffu, b3, d);
+#pragma unroll
+    for (int m = 0; m < NM; ++m) red[(e.warp * NM + m) * RCH + r] = mk2<T>(ar[m], ai[m]);
+  }
+  __syncthreads();
+  for (int idx = e.tid; idx < NM * nr; idx += blockDim.x) {
+    const int m = idx / nr, r = idx - m * nr;
+    T sr = (T)0, si = (T)0;
+    for (int w = 0; w < ENG_WARPS; ++w) {
+      const C q = red[(w * NM + m) * RCH + r];
+      sr += q.x;
+      si += q.y;
     }
-    if (e.lane == 0) {
-      const T kk = ((const T*)op.kxT)[k];
-      const T c1 = (T)2 * kk * kk;
-      const long long KM = (long long)op.Nk * op.Mz;
-      const long long base = (long long)k * op.Mz + s;
-      C r;
-      r.x = a0; r.y = b0; Fv[base] = r;
-      r.x = c1 * a1; r.y = c1 * b1; Fv[KM + base] = r;
-      r.x = a2; r.y = b2; Fv[2 * KM + base] = r;
-      r.x = kk * a3; r.y = kk * b3; Fv[3 * KM + base] = r;
+    S.out[m * RCH + r] = mk2<T>(sr, si);
+  }
+  __syncthreads();
+}
+
+// y[r] = (base[off + r] - sum_{i<mm} c_i V_i[off + r]) * scale for r < nr,
+// FP64; warps over i, lanes over r.  Results go to the shared row y and/or
+// to global gout[off + r].  Ends with __syncthreads.
+template <class T>
+__device__ void combine_rows(const double2* base, const double2* V, long long n, long long off,
+                             int nr, const double2* c, int mm, double scale, double2* y,
+                             double2* gout, EngSmem<T>& S, const EngCtx& e) {
+  double2* red = reinterpret_cast<double2*>(S.red);
+  for (int r0 = 0; r0 < nr; r0 += RCH) {
+    const int cnt = min(RCH, nr - r0);
+    for (int rc = 0; rc < cnt; rc += 32) {
+      const int r = rc + e.lane;
+      double sr = 0.0, si = 0.0;
+      if (r < cnt) {
+#pragma unroll 4
+        for (int i = e.warp; i < mm; i += ENG_WARPS) {
+          const double2 v = V[(long long)i * n + off + r0 + r];
+          const double2 ci = c[i];
+          sr += ci.x * v.x - ci.y * v.y;
+          si += ci.x * v.y + ci.y * v.x;
+        }
+      }
+      red[e.warp * RCH + r] = make_double2(sr, si);
+    }
+    __syncthreads();
+    for (int r = e.tid; r < cnt; r += blockDim.x) {
+      double sr = 0.0, si = 0.0;
+      for (int w = 0; w < ENG_WARPS; ++w) {
+        sr += red[w * RCH + r].x;
+        si += red[w * RCH + r].y;
+      }
+      const double2 bv = base ? base[off + r0 + r] : make_double2(0.0, 0.0);
+      const double2 o = make_double2((bv.x - sr) * scale, (bv.y - si) * scale);
+      if (y) y[r0 + r] = o;
+      if (gout) gout[off + r0 + r] = o;
+    }
+    __syncthreads();
+  }
+}
+
+// acc[i] += sum_{r<nr} conj(V_i[off + r]) y[r] for i < mm (y shared, FP64):
+// warps over i in batches of four (independent loads), lanes over r
+__device__ void dots_acc(const double2* V, long long n, long long off, int nr, const double2* y,
+                         int mm, double2* acc, const EngCtx& e) {
+  for (int i0 = e.warp; i0 < mm; i0 += 4 * ENG_WARPS) {
+    double sr[4] = {0.0, 0.0, 0.0, 0.0}, si[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int r = e.lane; r < nr; r += 32) {
+      const double2 x = y[r];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int i = i0 + t * ENG_WARPS;
+        if (i < mm) {
+          const double2 a = V[(long long)i * n + off + r];
+          sr[t] += a.x * x.x + a.y * x.y;
+          si[t] += a.x * x.y - a.y * x.x;
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int i = i0 + t * ENG_WARPS;
+      const double a = warp_sum(sr[t]), b = warp_sum(si[t]);
+      if (e.lane == 0 && i < mm) acc[i] = make_double2(acc[i].x + a, acc[i].y + b);
     }
   }
 }
 
+// out[i] = sum_{g<G} pp[i G + g] for i < mm, the same order in every CTA
+__device__ void reduce_parts(const double2* pp, int G, int mm, double2* out, const EngCtx& e) {
+  for (int i0 = e.warp; i0 < mm; i0 += 4 * ENG_WARPS) {
+    double sr[4] = {0.0, 0.0, 0.0, 0.0}, si[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int g = e.lane; g < G; g += 32) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int i = i0 + t * ENG_WARPS;
+        if (i < mm) {
+          const double2 q = pp[(size_t)i * G + g];
+          sr[t] += q.x;
+          si[t] += q.y;
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int i = i0 + t * ENG_WARPS;
+      const double a = warp_sum(sr[t]), b = warp_sum(si[t]);
+      if (e.lane == 0 && i < mm) out[i] = make_double2(a, b);
+    }
+  }
+}
+
+// sum_{g<G} p[g], the same order in every CTA; ends with __syncthreads
+__device__ double reduce_scalar(const double* p, int G, double* sh, const EngCtx& e) {
+  if (e.warp == 0) {
+    double a = 0.0;
+    for (int g = e.lane; g < G; g += 32) a += p[g];
+    a = warp_sum(a);
+    if (e.lane == 0) sh[0] = a;
+  }
+  __syncthreads();
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// sum over the CTA's threads of |y[r]|^2, r < nr, added to *acc by thread 0
+__device__ void norm_acc(const double2* y, int nr, double* acc, const EngCtx& e) {
+  if (e.warp == 0) {
+    double s = 0.0;
+    for (int r = e.lane; r < nr; r += 32) s += y[r].x * y[r].x + y[r].y * y[r].y;
+    s = warp_sum(s);
+    if (e.lane == 0) *acc += s;
+  }
+}
+
+// ||x|| over the grid (one barrier); every CTA returns the same value
+__device__ double grid_norm(const double2* x, long long n, double* part, const EngCtx& e,
+                            cg::grid_group& grid, double* sh) {
+  const long long per = (n + e.G - 1) / e.G;
+  const long long lo = (long long)e.b * per, hi = min(n, lo + per);
+  double s = 0.0;
+  for (long long t = lo + e.tid; t < hi; t += blockDim.x) s += x[t].x * x[t].x + x[t].y * x[t].y;
+  s = warp_sum(s);
+  if (e.lane == 0) sh[1 + e.warp] = s;
+  __syncthreads();
+  if (e.tid == 0) {
+    double a = 0.0;
+    for (int q = 0; q < ENG_WARPS; ++q) a += sh[1 + q];
+    part[e.b] = a;
+  }
+  grid.sync();
+  return sqrt(reduce_scalar(part, e.G, sh, e));
+}
+
+// ----------------------------------------------------- x-direction phases
 // Schur x-convolution: CTA per z-point s; the four fields are handled by
 // four groups of blockDim/4 threads with their own shared-memory slices
 template <class T>
@@ -181,88 +391,6 @@ __device__ void ph_schur_x(const EngineOps& op, unsigned char* smraw, const EngC
         o.y = hi * invL;
         Hv[((long long)grp * Nk + i) * Mz + s] = o;
       }
-    }
-  }
-}
-
-// Schur epilogue (warp per output (k, p)); tau rows from the FP64 input
-template <class T>
-__device__ void ph_schur_out(const EngineOps& op, const double2* v, double2* out, const EngCtx& e) {
-  using C = typename CT2<T>::type;
-  const int Nk = op.Nk, N = op.N, Mz = op.Mz;
-  const C* Hv = (const C*)op.Hv;
-  const long long KM = (long long)Nk * Mz;
-  for (long long o = e.gw; o < (long long)Nk * N; o += e.nw) {
-    const int k = (int)(o / N), p = (int)(o % N);
-    if (p >= N - 2) {
-      const double* Vr = op.V64 + (p == N - 2 ? 0 : (long long)(N - 1) * N);
-      const double2* vk = v + (long long)k * N;
-      double sr = 0, si = 0;
-      for (int m = e.lane; m < N; m += 32) { sr += vk[m].x * Vr[m]; si += vk[m].y * Vr[m]; }
-      sr = warp_sum(sr);
-      si = warp_sum(si);
-      if (e.lane == 0) out[o] = make_double2(sr, si);
-      continue;
-    }
-    const C* H0 = Hv + (long long)k * Mz;
-    const C* H1 = H0 + KM;
-    const C* H2 = H1 + KM;
-    const C* H3 = H2 + KM;
-    const T* a = (const T*)op.D2Zi + (long long)p * Mz;
-    const T* z = (const T*)op.Zi + (long long)p * Mz;
-    const T* dd = (const T*)op.DZi + (long long)p * Mz;
-    const T kk = ((const T*)op.kxT)[k];
-    const T k2 = kk * kk;
-    T ar = 0, ai = 0, br = 0, bi = 0, cr = 0, ci = 0;
-    for (int q = e.lane; q < Mz; q += 32) {
-      const T as = a[q], zs = z[q], ds = dd[q];
-      const C h0 = H0[q], h1 = H1[q], h2 = H2[q], h3 = H3[q];
-      ar += as * (h0.x + h1.x);
-      ai += as * (h0.y + h1.y);
-      br += zs * ((T)2 * k2 * h2.x - k2 * h0.x);
-      bi += zs * ((T)2 * k2 * h2.y - k2 * h0.y);
-      cr += ds * h3.x;
-      ci += ds * h3.y;
-    }
-    ar = warp_sum(ar); ai = warp_sum(ai); br = warp_sum(br);
-    bi = warp_sum(bi); cr = warp_sum(cr); ci = warp_sum(ci);
-    if (e.lane == 0) {
-      const T r = ar + br - (T)4 * kk * cr;
-      const T im = ai + bi - (T)4 * kk * ci;
-      out[o] = make_double2((double)r, (double)im);
-    }
-  }
-}
-
-// theta z-synthesis: X0[k][j] = i k (V v_k)[j], X1 = (VD v_k)[j]
-template <class T>
-__device__ void ph_theta_z(const EngineOps& op, const typename CT2<T>::type* v, const EngCtx& e) {
-  using C = typename CT2<T>::type;
-  const int Nk = op.Nk, N = op.N;
-  C* X = (C*)op.X;
-  for (long long o = e.gw; o < (long long)Nk * N; o += e.nw) {
-    const int k = (int)(o / N), j = (int)(o % N);
-    const T* a = (const T*)op.tV + (long long)j * N;
-    const T* d = (const T*)op.tVD + (long long)j * N;
-    const C* vk = v + (long long)k * N;
-    T ar = 0, ai = 0, dr = 0, di = 0;
-    for (int q = e.lane; q < N; q += 32) {
-      const C x = vk[q];
-      ar += a[q] * x.x;
-      ai += a[q] * x.y;
-      dr += d[q] * x.x;
-      di += d[q] * x.y;
-    }
-    ar = warp_sum(ar); ai = warp_sum(ai); dr = warp_sum(dr); di = warp_sum(di);
-    if (e.lane == 0) {
-      const T kk = ((const T*)op.kxT)[k];
-      C o0, o1;
-      o0.x = -kk * ai;
-      o0.y = kk * ar;
-      o1.x = dr;
-      o1.y = di;
-      X[(long long)k * N + j] = o0;
-      X[(long long)(Nk + k) * N + j] = o1;
     }
   }
 }
@@ -333,128 +461,339 @@ __device__ void ph_theta_x(const EngineOps& op, unsigned char* smraw, const EngC
   }
 }
 
-// theta epilogue: out = a0 v - (D2 v - k^2 v) - Vi A ; tau rows (warp per output)
+
+// ------------------------------------------------- block preconditioner
+// double-float helpers: (s, c) is an unevaluated sum s + c of floats
+__device__ __forceinline__ void df_add(float& s, float& c, float p) {
+  const float t = s + p;
+  const float bp = t - s;
+  c += (s - (t - bp)) + (p - bp);
+  s = t;
+}
+// (s, c) += (gh + gl)(xh + xl): exact product of the high parts (FMA), the
+// cross terms into the compensation; the lo*lo term (2^-48 relative) dropped
+__device__ __forceinline__ void df_mac(float& s, float& c, float gh, float gl, float xh, float xl) {
+  const float p = gh * xh;
+  const float pe = fmaf(gh, xh, -p);
+  df_add(s, c, p);
+  c += pe + fmaf(gh, xl, gl * xh);
+}
+
+// z = palpha G_k v for the row task (k, sub) into S.z (T) and, from the sub-0
+// CTA, Z_jv (FP64).  T = double: FP64 GEMV.  T = float: double-float GEMV on
+// (hi, lo) pairs of G and of v (lanes over output rows, warps over columns,
+// warp partials merged with compensated adds in a fixed order).
 template <class T>
-__device__ void ph_theta_out(const EngineOps& op, const double2* v, const typename CT2<T>::type* vT,
-                             double2* out, const EngCtx& e) {
+__device__ void precond_row(const EngineOps& op, const EngineIO& io, int k, int sub, int jv,
+                            long long off, EngSmem<T>& S, const EngCtx& e);
+
+template <>
+__device__ void precond_row<double>(const EngineOps& op, const EngineIO& io, int k, int sub, int jv,
+                                    long long off, EngSmem<double>& S, const EngCtx& e) {
+  const int N = op.N;
+  GemvArgs<double, 1> g;
+  g.a[0] = (const double*)op.GpT + (long long)k * N * N;
+  g.x[0] = S.vt;
+  for (int r0 = 0; r0 < N; r0 += RCH) {
+    const int nr = min(RCH, N - r0);
+    tgemv_chunk<double, 1>(g, N, r0, nr, N, S, e);
+    for (int r = e.tid; r < nr; r += blockDim.x) {
+      const double2 zz = make_double2(op.palpha * S.out[r].x, op.palpha * S.out[r].y);
+      S.z[r0 + r] = zz;
+      if (sub == 0) io.Z[(long long)jv * io.n + off + r0 + r] = zz;
+    }
+  }
+}
+
+template <>
+__device__ void precond_row<float>(const EngineOps& op, const EngineIO& io, int k, int sub, int jv,
+                                   long long off, EngSmem<float>& S, const EngCtx& e) {
+  const int N = op.N;
+  const float2* G = (const float2*)op.GpT + (long long)k * N * N;
+  float4* red = reinterpret_cast<float4*>(S.red);     // [warp][RCH] (re s, re c, im s, im c)
+  for (int r0 = 0; r0 < N; r0 += RCH) {
+    const int nr = min(RCH, N - r0);
+    for (int rc = 0; rc < nr; rc += 32) {
+      const int r = rc + e.lane;
+      float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+      if (r < nr) {
+#pragma unroll 4
+        for (int c = e.warp; c < N; c += ENG_WARPS) {
+          const float2 gg = G[(long long)c * N + r0 + r];
+          const float2 xh = S.vt[c], xl = S.vlo[c];
+          df_mac(sr, cr, gg.x, gg.y, xh.x, xl.x);
+          df_mac(si, ci, gg.x, gg.y, xh.y, xl.y);
+        }
+      }
+      red[e.warp * RCH + r] = make_float4(sr, cr, si, ci);
+    }
+    __syncthreads();
+    for (int r = e.tid; r < nr; r += blockDim.x) {
+      float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+      for (int w = 0; w < ENG_WARPS; ++w) {
+        const float4 q = red[w * RCH + r];
+        df_add(sr, cr, q.x);
+        cr += q.y;
+        df_add(si, ci, q.z);
+        ci += q.w;
+      }
+      const double2 zz = make_double2(op.palpha * ((double)sr + (double)cr),
+                                      op.palpha * ((double)si + (double)ci));
+      S.z[r0 + r] = make_float2((float)zz.x, (float)zz.y);
+      if (sub == 0) io.Z[(long long)jv * io.n + off + r0 + r] = zz;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ row phases
+// prep: for each row task (k, sub): the FP64 row v_k of a new basis vector
+//   mode 0: v = r * scale                 (start of a cycle; writes V_jv, Z_jv)
+//   mode 1: v = (w - V coef) * scale      (Arnoldi step; writes V_jv, Z_jv)
+//   mode 2: v = x                         (true residual: no preconditioner)
+// then z = palpha G_k v (modes 0/1) and this sub's slice of the z-contraction.
+template <class T>
+__device__ void phase_prep(const EngineOps& op, const EngineIO& io, int mode, int jv, double scale,
+                           const double2* coef, int mm, EngSmem<T>& S, const EngCtx& e) {
   using C = typename CT2<T>::type;
   const int Nk = op.Nk, N = op.N;
-  const C* A = (const C*)op.A;
-  for (long long o = e.gw; o < (long long)Nk * N; o += e.nw) {
-    const int k = (int)(o / N), n = (int)(o % N);
-    const double2* vk = v + (long long)k * N;
-    if (n >= N - 2) {
-      const double* Vr = op.V64 + (n == N - 2 ? 0 : (long long)(N - 1) * N);
-      double sr = 0, si = 0;
-      for (int m = e.lane; m < N; m += 32) { sr += vk[m].x * Vr[m]; si += vk[m].y * Vr[m]; }
+  const long long n = io.n;
+  const T* kxT = (const T*)op.kxT;
+  for (int t = e.b; t < e.ntask; t += e.G) {
+    const int k = t / e.R, sub = t - (t / e.R) * e.R;
+    const long long off = (long long)k * N;
+    if (mode == 1) {
+      combine_rows<T>(io.w, io.V, n, off, N, coef, mm, scale, S.v, nullptr, S, e);
+    } else {
+      const double2* src = mode == 0 ? io.r : io.x;
+      const double sc = mode == 0 ? scale : 1.0;
+      for (int q = e.tid; q < N; q += blockDim.x) {
+        const double2 a = src[off + q];
+        S.v[q] = make_double2(a.x * sc, a.y * sc);
+      }
+      __syncthreads();
+    }
+    if (mode != 2) {
+      for (int q = e.tid; q < N; q += blockDim.x) {
+        const double2 a = S.v[q];
+        const C h = mk2<T>((T)a.x, (T)a.y);
+        S.vt[q] = h;
+        S.vlo[q] = mk2<T>((T)(a.x - (double)h.x), (T)(a.y - (double)h.y));
+        if (sub == 0) io.V[(long long)jv * n + off + q] = a;
+      }
+      __syncthreads();
+      precond_row<T>(op, io, k, sub, jv, off, S, e);
+    } else {
+      for (int q = e.tid; q < N; q += blockDim.x) S.z[q] = mk2<T>((T)S.v[q].x, (T)S.v[q].y);
+    }
+    __syncthreads();
+    const T kk = kxT[k];
+    if (op.kind == 0) {
+      // Fv[b][k][s] = c_b(k) sum_q Z_b(k)[s][q] z[q], c = (1, 2 k^2, 1, k)
+      const int Mz = op.Mz;
+      const int rc = (Mz + e.R - 1) / e.R;
+      const int s_lo = sub * rc, s_hi = min(Mz, s_lo + rc);
+      const long long MN = (long long)Mz * N;
+      GemvArgs<T, 4> g;
+      g.a[0] = (const T*)op.ZfT;
+      g.a[1] = (const T*)op.Z1T + (long long)k * MN;
+      g.a[2] = (const T*)op.Z2T + (long long)k * MN;
+      g.a[3] = (const T*)op.Z3T + (long long)k * MN;
+      g.x[0] = g.x[1] = g.x[2] = g.x[3] = S.z;
+      C* Fv = (C*)op.Fv;
+      const long long KM = (long long)Nk * Mz;
+      const T c1 = (T)2 * kk * kk;
+      for (int s0 = s_lo; s0 < s_hi; s0 += RCH) {
+        const int nr = min(RCH, s_hi - s0);
+        tgemv_chunk<T, 4>(g, Mz, s0, nr, N, S, e);
+        for (int r = e.tid; r < nr; r += blockDim.x) {
+          const long long base = (long long)k * Mz + s0 + r;
+          const C f0 = S.out[r], f1 = S.out[RCH + r], f2 = S.out[2 * RCH + r], f3 = S.out[3 * RCH + r];
+          Fv[base] = f0;
+          Fv[KM + base] = mk2<T>(c1 * f1.x, c1 * f1.y);
+          Fv[2 * KM + base] = f2;
+          Fv[3 * KM + base] = mk2<T>(kk * f3.x, kk * f3.y);
+        }
+      }
+    } else {
+      // X0[k][j] = i k (V z)[j], X1[k][j] = (VD z)[j]
+      const int rc = (N + e.R - 1) / e.R;
+      const int j_lo = sub * rc, j_hi = min(N, j_lo + rc);
+      GemvArgs<T, 2> g;
+      g.a[0] = (const T*)op.tVT;
+      g.a[1] = (const T*)op.tVDT;
+      g.x[0] = g.x[1] = S.z;
+      C* X = (C*)op.X;
+      for (int j0 = j_lo; j0 < j_hi; j0 += RCH) {
+        const int nr = min(RCH, j_hi - j0);
+        tgemv_chunk<T, 2>(g, N, j0, nr, N, S, e);
+        for (int r = e.tid; r < nr; r += blockDim.x) {
+          const C a = S.out[r], d = S.out[RCH + r];
+          X[off + j0 + r] = mk2<T>(-kk * a.y, kk * a.x);
+          X[(long long)(Nk + k) * N + j0 + r] = d;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// post: epilogue rows [p_lo, p_hi) of each row task; the input vector of the
+// operator is zin (FP64: Z_j, or x for a residual).  Arnoldi mode writes w
+// and adds V_i^H w (i < mm) to acc; residual mode writes r = b - A x and adds
+// ||r||^2 to *nacc.
+template <class T>
+__device__ void phase_post(const EngineOps& op, const EngineIO& io, bool resid, const double2* zin,
+                           int mm, EngSmem<T>& S, double2* acc, double* nacc, const EngCtx& e) {
+  using C = typename CT2<T>::type;
+  const int Nk = op.Nk, N = op.N;
+  const long long n = io.n;
+  const T* kxT = (const T*)op.kxT;
+  for (int t = e.b; t < e.ntask; t += e.G) {
+    const int k = t / e.R, sub = t - (t / e.R) * e.R;
+    const long long off = (long long)k * N;
+    const int pc = (N + e.R - 1) / e.R;
+    const int p_lo = sub * pc, p_hi = min(N, p_lo + pc);
+    if (p_lo >= p_hi) continue;                 // uniform within the CTA
+    const int pe = min(p_hi, N - 2);            // rows above the tau rows
+    const T kk = kxT[k];
+    if (op.kind == 0) {
+      const int Mz = op.Mz;
+      const C* Hv = (const C*)op.Hv;
+      const long long KM = (long long)Nk * Mz;
+      const T k2 = kk * kk;
+      for (int q = e.tid; q < Mz; q += blockDim.x) {
+        const long long i0 = (long long)k * Mz + q;
+        const C h0 = Hv[i0], h1 = Hv[KM + i0], h2 = Hv[2 * KM + i0], h3 = Hv[3 * KM + i0];
+        S.aux[q] = mk2<T>(h0.x + h1.x, h0.y + h1.y);
+        S.aux[Mz + q] = mk2<T>((T)2 * k2 * h2.x - k2 * h0.x, (T)2 * k2 * h2.y - k2 * h0.y);
+        S.aux[2 * Mz + q] = h3;
+      }
+      __syncthreads();
+      GemvArgs<T, 3> g;
+      g.a[0] = (const T*)op.D2ZiT;
+      g.a[1] = (const T*)op.ZiT;
+      g.a[2] = (const T*)op.DZiT;
+      g.x[0] = S.aux;
+      g.x[1] = S.aux + Mz;
+      g.x[2] = S.aux + 2 * Mz;
+      for (int p0 = p_lo; p0 < pe; p0 += RCH) {
+        const int nr = min(RCH, pe - p0);
+        tgemv_chunk<T, 3>(g, N, p0, nr, Mz, S, e);
+        for (int r = e.tid; r < nr; r += blockDim.x) {
+          const C a = S.out[r], b = S.out[RCH + r], c = S.out[2 * RCH + r];
+          const T re = a.x + b.x - (T)4 * kk * c.x;
+          const T im = a.y + b.y - (T)4 * kk * c.y;
+          S.w[p0 - p_lo + r] = make_double2((double)re, (double)im);
+        }
+      }
+    } else {
+      const C* A = (const C*)op.A;
+      for (int q = e.tid; q < N; q += blockDim.x) {
+        const double2 a = zin[off + q];
+        S.v[q] = a;
+        S.z[q] = mk2<T>((T)a.x, (T)a.y);
+        S.aux[q] = A[off + q];
+      }
+      __syncthreads();
+      GemvArgs<T, 2> g;
+      g.a[0] = (const T*)op.tD2T;
+      g.a[1] = (const T*)op.tViT;
+      g.x[0] = S.z;
+      g.x[1] = S.aux;
+      const double k2 = op.kx[k] * op.kx[k];
+      for (int p0 = p_lo; p0 < pe; p0 += RCH) {
+        const int nr = min(RCH, pe - p0);
+        tgemv_chunk<T, 2>(g, N, p0, nr, N, S, e);
+        for (int r = e.tid; r < nr; r += blockDim.x) {
+          const C l = S.out[r], a = S.out[RCH + r];
+          const double2 vn = S.v[p0 + r];
+          const double Lr = (double)l.x - k2 * vn.x, Li = (double)l.y - k2 * vn.y;
+          S.w[p0 - p_lo + r] = make_double2((op.a0 * vn.x - Lr) - (double)a.x,
+                                            (op.a0 * vn.y - Li) - (double)a.y);
+        }
+      }
+    }
+    // tau rows N-2, N-1 in FP64 from the FP64 input (one warp each)
+    for (int p = max(p_lo, N - 2) + e.warp; p < p_hi; p += ENG_WARPS) {
+      const double* Vr = op.V64 + (p == N - 2 ? 0 : (long long)(N - 1) * N);
+      double sr = 0.0, si = 0.0;
+      for (int m = e.lane; m < N; m += 32) {
+        const double2 a = zin[off + m];
+        sr += a.x * Vr[m];
+        si += a.y * Vr[m];
+      }
       sr = warp_sum(sr);
       si = warp_sum(si);
-      if (e.lane == 0) out[o] = make_double2(sr, si);
-      continue;
+      if (e.lane == 0) S.w[p - p_lo] = make_double2(sr, si);
     }
-    const T* dr = (const T*)op.tD2 + (long long)n * N;
-    const T* vi = (const T*)op.tVi + (long long)n * N;
-    const C* Ak = A + (long long)k * N;
-    const C* vTk = vT + (long long)k * N;
-    T lr = 0, li = 0, ar = 0, ai = 0;
-    for (int m = e.lane; m < N; m += 32) {
-      lr += dr[m] * vTk[m].x;
-      li += dr[m] * vTk[m].y;
-      ar += vi[m] * Ak[m].x;
-      ai += vi[m] * Ak[m].y;
+    __syncthreads();
+    const int np = p_hi - p_lo;
+    if (!resid) {
+      for (int r = e.tid; r < np; r += blockDim.x) io.w[off + p_lo + r] = S.w[r];
+      dots_acc(io.V, n, off + p_lo, np, S.w, mm, acc, e);
+    } else {
+      for (int r = e.tid; r < np; r += blockDim.x) {
+        const double2 bb = io.b[off + p_lo + r];
+        const double2 rr = make_double2(bb.x - S.w[r].x, bb.y - S.w[r].y);
+        io.r[off + p_lo + r] = rr;
+        S.w[r] = rr;
+      }
+      __syncthreads();
+      norm_acc(S.w, np, nacc, e);
     }
-    lr = warp_sum(lr); li = warp_sum(li); ar = warp_sum(ar); ai = warp_sum(ai);
-    if (e.lane == 0) {
-      const double k2 = op.kx[k] * op.kx[k];
-      const double2 vn = vk[n];
-      const double Lr = (double)lr - k2 * vn.x, Li = (double)li - k2 * vn.y;
-      out[o] = make_double2((op.a0 * vn.x - Lr) - (double)ar, (op.a0 * vn.y - Li) - (double)ai);
-    }
+    __syncthreads();
   }
 }
 
-// out = A(in) (both FP64 vectors); grid barriers between the phases
+// update: w' = w - V coef on the owned rows (in place in io.w); then the dots
+// V_i^H w' (i < mm_dots) into acc and ||w'||^2 into *nacc
 template <class T>
-__device__ void apply_op(const EngineOps& op, const double2* in, double2* out, unsigned char* sm,
-                         const EngCtx& e, cg::grid_group& grid) {
-  using C = typename CT2<T>::type;
-  const long long n = (long long)op.Nk * op.N;
-  const C* vT;
-  if (std::is_same<T, float>::value) {
-    ph_convert<T>(op, in, (C*)op.vT, n, e);
-    grid.sync();
-    vT = (const C*)op.vT;
-  } else {
-    vT = reinterpret_cast<const C*>(in);
+__device__ void phase_update(const EngineOps& op, const EngineIO& io, const double2* coef, int mm,
+                             int mm_dots, EngSmem<T>& S, double2* acc, double* nacc,
+                             const EngCtx& e) {
+  const int N = op.N;
+  const long long n = io.n;
+  for (int t = e.b; t < e.ntask; t += e.G) {
+    const int k = t / e.R, sub = t - (t / e.R) * e.R;
+    const long long off = (long long)k * N;
+    const int pc = (N + e.R - 1) / e.R;
+    const int p_lo = sub * pc, p_hi = min(N, p_lo + pc);
+    if (p_lo >= p_hi) continue;
+    const int np = p_hi - p_lo;
+    combine_rows<T>(io.w, io.V, n, off + p_lo, np, coef, mm, 1.0, S.w, io.w, S, e);
+    if (mm_dots > 0) dots_acc(io.V, n, off + p_lo, np, S.w, mm_dots, acc, e);
+    norm_acc(S.w, np, nacc, e);
+    __syncthreads();
   }
-  if (op.kind == 0) {
-    ph_schur_fwd<T>(op, vT, e);
-    grid.sync();
-    ph_schur_x<T>(op, sm, e);
-    grid.sync();
-    ph_schur_out<T>(op, in, out, e);
-  } else {
-    ph_theta_z<T>(op, vT, e);
-    grid.sync();
-    ph_theta_x<T>(op, sm, e);
-    grid.sync();
-    ph_theta_out<T>(op, in, vT, out, e);
-  }
-  grid.sync();
-}
-
-// sum of the G per-CTA partials (same order in every CTA)
-__device__ double grid_total(const double* part, int G, const EngCtx& e, double* sh) {
-  if (e.warp == 0) {
-    double a = 0.0;
-    for (int g = e.lane; g < G; g += 32) a += part[g];
-    a = warp_sum(a);
-    if (e.lane == 0) sh[0] = a;
-  }
-  __syncthreads();
-  double r = sh[0];
-  __syncthreads();
-  return r;
-}
-
-// ||x|| over the grid (one barrier); every CTA returns the same value
-__device__ double grid_norm(const double2* x, long long n, double* part, const EngCtx& e,
-                            cg::grid_group& grid, double* sh) {
-  const long long per = (n + e.G - 1) / e.G;
-  const long long lo = (long long)e.b * per, hi = min(n, lo + per);
-  double s = 0.0;
-  for (long long t = lo + e.tid; t < hi; t += blockDim.x) s += x[t].x * x[t].x + x[t].y * x[t].y;
-  s = warp_sum(s);
-  if (e.lane == 0) sh[1 + e.warp] = s;
-  __syncthreads();
-  if (e.tid == 0) {
-    double a = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) a += sh[1 + q];
-    part[e.b] = a;
-  }
-  grid.sync();
-  return sqrt(grid_total(part, e.G, e, sh));
 }
 
 // ------------------------------------------------------------- the engine
 template <class T>
-__global__ void __launch_bounds__(256) smc_fgmres_engine_kernel(EngineOps op, EngineIO io) {
+__global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(EngineOps op, EngineIO io) {
   cg::grid_group grid = cg::this_grid();
-  extern __shared__ unsigned char smraw[];
+  extern __shared__ __align__(256) unsigned char smraw[];
   __shared__ double sh[40];
-  __shared__ double2 hcol[100], hsum[100];
-  // Givens state, kept by CTA 0 in shared memory for the whole solve
-  __shared__ double s_cs[100];
-  __shared__ double2 s_sn[100], s_g[101], s_y[100];
+  __shared__ double2 s_h1[ENG_MAXM], s_h2[ENG_MAXM], s_hc[ENG_MAXM + 1], s_acc[ENG_MAXM];
+  __shared__ double s_cs[ENG_MAXM];
+  __shared__ double2 s_sn[ENG_MAXM], s_g[ENG_MAXM + 1], s_y[ENG_MAXM];
+  __shared__ double s_nacc;
   __shared__ int s_flag;
   EngCtx e;
   e.G = gridDim.x; e.b = blockIdx.x; e.tid = threadIdx.x; e.lane = e.tid & 31; e.warp = e.tid >> 5;
-  e.gw = e.b * (blockDim.x >> 5) + e.warp;
-  e.nw = e.G * (blockDim.x >> 5);
+  e.gw = e.b * ENG_WARPS + e.warp;
+  e.nw = e.G * ENG_WARPS;
+  e.R = op.Nk <= e.G ? e.G / op.Nk : 1;
+  e.ntask = op.Nk * e.R;
+  EngSmem<T> S = eng_carve<T>(smraw, op.N, op.Mz);
   const long long n = io.n;
   const int m = io.restart;
   const long long per = (n + e.G - 1) / e.G;
   const long long lo = (long long)e.b * per, hi = min(n, lo + per);
+  double2* pp1 = io.part;
+  double2* pp2 = io.part + (size_t)(m + 1) * e.G;
+  PhaseClock pc;
+  pc.init(io.phase_cycles, e);
 
   // x = 0, r = b, beta = ||b||
   for (long long t = (long long)e.b * blockDim.x + e.tid; t < n; t += (long long)e.G * blockDim.x) {
@@ -465,129 +804,126 @@ __global__ void __launch_bounds__(256) smc_fgmres_engine_kernel(EngineOps op, En
   const double tol = io.rtol * beta;
   int total = 0, info = 1;
   if (beta <= tol) info = 0;
+  if (!isfinite(beta)) info = 3;              // non-finite right-hand side
   while (info == 1 && total < io.maxiter) {
-    // V0 = r / beta
-    for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
-      double2 v = io.r[t];
-      io.V[t] = make_double2(v.x / beta, v.y / beta);
-    }
-    if (e.b == 0) {
-      for (int i = e.tid; i <= m; i += blockDim.x) s_g[i] = make_double2(0.0, 0.0);
-      __syncthreads();
-      if (e.tid == 0) s_g[0] = make_double2(beta, 0.0);
-    }
+    // V0 = r / beta, Z0 = M V0 and its z-contraction
+    phase_prep<T>(op, io, 0, 0, 1.0 / beta, nullptr, 0, S, e);
+    for (int i = e.tid; i <= m; i += blockDim.x) s_g[i] = make_double2(0.0, 0.0);
+    __syncthreads();
+    if (e.tid == 0) s_g[0] = make_double2(beta, 0.0);
     grid.sync();
-    int k = 0;
+    pc.mark(EP_START);
+    int kc = 0;
     for (int j = 0; j < m; ++j) {
-      if (total >= io.maxiter) { info = 1; break; }
-      double2* Vj = io.V + (long long)j * n;
-      double2* Zj = io.Z + (long long)j * n;
-      ph_precond(op, Vj, Zj, e);
+      // x-direction convolution of A z_j
+      if (op.kind == 0) ph_schur_x<T>(op, smraw, e);
+      else ph_theta_x<T>(op, smraw, e);
       grid.sync();
-      apply_op<T>(op, Zj, io.w, smraw, e, grid);
-      // ---- CGS2 of w against V_0..V_j (all CTAs end with identical hsum, hn)
+      pc.mark(EP_XCONV);
+      // epilogue w = A z_j + first-pass dots
       const int mm = j + 1;
-      for (int i = e.tid; i < mm; i += blockDim.x) hsum[i] = make_double2(0.0, 0.0);
+      for (int i = e.tid; i < mm; i += blockDim.x) s_acc[i] = make_double2(0.0, 0.0);
       __syncthreads();
-      for (int pass = 0; pass < 2; ++pass) {
-        double2* pp = io.part + (size_t)pass * e.G * (m + 1);
-        for (int i = e.warp; i < mm; i += (blockDim.x >> 5)) {
-          const double2* Vi = io.V + (long long)i * n;
-          double sr = 0.0, si = 0.0;
-          for (long long t = lo + e.lane; t < hi; t += 32) {
-            const double2 a = Vi[t], x = io.w[t];
-            sr += a.x * x.x + a.y * x.y;
-            si += a.x * x.y - a.y * x.x;
-          }
-          sr = warp_sum(sr);
-          si = warp_sum(si);
-          if (e.lane == 0) pp[(size_t)e.b * (m + 1) + i] = make_double2(sr, si);
-        }
-        grid.sync();
-        for (int i = e.warp; i < mm; i += (blockDim.x >> 5)) {
-          double sr = 0.0, si = 0.0;
-          for (int g = e.lane; g < e.G; g += 32) {
-            const double2 q = pp[(size_t)g * (m + 1) + i];
-            sr += q.x;
-            si += q.y;
-          }
-          sr = warp_sum(sr);
-          si = warp_sum(si);
-          if (e.lane == 0) {
-            hcol[i] = make_double2(sr, si);
-            hsum[i] = cadd(hsum[i], hcol[i]);
-          }
-        }
-        __syncthreads();
-        for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
-          double2 x = io.w[t];
-          for (int i = 0; i < mm; ++i) x = csub(x, cmul(hcol[i], io.V[(long long)i * n + t]));
-          io.w[t] = x;
-        }
-        __syncthreads();
-      }
-      const double hn = grid_norm(io.w, n, io.npart, e, grid, sh);
-      // ---- Givens update of column j (CTA 0, shared-memory state) and the
-      //      stopping decision, published through global memory
-      if (e.b == 0) {
-        if (e.tid == 0) {
-          hsum[j + 1] = make_double2(hn, 0.0);
-          for (int i = 0; i < j; ++i) {
-            const double c = s_cs[i];
-            const double2 sv = s_sn[i];
-            const double2 hi0 = hsum[i], hi1 = hsum[i + 1];
-            const double2 t = cadd(cscale(hi0, c), cmul(sv, hi1));
-            hsum[i + 1] = cadd(cmul(make_double2(-sv.x, sv.y), hi0), cscale(hi1, c));  // -conj(s) h_i + c h_{i+1}
-            hsum[i] = t;
-          }
-          const double2 a = hsum[j], bb = hsum[j + 1];
-          const double aa = hypot(a.x, a.y), bba = hypot(bb.x, bb.y);
-          double c;
-          double2 sv, rjj;
-          if (bba == 0.0) { c = 1.0; sv = make_double2(0.0, 0.0); rjj = a; }
-          else if (aa == 0.0) { c = 0.0; sv = make_double2(bb.x / bba, -bb.y / bba); rjj = make_double2(bba, 0.0); }
-          else {
-            const double den = sqrt(aa * aa + bba * bba);
-            c = aa / den;
-            sv = cscale(cdiv(cconj(bb), cconj(a)), c);
-            rjj = cscale(cdiv(make_double2(1.0, 0.0), cconj(a)), c * (aa * aa + bba * bba));
-          }
-          s_cs[j] = c;
-          s_sn[j] = sv;
-          hsum[j] = rjj;
-          hsum[j + 1] = make_double2(0.0, 0.0);
-          const double2 gj = s_g[j], gj1 = s_g[j + 1];
-          s_g[j] = cadd(cscale(gj, c), cmul(sv, gj1));
-          s_g[j + 1] = cadd(cmul(make_double2(-sv.x, sv.y), gj), cscale(gj1, c));
-          const double rn = hypot(s_g[j + 1].x, s_g[j + 1].y);
-          s_flag = (rn <= tol) ? 1 : ((hn == 0.0) ? 2 : 0);
-        }
-        __syncthreads();
-        double2* Hc = io.H + (size_t)j * (m + 1);     // rotated column j, rows 0..j
-        for (int i = e.tid; i <= j; i += blockDim.x) Hc[i] = hsum[i];
-        if (e.tid == 0) io.flag[0] = s_flag;
-      }
-      if (hn != 0.0) {
-        double2* Vn = io.V + (long long)(j + 1) * n;
-        for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
-          const double2 x = io.w[t];
-          Vn[t] = make_double2(x.x / hn, x.y / hn);
-        }
-      }
+      phase_post<T>(op, io, false, io.Z + (long long)j * n, mm, S, s_acc, nullptr, e);
+      __syncthreads();
+      for (int i = e.tid; i < mm; i += blockDim.x) pp1[(size_t)i * e.G + e.b] = s_acc[i];
       grid.sync();
-      const int fl = *((volatile int*)io.flag);
+      pc.mark(EP_POST);
+      // h1 = V^H w; w' = w - V h1; second-pass dots and ||w'||^2
+      reduce_parts(pp1, e.G, mm, s_h1, e);
+      for (int i = e.tid; i < mm; i += blockDim.x) s_acc[i] = make_double2(0.0, 0.0);
+      if (e.tid == 0) s_nacc = 0.0;
+      __syncthreads();
+      phase_update<T>(op, io, s_h1, mm, mm, S, s_acc, &s_nacc, e);
+      __syncthreads();
+      for (int i = e.tid; i < mm; i += blockDim.x) pp2[(size_t)i * e.G + e.b] = s_acc[i];
+      if (e.tid == 0) io.npart[e.b] = s_nacc;
+      grid.sync();
+      pc.mark(EP_UPDATE);
+      // h2 = V^H w', ||w''||^2 = ||w'||^2 - ||h2||^2
+      reduce_parts(pp2, e.G, mm, s_h2, e);
+      const double wn2 = reduce_scalar(io.npart, e.G, sh, e);    // ends with __syncthreads
+      double hh = 0.0;
+      for (int i = 0; i < mm; ++i) hh += s_h2[i].x * s_h2[i].x + s_h2[i].y * s_h2[i].y;
+      if (!isfinite(wn2) || !isfinite(hh)) {     // non-finite operator output: give up
+        info = 3;
+        break;
+      }
+      double hn2 = wn2 - hh;
+      bool subtracted = false;
+      if (!(hn2 > 1e-4 * wn2)) {
+        // heavy cancellation: form w'' = w' - V h2 and take its exact norm
+        if (e.tid == 0) s_nacc = 0.0;
+        __syncthreads();
+        phase_update<T>(op, io, s_h2, mm, 0, S, nullptr, &s_nacc, e);
+        __syncthreads();
+        // second partial array: other CTAs may still be reading npart here
+        if (e.tid == 0) io.npart[e.G + e.b] = s_nacc;
+        grid.sync();
+        hn2 = reduce_scalar(io.npart + e.G, e.G, sh, e);
+        subtracted = true;
+        pc.mark(EP_EXACT);
+      }
+      const double hn = sqrt(hn2 > 0.0 ? hn2 : 0.0);
+      // Givens update of column j (every CTA, identical data)
+      if (e.tid == 0) {
+        for (int i = 0; i < mm; ++i) s_hc[i] = cadd(s_h1[i], s_h2[i]);
+        s_hc[j + 1] = make_double2(hn, 0.0);
+        for (int i = 0; i < j; ++i) {
+          const double c = s_cs[i];
+          const double2 sv = s_sn[i];
+          const double2 hi0 = s_hc[i], hi1 = s_hc[i + 1];
+          const double2 tt = cadd(cscale(hi0, c), cmul(sv, hi1));
+          s_hc[i + 1] = cadd(cmul(make_double2(-sv.x, sv.y), hi0), cscale(hi1, c));  // -conj(s) h_i + c h_{i+1}
+          s_hc[i] = tt;
+        }
+        const double2 a = s_hc[j], bb = s_hc[j + 1];
+        const double aa = hypot(a.x, a.y), bba = hypot(bb.x, bb.y);
+        double c;
+        double2 sv, rjj;
+        if (bba == 0.0) { c = 1.0; sv = make_double2(0.0, 0.0); rjj = a; }
+        else if (aa == 0.0) { c = 0.0; sv = make_double2(bb.x / bba, -bb.y / bba); rjj = make_double2(bba, 0.0); }
+        else {
+          const double den = sqrt(aa * aa + bba * bba);
+          c = aa / den;
+          sv = cscale(cdiv(cconj(bb), cconj(a)), c);
+          rjj = cscale(cdiv(make_double2(1.0, 0.0), cconj(a)), c * (aa * aa + bba * bba));
+        }
+        s_cs[j] = c;
+        s_sn[j] = sv;
+        s_hc[j] = rjj;
+        const double2 gj = s_g[j], gj1 = s_g[j + 1];
+        s_g[j] = cadd(cscale(gj, c), cmul(sv, gj1));
+        s_g[j + 1] = cadd(cmul(make_double2(-sv.x, sv.y), gj), cscale(gj1, c));
+        const double rn = hypot(s_g[j + 1].x, s_g[j + 1].y);
+        s_flag = (rn <= tol) ? 1 : ((hn == 0.0) ? 2 : 0);
+      }
+      __syncthreads();
+      if (e.b == 0) {
+        double2* Hc = io.H + (size_t)j * (m + 1);     // rotated column j, rows 0..j
+        for (int i = e.tid; i <= j; i += blockDim.x) Hc[i] = s_hc[i];
+      }
+      const int fl = s_flag;
       ++total;
-      k = j + 1;
-      if (fl == 1) { info = 0; break; }
-      if (fl == 2) { info = 2; break; }
+      kc = j + 1;
+      const bool stop = fl != 0 || j + 1 == m || total >= io.maxiter;
+      if (!stop)
+        phase_prep<T>(op, io, 1, j + 1, 1.0 / hn, s_h2, subtracted ? 0 : mm, S, e);
+      grid.sync();
+      pc.mark(EP_NEXT);
+      if (stop) {
+        if (fl == 1) info = 0;
+        else if (fl == 2) info = 2;
+        break;
+      }
     }
-    if (k == 0) break;
+    if (kc == 0) break;
     // y = H[:k,:k]^{-1} g[:k]: column sweep by CTA 0 (the column of H is
     // contiguous in the column-major layout), then x += Z y everywhere
     if (e.b == 0) {
-      for (int i = e.tid; i < k; i += blockDim.x) s_y[i] = s_g[i];
+      for (int i = e.tid; i < kc; i += blockDim.x) s_y[i] = s_g[i];
       __syncthreads();
-      for (int q = k - 1; q >= 0; --q) {
+      for (int q = kc - 1; q >= 0; --q) {
         const double2* Hq = io.H + (size_t)q * (m + 1);
         if (e.tid == 0) s_y[q] = cdiv(s_y[q], Hq[q]);
         __syncthreads();
@@ -595,22 +931,33 @@ __global__ void __launch_bounds__(256) smc_fgmres_engine_kernel(EngineOps op, En
         for (int i = e.tid; i < q; i += blockDim.x) s_y[i] = csub(s_y[i], cmul(Hq[i], yq));
         __syncthreads();
       }
-      for (int i = e.tid; i < k; i += blockDim.x) io.y[i] = s_y[i];
+      for (int i = e.tid; i < kc; i += blockDim.x) io.y[i] = s_y[i];
     }
     grid.sync();
     for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
       double2 acc = make_double2(0.0, 0.0);
-      for (int q = 0; q < k; ++q) acc = cadd(acc, cmul(io.y[q], io.Z[(long long)q * n + t]));
+      for (int q = 0; q < kc; ++q) acc = cadd(acc, cmul(io.y[q], io.Z[(long long)q * n + t]));
       io.x[t] = cadd(io.x[t], acc);
     }
     grid.sync();
-    if (info == 0 || info == 2) break;
+    pc.mark(EP_LSQ);
+    if (info != 1 || total >= io.maxiter) break;
     // true residual at the restart: r = b - A x
-    apply_op<T>(op, io.x, io.r, smraw, e, grid);
-    for (long long t = lo + e.tid; t < hi; t += blockDim.x) io.r[t] = csub(io.b[t], io.r[t]);
+    phase_prep<T>(op, io, 2, 0, 1.0, nullptr, 0, S, e);
     grid.sync();
-    beta = grid_norm(io.r, n, io.npart, e, grid, sh);
+    if (op.kind == 0) ph_schur_x<T>(op, smraw, e);
+    else ph_theta_x<T>(op, smraw, e);
+    grid.sync();
+    if (e.tid == 0) s_nacc = 0.0;
+    __syncthreads();
+    phase_post<T>(op, io, true, io.x, 0, S, nullptr, &s_nacc, e);
+    __syncthreads();
+    if (e.tid == 0) io.npart[e.b] = s_nacc;
+    grid.sync();
+    beta = sqrt(reduce_scalar(io.npart, e.G, sh, e));
+    pc.mark(EP_RESID);
     if (beta <= tol) { info = 0; break; }
+    if (!isfinite(beta)) { info = 3; break; }
   }
   if (e.b == 0 && e.tid == 0) {
     io.result[0] = info;
@@ -621,9 +968,13 @@ __global__ void __launch_bounds__(256) smc_fgmres_engine_kernel(EngineOps op, En
 template <class T>
 static size_t engine_smem(const EngineOps& op) {
   using C = typename CT2<T>::type;
-  size_t a = (size_t)(op.L + 4 * (op.Nk + op.L)) * sizeof(C);
-  size_t b = (size_t)(2 * op.Nk + op.Np) * sizeof(C) + op.Np * sizeof(T);
-  return a > b ? a : b;
+  const size_t a = (size_t)(op.L + 4 * (op.Nk + op.L)) * sizeof(C);                 // Schur x
+  const size_t b = (size_t)(2 * op.Nk + op.Np) * sizeof(C) + op.Np * sizeof(T);     // theta x
+  const size_t rows = eng_rows_bytes<T>(op.N, op.kind == 0 ? op.Mz : 0);
+  size_t s = rows;
+  if (op.kind == 0 && a > s) s = a;
+  if (op.kind == 1 && b > s) s = b;
+  return s;
 }
 
 template <class T>
@@ -633,21 +984,80 @@ static void engine_launch(const Ctx& c, const EngineOps& op, const EngineIO& io)
   if (sm > 48 * 1024)
     SMC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   int per_sm = 0;
-  SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, sm));
+  SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ENG_THREADS, sm));
   if (per_sm < 1) throw std::runtime_error("fgmres engine: kernel cannot be co-resident");
   const int G = c.num_sms * (per_sm >= 2 ? 2 : 1);
   if (G > io.max_grid) throw std::runtime_error("fgmres engine: partial buffers too small");
   EngineOps o = op;
   EngineIO i = io;
   void* args[] = {(void*)&o, (void*)&i};
-  SMC_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(G), dim3(256), args, sm, c.s));
+  SMC_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(G), dim3(ENG_THREADS), args, sm, c.s));
   SMC_LAUNCH_CHECK(c);
 }
 
 void fgmres_engine(const Ctx& c, const EngineOps& op, const EngineIO& io, bool fp32) {
-  if (io.restart + 1 > 100) throw std::runtime_error("fgmres engine: restart above 99");
+  if (io.restart + 1 > ENG_MAXM) throw std::runtime_error("fgmres engine: restart above 99");
   if (fp32) engine_launch<float>(c, op, io);
   else engine_launch<double>(c, op, io);
+}
+
+// ------------------------------------------------------------- transpose
+template <class To>
+__global__ void smc_transpose_kernel(const double* __restrict__ in, To* __restrict__ out,
+                                     long long rows, long long cols) {
+  __shared__ double tile[32][33];
+  const long long bofs = (long long)blockIdx.z * rows * cols;
+  const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const long long r = r0 + i, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[i][threadIdx.x] = in[bofs + r * cols + c];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const long long c = c0 + i, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) out[bofs + c * rows + r] = (To)tile[threadIdx.x][i];
+  }
+}
+
+template <class To>
+static void transpose_impl(const Ctx& c, const double* in, To* out, long long rows, long long cols,
+                           int batch) {
+  dim3 grid(ceil_div(cols, 32), ceil_div(rows, 32), batch);
+  smc_transpose_kernel<To><<<grid, dim3(32, 8), 0, c.s>>>(in, out, rows, cols);
+  SMC_LAUNCH_CHECK(c);
+}
+void transpose_as(const Ctx& c, const double* in, float* out, long long rows, long long cols, int batch) {
+  transpose_impl<float>(c, in, out, rows, cols, batch);
+}
+void transpose_as(const Ctx& c, const double* in, double* out, long long rows, long long cols, int batch) {
+  transpose_impl<double>(c, in, out, rows, cols, batch);
+}
+
+__global__ void smc_transpose_split_kernel(const double* __restrict__ in, float2* __restrict__ out,
+                                           long long rows, long long cols) {
+  __shared__ double tile[32][33];
+  const long long bofs = (long long)blockIdx.z * rows * cols;
+  const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const long long r = r0 + i, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[i][threadIdx.x] = in[bofs + r * cols + c];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const long long c = c0 + i, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) {
+      const double v = tile[threadIdx.x][i];
+      const float hi = (float)v;
+      out[bofs + c * rows + r] = make_float2(hi, (float)(v - (double)hi));
+    }
+  }
+}
+
+void transpose_split(const Ctx& c, const double* in, float2* out, long long rows, long long cols,
+                     int batch) {
+  dim3 grid(ceil_div(cols, 32), ceil_div(rows, 32), batch);
+  smc_transpose_split_kernel<<<grid, dim3(32, 8), 0, c.s>>>(in, out, rows, cols);
+  SMC_LAUNCH_CHECK(c);
 }
 
 }  // namespace smc

@@ -6,25 +6,33 @@ namespace smc {
 
 // Operator + preconditioner of one engine solve.  Arrays typed T (the
 // working precision) are passed as void*; kind 0 = fused Schur matvec,
-// kind 1 = fused temperature matvec.
+// kind 1 = fused temperature matvec.  The dense operator matrices are
+// stored TRANSPOSED (column index outermost) so that a warp reads 32
+// consecutive output rows of one column in one coalesced access.
 struct EngineOps {
   int kind = 0;
   int Nk = 0, N = 0, Mz = 0, L = 0, Np = 0;
-  // Schur operator (T)
-  const void *Zf = nullptr, *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr;
-  const void *Zi = nullptr, *D2Zi = nullptr, *DZi = nullptr, *E = nullptr, *twS = nullptr;
-  // temperature operator (T)
-  const void *tV = nullptr, *tVD = nullptr, *tD2 = nullptr, *tVi = nullptr, *twT = nullptr;
+  // Schur operator (T): z-contraction [q][s] (Zf shared by all k; Z1..Z3 per
+  // k, [k][q][s]), epilogue [q][p], x-convolution weights E [l][s], twiddles
+  const void *ZfT = nullptr, *Z1T = nullptr, *Z2T = nullptr, *Z3T = nullptr;
+  const void *D2ZiT = nullptr, *ZiT = nullptr, *DZiT = nullptr;
+  const void *E = nullptr, *twS = nullptr;
+  // temperature operator (T): z-synthesis [q][j], epilogue [m][n], twiddles,
+  // frozen velocities on the padded grid
+  const void *tVT = nullptr, *tVDT = nullptr, *tD2T = nullptr, *tViT = nullptr, *twT = nullptr;
   const void *ux = nullptr, *uz = nullptr;
   double a0 = 0.0;
   const void* kxT = nullptr;          // kx in T
   const double* kx = nullptr;         // kx in FP64
   const double* V64 = nullptr;        // FP64 basis (tau rows)
-  // preconditioner: out = palpha * Gp_k in_k (FP64 per-k operators)
-  const double* Gp = nullptr;
+  // preconditioner: z_k = palpha * G_k v_k, G stored transposed [k][m][n]:
+  // FP64 values for T = double; (hi, lo) float pairs for T = float, applied
+  // in double-float arithmetic (the products G_k v cancel too strongly for
+  // plain FP32 on the later refinement corrections)
+  const void* GpT = nullptr;
   double palpha = 1.0;
-  // scratch (T complex): vT (Nk N), Fv/Hv (4 Nk Mz), X (2 Nk N), A (Nk N)
-  void *vT = nullptr, *Fv = nullptr, *Hv = nullptr, *X = nullptr, *A = nullptr;
+  // scratch (T complex): Fv/Hv (4 Nk Mz), X (2 Nk N), A (Nk N)
+  void *Fv = nullptr, *Hv = nullptr, *X = nullptr, *A = nullptr;
 };
 
 struct EngineIO {
@@ -38,12 +46,36 @@ struct EngineIO {
   double2 *g = nullptr, *sn = nullptr, *y = nullptr;
   double* cs = nullptr;
   double2* part = nullptr;   // 2 * max_grid * (restart + 1)
-  double* npart = nullptr;   // max_grid
+  double* npart = nullptr;   // 2 * max_grid
   int* flag = nullptr;
   int* result = nullptr;     // {info, iterations}
   int max_grid = 0;
+  // optional: SM cycles CTA 0 spent between consecutive grid barriers, summed
+  // per phase (ENGINE_PHASES slots, names in engine_phase_names); null = off
+  long long* phase_cycles = nullptr;
 };
 
+// phases of one Arnoldi step (and of a restart cycle) between grid barriers
+enum EnginePhase {
+  EP_START = 0,  // V0 = r / beta, its preconditioned vector and z-contraction
+  EP_XCONV,      // x-direction convolution (per z-point / grid column)
+  EP_POST,       // operator epilogue + first-pass orthogonalisation dots
+  EP_UPDATE,     // first-pass update + second-pass dots + ||w'||^2
+  EP_EXACT,      // exact norm after heavy cancellation (rare)
+  EP_NEXT,       // Givens update + next basis vector, its preconditioned vector, z-contraction
+  EP_LSQ,        // triangular solve + x update at the end of a cycle
+  EP_RESID,      // true residual at a restart
+  ENGINE_PHASES
+};
+extern const char* const engine_phase_names[2][ENGINE_PHASES];
+
 void fgmres_engine(const Ctx& c, const EngineOps& op, const EngineIO& io, bool fp32);
+
+// out[b][c][r] = (To) in[b][r][c] for batch matrices of rows x cols
+void transpose_as(const Ctx& c, const double* in, float* out, long long rows, long long cols, int batch);
+void transpose_as(const Ctx& c, const double* in, double* out, long long rows, long long cols, int batch);
+// out[b][c][r] = (hi, lo) with hi = (float) in[b][r][c], lo = (float)(in - hi)
+void transpose_split(const Ctx& c, const double* in, float2* out, long long rows, long long cols,
+                     int batch);
 
 }  // namespace smc

@@ -33,7 +33,7 @@ struct CudaError : std::runtime_error {
 // the kernels of a tag with CUDA events on the handle's stream; elapsed
 // times are resolved (and the events recycled) by Profiler::resolve.
 struct Profiler {
-  static constexpr int MAXTAG = 24;
+  static constexpr int MAXTAG = 48;
   bool enabled = false;
   const char* names[MAXTAG] = {nullptr};
   double ms[MAXTAG] = {0};
@@ -50,6 +50,8 @@ struct Profiler {
   void end(cudaStream_t s, int tag, cudaEvent_t a, double work_amount, int is_bytes);
   void resolve();
   void reset();
+  // a region timed on the device by other means (ms, launch count)
+  void add(const char* name, double ms_, long long n_);
   ~Profiler();
 };
 

@@ -138,6 +138,8 @@ struct LamSlot {
   double* LU = nullptr;
   int* piv = nullptr;
   double* Ginv = nullptr;   // A^{-1} P (tau columns zero): the solve as one GEMV
+  float2* GinvT32 = nullptr;  // the same transposed per k ([k][m][n]) as (hi, lo) floats (engine)
+  double* GinvT64 = nullptr;  // transposed, FP64 (engine)
   bool used = false;
 };
 
@@ -194,6 +196,11 @@ void Profiler::resolve() {
     pool[npool++] = pend[i].b;
   }
   npend = 0;
+}
+void Profiler::add(const char* name, double ms_, long long n_) {
+  const int t = tag_of(name);
+  ms[t] += ms_;
+  launches[t] += n_;
 }
 void Profiler::reset() {
   resolve();
@@ -281,8 +288,22 @@ struct Model {
   // solve and explicit per-k inverse operators for the block preconditioners
   bool fast = false;
   double* dRedG = nullptr;
+  float2* dRedGT32 = nullptr;      // transposed per k ([k][m][n]), (hi, lo) floats (engine)
+  double* dRedGT64 = nullptr;      // transposed, FP64 (engine)
   FusedSchur<double> fs64;
   FusedSchur<float> fs32;
+  // transposed operator matrices of the engine, per precision
+  struct EngMats {
+    const void *ZfT = nullptr, *Z1T = nullptr, *Z2T = nullptr, *Z3T = nullptr;
+    const void *D2ZiT = nullptr, *ZiT = nullptr, *DZiT = nullptr;
+    const void *tVT = nullptr, *tVDT = nullptr, *tD2T = nullptr, *tViT = nullptr;
+  } em32, em64;
+  template <class To>
+  const To* dev_transposed(const double* in, long long rows, long long cols, int batch) {
+    To* out = mem.alloc<To>((size_t)rows * cols * batch);
+    transpose_as(ctx, in, out, rows, cols, batch);
+    return out;
+  }
   FusedTheta<double> ft64;
   FusedTheta<float> ft32;
   float *dE32 = nullptr, *dUx32 = nullptr, *dUz32 = nullptr;
@@ -291,11 +312,17 @@ struct Model {
   long long n_outer = 0;
   int matvec_variant = 0;   // smc_schur_matvec: 0 plain, 1 fused FP64, 2 fused FP32
   bool inner_fp32 = true;   // fast form: FP32 inner Krylov operators + FP64 refinement
+  double inner_floor = 1e-4; // smallest relative tolerance asked of an FP32 inner solve
+  double theta_lag = 0.1;    // fast form: relative a0 change before the theta preconditioner is rebuilt
+  long long n_theta_lag_hits = 0;
+  long long n_fp64_fallback = 0;     // fast form: inner FP32 solves redone in FP64
   bool use_engine = true;   // fast form: Krylov solves in the persistent on-device engine
   EngineIO eio;
   float* dKx32 = nullptr;
-  float2* dTheta32 = nullptr;
   int* dEngInt = nullptr;
+  bool eng_phase = false;            // per-phase cycle counts of engine solves into the profiler
+  long long* dEngPhase = nullptr;    // ENGINE_PHASES accumulators
+  double sm_khz = 0.0;               // peak SM clock (cycles -> ms)
 
   // ------------------------------------------------------------ utilities
   void sync_read(const double* d, int count) {
@@ -340,6 +367,16 @@ struct Model {
     double key = std::round(lam * 1e10) / 1e10;
     for (auto& s : lam_slots)
       if (s.used && s.key == key) return s;
+    // fast form: the preconditioner of the temperature solve may lag a0 by
+    // a small relative amount (the solve's residual is still enforced in FP64)
+    if (fast && theta_lag > 0.0) {
+      LamSlot* best = nullptr;
+      for (auto& s : lam_slots)
+        if (s.used && std::fabs(s.key - key) <= theta_lag * std::fabs(key) &&
+            (!best || std::fabs(s.key - key) < std::fabs(best->key - key)))
+          best = &s;
+      if (best) { ++n_theta_lag_hits; return *best; }
+    }
     int used = 0;
     for (auto& s : lam_slots) used += s.used;
     if (used >= 4)
@@ -347,9 +384,14 @@ struct Model {
     LamSlot* slot = nullptr;
     for (auto& s : lam_slots)
       if (!s.used) { slot = &s; break; }
+    ProfScope ps(ctx, "theta_lu_build");
     tau_ops(ctx, dD2, dkx, lam, slot->LU, N, Nk);
     lu_small_batched(ctx, slot->LU, slot->piv, nullptr, N, Nk);
-    if (fast) green_from_lu(ctx, slot->LU, slot->piv, slot->Ginv, N, Nk);
+    if (fast) {
+      green_from_lu(ctx, slot->LU, slot->piv, slot->Ginv, N, Nk);
+      transpose_split(ctx, slot->Ginv, slot->GinvT32, N, N, Nk);
+      transpose_as(ctx, slot->Ginv, slot->GinvT64, N, N, Nk);
+    }
     slot->key = key;
     slot->used = true;
     return *slot;
@@ -405,7 +447,11 @@ struct Model {
     for (auto& s : lam_slots) {
       s.LU = mem.alloc<double>(Nk * NN);
       s.piv = mem.alloc<int>(Nk * N);
-      if (fast) s.Ginv = mem.alloc<double>(Nk * NN);
+      if (fast) {
+        s.Ginv = mem.alloc<double>(Nk * NN);
+        s.GinvT32 = mem.alloc<float2>(Nk * NN);
+        s.GinvT64 = mem.alloc<double>(Nk * NN);
+      }
     }
     dLU0 = mem.alloc<double>(Nk * NN);
     dPiv0 = mem.alloc<int>(Nk * N);
@@ -459,17 +505,24 @@ struct Model {
         eio.y = mem.alloc<double2>(mr + 1);
         eio.cs = mem.alloc<double>(mr + 1);
         eio.part = mem.alloc<double2>((size_t)2 * gmax * (mr + 1));
-        eio.npart = mem.alloc<double>(gmax);
+        eio.npart = mem.alloc<double>(2 * gmax);
         dEngInt = mem.alloc<int>(8);
         eio.flag = dEngInt;
         eio.result = dEngInt + 4;
         eio.V = dKV; eio.Z = dKZ; eio.w = dKw; eio.r = dKr;
+        dEngPhase = mem.alloc<long long>(ENGINE_PHASES);
+        {
+          int khz = 0;
+          SMC_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, device));
+          sm_khz = khz > 0 ? (double)khz : 2.0e6;
+        }
         dKx32 = mem.alloc<float>(Nk);
         to_float(ctx, dkx, dKx32, Nk);
-        dTheta32 = mem.alloc<float2>(n);
       }
       dRedLU = mem.alloc<double>(Nk * NN); dRedPiv = mem.alloc<int>(Nk * N);
       dRedG = mem.alloc<double>(Nk * NN);
+      dRedGT32 = mem.alloc<float2>(Nk * NN);
+      dRedGT64 = mem.alloc<double>(Nk * NN);
       dM0 = mem.alloc<double>(NN); dDM0 = mem.alloc<double>(NN);
       dT1 = mem.alloc<double>(NN); dT2 = mem.alloc<double>(NN); dT3 = mem.alloc<double>(NN);
       dComm = mem.alloc<double>(NN); dCommG = mem.alloc<double>(Nk * NN);
@@ -638,6 +691,14 @@ struct Model {
         ft32.tw = dev_copy_as<float>(reinterpret_cast<const double*>(dtwNp), 2LL * Np);
       }
     }
+    em64.tVT = dev_transposed<double>(dV, N, N, 1);
+    em64.tVDT = dev_transposed<double>(dVD, N, N, 1);
+    em64.tD2T = dev_transposed<double>(dD2, N, N, 1);
+    em64.tViT = dev_transposed<double>(dVi, N, N, 1);
+    em32.tVT = dev_transposed<float>(dV, N, N, 1);
+    em32.tVDT = dev_transposed<float>(dVD, N, N, 1);
+    em32.tD2T = dev_transposed<float>(dD2, N, N, 1);
+    em32.tViT = dev_transposed<float>(dVi, N, N, 1);
     dUx32 = mem.alloc<float>((size_t)Np * N);
     dUz32 = mem.alloc<float>((size_t)Np * N);
     dFtX = mem.alloc<double2>((size_t)2 * n);
@@ -674,6 +735,20 @@ struct Model {
     fs32.DZi = dev_copy_as<float>(DZi, MN);
     fs32.tw = dev_copy_as<float>(reinterpret_cast<const double*>(psplan.tw), 2LL * L);
     fs32.vbuf = mem.alloc<float2>(n);
+    em64.ZfT = dev_transposed<double>(psplan.Zf, Mz, N, 1);
+    em64.Z1T = dev_transposed<double>(Z1, Mz, N, Nk);
+    em64.Z2T = dev_transposed<double>(Z2, Mz, N, Nk);
+    em64.Z3T = dev_transposed<double>(Z3, Mz, N, Nk);
+    em64.D2ZiT = dev_transposed<double>(D2Zi, N, Mz, 1);
+    em64.ZiT = dev_transposed<double>(psplan.Zi, N, Mz, 1);
+    em64.DZiT = dev_transposed<double>(DZi, N, Mz, 1);
+    em32.ZfT = dev_transposed<float>(psplan.Zf, Mz, N, 1);
+    em32.Z1T = dev_transposed<float>(Z1, Mz, N, Nk);
+    em32.Z2T = dev_transposed<float>(Z2, Mz, N, Nk);
+    em32.Z3T = dev_transposed<float>(Z3, Mz, N, Nk);
+    em32.D2ZiT = dev_transposed<float>(D2Zi, N, Mz, 1);
+    em32.ZiT = dev_transposed<float>(psplan.Zi, N, Mz, 1);
+    em32.DZiT = dev_transposed<float>(DZi, N, Mz, 1);
     dE32 = mem.alloc<float>((size_t)L * Mz);
     dFsFv = mem.alloc<double2>((size_t)4 * Nk * Mz);
     dFsHv = mem.alloc<double2>((size_t)4 * Nk * Mz);
@@ -709,42 +784,46 @@ struct Model {
 
   // one FGMRES solve in the persistent engine; kind 0 = Schur, 1 = theta
   FgmresResult engine_solve(int kind, bool fp32, const double2* b, double2* x, double rtol,
-                            int restart, int maxiter, const double* Gp, double palpha) {
+                            int restart, int maxiter, const void* GpT, double palpha) {
     ProfScope ps(ctx, kind == 0 ? "engine_stokes" : "engine_theta");
+    const EngMats& em = fp32 ? em32 : em64;
     EngineOps op;
     op.kind = kind; op.Nk = Nk; op.N = N; op.kx = dkx; op.V64 = dV;
-    op.Gp = Gp; op.palpha = palpha;
+    op.GpT = GpT; op.palpha = palpha;
     op.kxT = fp32 ? (const void*)dKx32 : (const void*)dkx;
     if (kind == 0) {
       op.Mz = psplan.Mz; op.L = psplan.L;
-      if (fp32) {
-        op.Zf = fs32.Zf; op.Z1 = fs32.Z1; op.Z2 = fs32.Z2; op.Z3 = fs32.Z3;
-        op.Zi = fs32.Zi; op.D2Zi = fs32.D2Zi; op.DZi = fs32.DZi; op.E = dE32; op.twS = fs32.tw;
-        op.vT = fs32.vbuf;
-      } else {
-        op.Zf = fs64.Zf; op.Z1 = fs64.Z1; op.Z2 = fs64.Z2; op.Z3 = fs64.Z3;
-        op.Zi = fs64.Zi; op.D2Zi = fs64.D2Zi; op.DZi = fs64.DZi; op.E = dPsE; op.twS = fs64.tw;
-      }
+      op.ZfT = em.ZfT; op.Z1T = em.Z1T; op.Z2T = em.Z2T; op.Z3T = em.Z3T;
+      op.D2ZiT = em.D2ZiT; op.ZiT = em.ZiT; op.DZiT = em.DZiT;
+      if (fp32) { op.E = dE32; op.twS = fs32.tw; }
+      else { op.E = dPsE; op.twS = fs64.tw; }
       op.Fv = dFsFv; op.Hv = dFsHv;
     } else {
       op.Np = Np; op.a0 = a0;
-      if (fp32) {
-        op.tV = ft32.V; op.tVD = ft32.VD; op.tD2 = ft32.D2; op.tVi = ft32.Vi; op.twT = ft32.tw;
-        op.ux = dUx32; op.uz = dUz32; op.vT = dTheta32;
-      } else {
-        op.tV = ft64.V; op.tVD = ft64.VD; op.tD2 = ft64.D2; op.tVi = ft64.Vi; op.twT = ft64.tw;
-        op.ux = gr[0]; op.uz = gr[1];
-      }
+      op.tVT = em.tVT; op.tVDT = em.tVDT; op.tD2T = em.tD2T; op.tViT = em.tViT;
+      if (fp32) { op.twT = ft32.tw; op.ux = dUx32; op.uz = dUz32; }
+      else { op.twT = ft64.tw; op.ux = gr[0]; op.uz = gr[1]; }
       op.X = dFtX; op.A = dFtA;
     }
     EngineIO io = eio;
     io.b = b; io.x = x; io.rtol = rtol; io.n = n;
     io.restart = std::max(1, std::min(restart, mmax));
     io.maxiter = maxiter;
+    const bool phases = eng_phase && prof.enabled;
+    if (phases) {
+      SMC_CUDA(cudaMemsetAsync(dEngPhase, 0, ENGINE_PHASES * sizeof(long long), stream));
+      io.phase_cycles = dEngPhase;
+    }
     fgmres_engine(ctx, op, io, fp32);
     int res[2];
+    long long cyc[ENGINE_PHASES];
     SMC_CUDA(cudaMemcpyAsync(res, eio.result, sizeof(res), cudaMemcpyDeviceToHost, stream));
+    if (phases)
+      SMC_CUDA(cudaMemcpyAsync(cyc, dEngPhase, sizeof(cyc), cudaMemcpyDeviceToHost, stream));
     SMC_CUDA(cudaStreamSynchronize(stream));
+    if (phases)
+      for (int q = 0; q < ENGINE_PHASES; ++q)
+        prof.add(engine_phase_names[kind][q], (double)cyc[q] / sm_khz, 1);
     FgmresResult fr;
     fr.info = res[0];
     fr.iters = res[1];
@@ -768,17 +847,19 @@ struct Model {
     for (int outer = 0; outer < 12; ++outer) {
       if (beta <= tol) { res.info = 0; break; }
       if (total >= maxiter) break;
-      const double inner_rtol = std::max(0.3 * tol / beta, 2e-6);
+      const double inner_rtol = std::max(0.3 * tol / beta, inner_floor);
       FgmresResult fr = inner(dRefR, dRefE, inner_rtol, maxiter - total);
       total += fr.iters;
+      if (fr.info == 3) { res.info = 3; break; }   // non-finite data in the inner solve
       vec_axpby(ctx, x, make_double2(1.0, 0.0), dRefE, make_double2(1.0, 0.0), n);
       A64(x, dRefR);
       vec_axpby(ctx, dRefR, make_double2(1.0, 0.0), b, make_double2(-1.0, 0.0), n);
       beta = norm(dRefR);
       n_outer++;
+      if (!std::isfinite(beta)) { res.info = 3; break; }
       if (fr.iters == 0 && beta > tol) break;     // no progress possible
     }
-    if (beta <= tol) res.info = 0;
+    if (beta <= tol && res.info != 3) res.info = 0;
     res.iters = total;
     if (true_res) *true_res = beta / std::max(bn, 1e-300);
     return res;
@@ -997,8 +1078,13 @@ struct Model {
       bfbt_age = 1;
     }
     ++n_bfbt_builds;
+    ProfScope ps(ctx, "bfbt_build");
     build_reduced_lu(dBfbtRhs, dRedLU, dRedPiv);
-    if (fast) green_from_lu(ctx, dRedLU, dRedPiv, dRedG, N, Nk);
+    if (fast) {
+      green_from_lu(ctx, dRedLU, dRedPiv, dRedG, N, Nk);
+      transpose_split(ctx, dRedG, dRedGT32, N, N, Nk);
+      transpose_as(ctx, dRedG, dRedGT64, N, N, Nk);
+    }
   }
   void to_complex(const double* in, double2* out, int count);
 
@@ -1026,14 +1112,14 @@ struct Model {
       if (inner_fp32) {
         InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
           if (use_engine)
-            return engine_solve(0, true, r, e, tol, cfg.stokes_restart, mi, dRedG, 1.0);
+            return engine_solve(0, true, r, e, tol, cfg.stokes_restart, mi, dRedGT32, 1.0);
           return fgmres(A32, M, r, e, tol, cfg.stokes_restart, mi);
         };
         fr = fgmres_refined(A64, inner, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, &res);
       } else {
         if (use_engine)
           fr = engine_solve(0, false, dSb, x, cfg.stokes_rtol, cfg.stokes_restart,
-                            cfg.stokes_maxiter, dRedG, 1.0);
+                            cfg.stokes_maxiter, dRedGT64, 1.0);
         else
           fr = fgmres(A64, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
         schur_matvec_fast(x, dSAx, false);
@@ -1085,6 +1171,7 @@ struct Model {
 
   // memoised Stokes solve of the coupled model (coupled_model.py:725-765)
   void stokes_memo(const double2* th, double2* psi, double2* om) {
+    ProfScope psm(ctx, "stokes_memo_check");
     zop(dV, 0, th, sp[3]);
     if (memo_valid) {
       memo_compare(ctx, th, dMemoThat, sp[3], dMemoX, n, dScal, dRed);
@@ -1232,13 +1319,19 @@ struct Model {
     const double2* ps = dPsi;
     if (have_prev) { extrapolate(ctx, dPsi, dPsiPrev, dPsiStar, n); ps = dPsiStar; }
     // frozen velocity on the padded grid
-    KFactor mik; mik.cre = 0.0; mik.cim = -1.0; mik.kpow = 1;
-    synth(ps, dVD, KFactor(), gr[0], Np, sp[12]);
-    synth(ps, dV, mik, gr[1], Np, sp[12]);
+    {
+      ProfScope psa(ctx, "theta_rhs");
+      KFactor mik; mik.cre = 0.0; mik.cim = -1.0; mik.kpow = 1;
+      synth(ps, dVD, KFactor(), gr[0], Np, sp[12]);
+      synth(ps, dV, mik, gr[1], Np, sp[12]);
+    }
     const double2* phi = nullptr;
     if (cfg.dissipation_number != 0.0) { phi_source(ps, dPhi); phi = dPhi; }
     set_step(dt, have_prev, dt_prev);
-    theta_rhs(ctx, th2, dPrev, ps, phi, dkx, b0, b1, cfg.internal_heating, dKb, Nk, N);
+    {
+      ProfScope psa(ctx, "theta_rhs");
+      theta_rhs(ctx, th2, dPrev, ps, phi, dkx, b0, b1, cfg.internal_heating, dKb, Nk, N);
+    }
     Op A = [&](const double2* v, double2* o) { theta_matvec(v, o); };
     LamSlot* Lp = &lam_lu(a0);
     double* LU = Lp->LU;
@@ -1262,14 +1355,22 @@ struct Model {
       if (inner_fp32) {
         InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
           if (use_engine)
-            return engine_solve(1, true, r, e, tol, cfg.theta_restart, mi, Gi, -1.0);
+            return engine_solve(1, true, r, e, tol, cfg.theta_restart, mi, Lp->GinvT32, -1.0);
           return fgmres(A32, M, r, e, tol, cfg.theta_restart, mi);
         };
         fr = fgmres_refined(A64, inner, dKb, dRhs, cfg.theta_rtol, cfg.theta_maxiter, &tr);
+        if (fr.info == 3) {
+          // non-finite values in the FP32 inner solves: redo the solve in FP64
+          ++n_fp64_fallback;
+          fr = fgmres(A64, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
+          theta_matvec_fast(dRhs, sp[13], false);
+          vec_axpby(ctx, sp[13], make_double2(1.0, 0.0), dKb, make_double2(-1.0, 0.0), n);
+          tr = norm(sp[13]) / std::max(norm(dKb), 1e-300);
+        }
       } else {
         if (use_engine)
           fr = engine_solve(1, false, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart,
-                            cfg.theta_maxiter, Gi, -1.0);
+                            cfg.theta_maxiter, Lp->GinvT64, -1.0);
         else
           fr = fgmres(A64, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
         theta_matvec_fast(dRhs, sp[13], false);
@@ -1594,8 +1695,14 @@ int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety,
     double dt = NAN;
     long long steps = 0;
     while (m.t_resident < tstop && (max_steps <= 0 || steps < max_steps)) {
-      dt = m.production_dt(cur, safety, dtmax);
-      m.step(cur, nxt, dt);
+      {
+        smc::ProfScope ps(m.ctx, "step.dt_select");
+        dt = m.production_dt(cur, safety, dtmax);
+      }
+      {
+        smc::ProfScope ps(m.ctx, "step.advance");
+        m.step(cur, nxt, dt);
+      }
       std::swap(cur, nxt);
       m.resident_cur0 = !m.resident_cur0;
       m.t_resident += dt;
@@ -1748,6 +1855,14 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
       h->m.inner_fp32 = value != 0.0;
     } else if (k == "krylov_engine") {
       h->m.use_engine = value != 0.0;
+    } else if (k == "theta_precond_lag") {
+      if (!(value >= 0.0 && value < 1.0)) throw std::runtime_error("theta_precond_lag must be in [0, 1)");
+      h->m.theta_lag = value;
+    } else if (k == "inner_rtol_floor") {
+      if (!(value > 0.0 && value < 1.0)) throw std::runtime_error("inner_rtol_floor must be in (0, 1)");
+      h->m.inner_floor = value;
+    } else if (k == "engine_phase_profile") {
+      h->m.eng_phase = value != 0.0;
     } else throw std::runtime_error("unknown option " + k);
   })
 }

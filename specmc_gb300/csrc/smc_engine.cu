@@ -4,9 +4,12 @@
 // least-squares update -- with no host round trip per iteration.
 //
 // Operators: the fused Schur matvec (stokes/lagged_stokes.py:202-220) or the
-// fused temperature matvec (implicit_theta.py:354-383), in working precision
-// T (float: the inner solves of the mixed form; double: FP64).  Krylov
-// vectors, the Hessenberg matrix and the Givens data stay FP64.
+// fused temperature matvec (implicit_theta.py:354-383).  Everything of the
+// Krylov process -- basis vectors, dot products, Hessenberg matrix, Givens
+// rotations -- is carried in the working precision T: float for the inner
+// solves of the mixed form (which only have to reach a relative residual of
+// about 1e-4 before the FP64 refinement takes over), double for a solve in
+// FP64.  Only the right-hand side b and the solution x are FP64.
 //
 // Work decomposition.  Both operators have the shape
 //     per-k z-contraction -> per-z-point x-convolution -> per-k z-epilogue,
@@ -20,12 +23,11 @@
 //   XCONV  x-direction convolution                          (per z-point)
 //   POST   w = z-epilogue, first-pass dots V^H w            (per k, rows)
 //   UPDATE w' = w - V h1, second-pass dots V^H w', ||w'||^2 (per k, rows)
-// The norm of w'' = w' - V h2 follows from ||w''||^2 = ||w'||^2 - ||h2||^2
-// (h2 is orthogonal-projection data, so this is exact up to rounding); when
-// that difference loses more than four digits an exact norm is taken with
-// one extra barrier.  Every CTA reduces the per-CTA dot partials in the same
-// order and runs the Givens update itself, so all CTAs hold identical
-// coefficients and take identical branches.
+// The norm of w'' = w' - V h2 follows from ||w''||^2 = ||w'||^2 - ||h2||^2;
+// when that difference cancels badly an exact norm is taken with one extra
+// barrier.  Every CTA reduces the per-CTA dot partials in the same order and
+// runs the Givens update itself, so all CTAs hold identical coefficients and
+// take identical branches.
 //
 // Uniform control: every branch that decides how many grid barriers a CTA
 // executes depends only on values every CTA computes identically from the
@@ -46,6 +48,7 @@ namespace smc {
 template <class T> struct CT2;
 template <> struct CT2<double> { using type = double2; };
 template <> struct CT2<float> { using type = float2; };
+template <class T> using Cx = typename CT2<T>::type;
 
 static constexpr int ENG_THREADS = 256;
 static constexpr int ENG_WARPS = ENG_THREADS / 32;
@@ -57,11 +60,13 @@ struct EngCtx {
   int R, ntask;                        // CTAs per Fourier row, row tasks
 };
 
-const char* const engine_phase_names[2][ENGINE_PHASES] = {
-    {"engine_stokes.start", "engine_stokes.xconv", "engine_stokes.post", "engine_stokes.update",
-     "engine_stokes.exact_norm", "engine_stokes.next", "engine_stokes.lsq", "engine_stokes.resid"},
-    {"engine_theta.start", "engine_theta.xconv", "engine_theta.post", "engine_theta.update",
-     "engine_theta.exact_norm", "engine_theta.next", "engine_theta.lsq", "engine_theta.resid"}};
+#define SMC_PHASE_NAMES(P)                                                                   \
+  {P ".start", P ".xconv", P ".xconv_wait", P ".post", P ".post_wait", P ".update_reduce",      \
+   P ".update", P ".update_wait", P ".exact_norm", P ".next_reduce", P ".givens", P ".combine", \
+   P ".precond", P ".contract", P ".next_wait", P ".lsq", P ".resid"}
+const char* const engine_phase_names[2][ENGINE_PHASES] = {SMC_PHASE_NAMES("engine_stokes"),
+                                                          SMC_PHASE_NAMES("engine_theta")};
+#undef SMC_PHASE_NAMES
 
 // phase timer of CTA 0 / thread 0: cycles since the previous mark go to slot
 struct PhaseClock {
@@ -89,53 +94,71 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// ------------------------------------------------- complex arithmetic in T
 template <class T>
-__device__ __forceinline__ typename CT2<T>::type mk2(T a, T b) {
-  typename CT2<T>::type r;
+__device__ __forceinline__ Cx<T> mk2(T a, T b) {
+  Cx<T> r;
   r.x = a;
   r.y = b;
   return r;
 }
+template <class T> __device__ __forceinline__ Cx<T> x_add(Cx<T> a, Cx<T> b) { return mk2<T>(a.x + b.x, a.y + b.y); }
+template <class T> __device__ __forceinline__ Cx<T> x_sub(Cx<T> a, Cx<T> b) { return mk2<T>(a.x - b.x, a.y - b.y); }
+template <class T> __device__ __forceinline__ Cx<T> x_mul(Cx<T> a, Cx<T> b) {
+  return mk2<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <class T> __device__ __forceinline__ Cx<T> x_scale(Cx<T> a, T s) { return mk2<T>(a.x * s, a.y * s); }
+template <class T> __device__ __forceinline__ Cx<T> x_conj(Cx<T> a) { return mk2<T>(a.x, -a.y); }
+// a / b, Smith's scaling
+template <class T> __device__ __forceinline__ Cx<T> x_div(Cx<T> a, Cx<T> b) {
+  if (fabs(b.x) >= fabs(b.y)) {
+    const T r = b.y / b.x, d = b.x + b.y * r;
+    return mk2<T>((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+  }
+  const T r = b.x / b.y, d = b.y + b.x * r;
+  return mk2<T>((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
+template <class T> __device__ __forceinline__ T x_abs(Cx<T> a) { return hypot(a.x, a.y); }
 
 // per-CTA shared-memory rows of the per-k phases (carved from dynamic smem;
 // the x-convolution phases reuse the same bytes from offset 0)
 template <class T>
 struct EngSmem {
-  using C = typename CT2<T>::type;
-  double2* v;     // N   FP64 row (basis row / epilogue input)
-  double2* w;     // N   FP64 epilogue outputs of the owned rows
-  C* vt;          // N   row in T (preconditioner input; the high part for T = float)
-  C* vlo;         // N   low part of the row (T = float: v - (double) vt)
-  C* z;           // N   preconditioned row in T (contraction input)
-  C* aux;         // max(3 Mz, N) epilogue vectors
-  C* out;         // 4 RCH GEMV results
-  void* red;      // ENG_WARPS * max(4 RCH sizeof(C), RCH sizeof(double2)) partials
+  using C = Cx<T>;
+  C* v;       // N   row being formed (basis row / epilogue input)
+  C* w;       // N   epilogue outputs / updated rows of the task
+  C* z;       // N   preconditioned row (contraction input)
+  C* aux;     // max(3 Mz, N) epilogue vectors
+  C* out;     // 4 RCH GEMV results
+  void* red;  // warp partials
 };
 
 __host__ __device__ inline size_t eng_align(size_t b) { return (b + 255) & ~(size_t)255; }
 
 template <class T>
+__host__ __device__ inline size_t eng_red_bytes() {
+  using C = Cx<T>;
+  const size_t a = (size_t)ENG_WARPS * 4 * RCH * sizeof(C);      // 4-matrix GEMV partials
+  const size_t b = (size_t)ENG_WARPS * RCH * 16;                  // double-float / FP64 partials
+  return a > b ? a : b;
+}
+
+template <class T>
 __host__ __device__ inline size_t eng_rows_bytes(int N, int Mz) {
-  using C = typename CT2<T>::type;
-  const size_t NN = (size_t)N;
+  using C = Cx<T>;
   const size_t aux = (size_t)(3 * Mz > N ? 3 * Mz : N);
-  const size_t redc = (size_t)ENG_WARPS * 4 * RCH * sizeof(C);
-  const size_t redd = (size_t)ENG_WARPS * RCH * sizeof(double2);
-  return eng_align(NN * sizeof(double2)) * 2 + eng_align(NN * sizeof(C)) * 3 +
-         eng_align(aux * sizeof(C)) + eng_align(4 * RCH * sizeof(C)) +
-         eng_align(redc > redd ? redc : redd);
+  return eng_align((size_t)N * sizeof(C)) * 3 + eng_align(aux * sizeof(C)) +
+         eng_align(4 * RCH * sizeof(C)) + eng_align(eng_red_bytes<T>());
 }
 
 template <class T>
 __device__ EngSmem<T> eng_carve(unsigned char* base, int N, int Mz) {
-  using C = typename CT2<T>::type;
+  using C = Cx<T>;
   EngSmem<T> S;
   size_t o = 0;
   const int aux = 3 * Mz > N ? 3 * Mz : N;
-  S.v = reinterpret_cast<double2*>(base + o); o += eng_align((size_t)N * sizeof(double2));
-  S.w = reinterpret_cast<double2*>(base + o); o += eng_align((size_t)N * sizeof(double2));
-  S.vt = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
-  S.vlo = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
+  S.v = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
+  S.w = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
   S.z = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
   S.aux = reinterpret_cast<C*>(base + o); o += eng_align((size_t)aux * sizeof(C));
   S.out = reinterpret_cast<C*>(base + o); o += eng_align(4 * RCH * sizeof(C));
@@ -150,13 +173,13 @@ __device__ EngSmem<T> eng_carve(unsigned char* base, int N, int Mz) {
 template <class T, int NM>
 struct GemvArgs {
   const T* a[NM];
-  const typename CT2<T>::type* x[NM];
+  const Cx<T>* x[NM];
 };
 
 template <class T, int NM>
 __device__ void tgemv_chunk(const GemvArgs<T, NM>& g, long long ld, int r0, int nr, int ncol,
                             EngSmem<T>& S, const EngCtx& e) {
-  using C = typename CT2<T>::type;
+  using C = Cx<T>;
   C* red = reinterpret_cast<C*>(S.red);
   for (int rc = 0; rc < nr; rc += 32) {
     const int r = rc + e.lane;
@@ -192,39 +215,40 @@ __device__ void tgemv_chunk(const GemvArgs<T, NM>& g, long long ld, int r0, int 
   __syncthreads();
 }
 
-// y[r] = (base[off + r] - sum_{i<mm} c_i V_i[off + r]) * scale for r < nr,
-// FP64; warps over i, lanes over r.  Results go to the shared row y and/or
-// to global gout[off + r].  Ends with __syncthreads.
+// y[r] = (base[off + r] - sum_{i<mm} c_i V_i[off + r]) * scale for r < nr;
+// warps over i, lanes over r.  Results go to the shared row y and/or to
+// global gout[off + r].  Ends with __syncthreads.
 template <class T>
-__device__ void combine_rows(const double2* base, const double2* V, long long n, long long off,
-                             int nr, const double2* c, int mm, double scale, double2* y,
-                             double2* gout, EngSmem<T>& S, const EngCtx& e) {
-  double2* red = reinterpret_cast<double2*>(S.red);
+__device__ void combine_rows(const Cx<T>* base, const Cx<T>* V, long long n, long long off, int nr,
+                             const Cx<T>* c, int mm, T scale, Cx<T>* y, Cx<T>* gout,
+                             EngSmem<T>& S, const EngCtx& e) {
+  using C = Cx<T>;
+  C* red = reinterpret_cast<C*>(S.red);
   for (int r0 = 0; r0 < nr; r0 += RCH) {
     const int cnt = min(RCH, nr - r0);
     for (int rc = 0; rc < cnt; rc += 32) {
       const int r = rc + e.lane;
-      double sr = 0.0, si = 0.0;
+      T sr = (T)0, si = (T)0;
       if (r < cnt) {
 #pragma unroll 4
         for (int i = e.warp; i < mm; i += ENG_WARPS) {
-          const double2 v = V[(long long)i * n + off + r0 + r];
-          const double2 ci = c[i];
+          const C v = V[(long long)i * n + off + r0 + r];
+          const C ci = c[i];
           sr += ci.x * v.x - ci.y * v.y;
           si += ci.x * v.y + ci.y * v.x;
         }
       }
-      red[e.warp * RCH + r] = make_double2(sr, si);
+      red[e.warp * RCH + r] = mk2<T>(sr, si);
     }
     __syncthreads();
     for (int r = e.tid; r < cnt; r += blockDim.x) {
-      double sr = 0.0, si = 0.0;
+      T sr = (T)0, si = (T)0;
       for (int w = 0; w < ENG_WARPS; ++w) {
         sr += red[w * RCH + r].x;
         si += red[w * RCH + r].y;
       }
-      const double2 bv = base ? base[off + r0 + r] : make_double2(0.0, 0.0);
-      const double2 o = make_double2((bv.x - sr) * scale, (bv.y - si) * scale);
+      const C bv = base ? base[off + r0 + r] : mk2<T>((T)0, (T)0);
+      const C o = mk2<T>((bv.x - sr) * scale, (bv.y - si) * scale);
       if (y) y[r0 + r] = o;
       if (gout) gout[off + r0 + r] = o;
     }
@@ -232,19 +256,21 @@ __device__ void combine_rows(const double2* base, const double2* V, long long n,
   }
 }
 
-// acc[i] += sum_{r<nr} conj(V_i[off + r]) y[r] for i < mm (y shared, FP64):
-// warps over i in batches of four (independent loads), lanes over r
-__device__ void dots_acc(const double2* V, long long n, long long off, int nr, const double2* y,
-                         int mm, double2* acc, const EngCtx& e) {
+// acc[i] += sum_{r<nr} conj(V_i[off + r]) y[r] for i < mm: warps over i in
+// batches of four (independent loads), lanes over r
+template <class T>
+__device__ void dots_acc(const Cx<T>* V, long long n, long long off, int nr, const Cx<T>* y, int mm,
+                         Cx<T>* acc, const EngCtx& e) {
+  using C = Cx<T>;
   for (int i0 = e.warp; i0 < mm; i0 += 4 * ENG_WARPS) {
-    double sr[4] = {0.0, 0.0, 0.0, 0.0}, si[4] = {0.0, 0.0, 0.0, 0.0};
+    T sr[4] = {0, 0, 0, 0}, si[4] = {0, 0, 0, 0};
     for (int r = e.lane; r < nr; r += 32) {
-      const double2 x = y[r];
+      const C x = y[r];
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
         const int i = i0 + t * ENG_WARPS;
         if (i < mm) {
-          const double2 a = V[(long long)i * n + off + r];
+          const C a = V[(long long)i * n + off + r];
           sr[t] += a.x * x.x + a.y * x.y;
           si[t] += a.x * x.y - a.y * x.x;
         }
@@ -253,22 +279,26 @@ __device__ void dots_acc(const double2* V, long long n, long long off, int nr, c
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int i = i0 + t * ENG_WARPS;
-      const double a = warp_sum(sr[t]), b = warp_sum(si[t]);
-      if (e.lane == 0 && i < mm) acc[i] = make_double2(acc[i].x + a, acc[i].y + b);
+      const T a = warp_sum(sr[t]), b = warp_sum(si[t]);
+      if (e.lane == 0 && i < mm) acc[i] = mk2<T>(acc[i].x + a, acc[i].y + b);
     }
   }
 }
 
-// out[i] = sum_{g<G} pp[i G + g] for i < mm, the same order in every CTA
-__device__ void reduce_parts(const double2* pp, int G, int mm, double2* out, const EngCtx& e) {
+// out[i] = sum_{g<G} pp[i G + g] for i < mm, the same order in every CTA;
+// the partial loads of a lane are unrolled so that they are in flight together
+template <class T>
+__device__ void reduce_parts(const Cx<T>* pp, int G, int mm, Cx<T>* out, const EngCtx& e) {
+  using C = Cx<T>;
   for (int i0 = e.warp; i0 < mm; i0 += 4 * ENG_WARPS) {
-    double sr[4] = {0.0, 0.0, 0.0, 0.0}, si[4] = {0.0, 0.0, 0.0, 0.0};
+    T sr[4] = {0, 0, 0, 0}, si[4] = {0, 0, 0, 0};
+#pragma unroll 10
     for (int g = e.lane; g < G; g += 32) {
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
         const int i = i0 + t * ENG_WARPS;
         if (i < mm) {
-          const double2 q = pp[(size_t)i * G + g];
+          const C q = pp[(size_t)i * G + g];
           sr[t] += q.x;
           si[t] += q.y;
         }
@@ -277,53 +307,37 @@ __device__ void reduce_parts(const double2* pp, int G, int mm, double2* out, con
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int i = i0 + t * ENG_WARPS;
-      const double a = warp_sum(sr[t]), b = warp_sum(si[t]);
-      if (e.lane == 0 && i < mm) out[i] = make_double2(a, b);
+      const T a = warp_sum(sr[t]), b = warp_sum(si[t]);
+      if (e.lane == 0 && i < mm) out[i] = mk2<T>(a, b);
     }
   }
 }
 
 // sum_{g<G} p[g], the same order in every CTA; ends with __syncthreads
-__device__ double reduce_scalar(const double* p, int G, double* sh, const EngCtx& e) {
+template <class T>
+__device__ T reduce_scalar(const T* p, int G, T* sh, const EngCtx& e) {
   if (e.warp == 0) {
-    double a = 0.0;
+    T a = (T)0;
+#pragma unroll 10
     for (int g = e.lane; g < G; g += 32) a += p[g];
     a = warp_sum(a);
     if (e.lane == 0) sh[0] = a;
   }
   __syncthreads();
-  const double r = sh[0];
+  const T r = sh[0];
   __syncthreads();
   return r;
 }
 
-// sum over the CTA's threads of |y[r]|^2, r < nr, added to *acc by thread 0
-__device__ void norm_acc(const double2* y, int nr, double* acc, const EngCtx& e) {
+// sum over the CTA of |y[r]|^2, r < nr, added to *acc by warp 0 / lane 0
+template <class T>
+__device__ void norm_acc(const Cx<T>* y, int nr, T* acc, const EngCtx& e) {
   if (e.warp == 0) {
-    double s = 0.0;
+    T s = (T)0;
     for (int r = e.lane; r < nr; r += 32) s += y[r].x * y[r].x + y[r].y * y[r].y;
     s = warp_sum(s);
     if (e.lane == 0) *acc += s;
   }
-}
-
-// ||x|| over the grid (one barrier); every CTA returns the same value
-__device__ double grid_norm(const double2* x, long long n, double* part, const EngCtx& e,
-                            cg::grid_group& grid, double* sh) {
-  const long long per = (n + e.G - 1) / e.G;
-  const long long lo = (long long)e.b * per, hi = min(n, lo + per);
-  double s = 0.0;
-  for (long long t = lo + e.tid; t < hi; t += blockDim.x) s += x[t].x * x[t].x + x[t].y * x[t].y;
-  s = warp_sum(s);
-  if (e.lane == 0) sh[1 + e.warp] = s;
-  __syncthreads();
-  if (e.tid == 0) {
-    double a = 0.0;
-    for (int q = 0; q < ENG_WARPS; ++q) a += sh[1 + q];
-    part[e.b] = a;
-  }
-  grid.sync();
-  return sqrt(reduce_scalar(part, e.G, sh, e));
 }
 
 // ----------------------------------------------------- x-direction phases
@@ -470,19 +484,21 @@ __device__ __forceinline__ void df_add(float& s, float& c, float p) {
   c += (s - (t - bp)) + (p - bp);
   s = t;
 }
-// (s, c) += (gh + gl)(xh + xl): exact product of the high parts (FMA), the
-// cross terms into the compensation; the lo*lo term (2^-48 relative) dropped
-__device__ __forceinline__ void df_mac(float& s, float& c, float gh, float gl, float xh, float xl) {
-  const float p = gh * xh;
-  const float pe = fmaf(gh, xh, -p);
+// (s, c) += (gh + gl) x for an FP32 x: exact product of the high part (FMA
+// error term), the low part's product into the compensation
+__device__ __forceinline__ void df_mac(float& s, float& c, float gh, float gl, float x) {
+  const float p = gh * x;
+  const float pe = fmaf(gh, x, -p);
   df_add(s, c, p);
-  c += pe + fmaf(gh, xl, gl * xh);
+  c += fmaf(gl, x, pe);
 }
 
-// z = palpha G_k v for the row task (k, sub) into S.z (T) and, from the sub-0
-// CTA, Z_jv (FP64).  T = double: FP64 GEMV.  T = float: double-float GEMV on
-// (hi, lo) pairs of G and of v (lanes over output rows, warps over columns,
-// warp partials merged with compensated adds in a fixed order).
+// z = palpha G_k v for the row task into S.z and (sub-0 CTA) Z_jv.
+// T = double: FP64 GEMV.  T = float: the row v is exact in FP32 and G comes
+// as (hi, lo) float pairs; the products G v cancel strongly for some rows, so
+// they are summed in double-float arithmetic (lanes over output rows, warps
+// over columns, warp partials merged with compensated adds in a fixed order)
+// and rounded to FP32 once at the end.
 template <class T>
 __device__ void precond_row(const EngineOps& op, const EngineIO& io, int k, int sub, int jv,
                             long long off, EngSmem<T>& S, const EngCtx& e);
@@ -491,16 +507,17 @@ template <>
 __device__ void precond_row<double>(const EngineOps& op, const EngineIO& io, int k, int sub, int jv,
                                     long long off, EngSmem<double>& S, const EngCtx& e) {
   const int N = op.N;
+  double2* Z = io.Z;
   GemvArgs<double, 1> g;
   g.a[0] = (const double*)op.GpT + (long long)k * N * N;
-  g.x[0] = S.vt;
+  g.x[0] = S.v;
   for (int r0 = 0; r0 < N; r0 += RCH) {
     const int nr = min(RCH, N - r0);
     tgemv_chunk<double, 1>(g, N, r0, nr, N, S, e);
     for (int r = e.tid; r < nr; r += blockDim.x) {
       const double2 zz = make_double2(op.palpha * S.out[r].x, op.palpha * S.out[r].y);
       S.z[r0 + r] = zz;
-      if (sub == 0) io.Z[(long long)jv * io.n + off + r0 + r] = zz;
+      if (sub == 0) Z[(long long)jv * io.n + off + r0 + r] = zz;
     }
   }
 }
@@ -510,7 +527,9 @@ __device__ void precond_row<float>(const EngineOps& op, const EngineIO& io, int 
                                    long long off, EngSmem<float>& S, const EngCtx& e) {
   const int N = op.N;
   const float2* G = (const float2*)op.GpT + (long long)k * N * N;
+  double2* Z = io.Z;
   float4* red = reinterpret_cast<float4*>(S.red);     // [warp][RCH] (re s, re c, im s, im c)
+  const float pa = (float)op.palpha;
   for (int r0 = 0; r0 < N; r0 += RCH) {
     const int nr = min(RCH, N - r0);
     for (int rc = 0; rc < nr; rc += 32) {
@@ -520,9 +539,9 @@ __device__ void precond_row<float>(const EngineOps& op, const EngineIO& io, int 
 #pragma unroll 4
         for (int c = e.warp; c < N; c += ENG_WARPS) {
           const float2 gg = G[(long long)c * N + r0 + r];
-          const float2 xh = S.vt[c], xl = S.vlo[c];
-          df_mac(sr, cr, gg.x, gg.y, xh.x, xl.x);
-          df_mac(si, ci, gg.x, gg.y, xh.y, xl.y);
+          const float2 x = S.v[c];
+          df_mac(sr, cr, gg.x, gg.y, x.x);
+          df_mac(si, ci, gg.x, gg.y, x.y);
         }
       }
       red[e.warp * RCH + r] = make_float4(sr, cr, si, ci);
@@ -537,54 +556,55 @@ __device__ void precond_row<float>(const EngineOps& op, const EngineIO& io, int 
         df_add(si, ci, q.z);
         ci += q.w;
       }
-      const double2 zz = make_double2(op.palpha * ((double)sr + (double)cr),
-                                      op.palpha * ((double)si + (double)ci));
-      S.z[r0 + r] = make_float2((float)zz.x, (float)zz.y);
-      if (sub == 0) io.Z[(long long)jv * io.n + off + r0 + r] = zz;
+      S.z[r0 + r] = make_float2(pa * (sr + cr), pa * (si + ci));
+      if (sub == 0)   // the full double-float value (the tau rows and x use it)
+        Z[(long long)jv * io.n + off + r0 + r] =
+            make_double2(op.palpha * ((double)sr + (double)cr), op.palpha * ((double)si + (double)ci));
     }
     __syncthreads();
   }
 }
 
 // ------------------------------------------------------------ row phases
-// prep: for each row task (k, sub): the FP64 row v_k of a new basis vector
+// prep: for each row task (k, sub): the row v_k of a new basis vector
 //   mode 0: v = r * scale                 (start of a cycle; writes V_jv, Z_jv)
 //   mode 1: v = (w - V coef) * scale      (Arnoldi step; writes V_jv, Z_jv)
 //   mode 2: v = x                         (true residual: no preconditioner)
 // then z = palpha G_k v (modes 0/1) and this sub's slice of the z-contraction.
 template <class T>
-__device__ void phase_prep(const EngineOps& op, const EngineIO& io, int mode, int jv, double scale,
-                           const double2* coef, int mm, EngSmem<T>& S, const EngCtx& e) {
-  using C = typename CT2<T>::type;
+__device__ void phase_prep(const EngineOps& op, const EngineIO& io, int mode, int jv, T scale,
+                           const Cx<T>* coef, int mm, EngSmem<T>& S, const EngCtx& e,
+                           PhaseClock* pc = nullptr, double scale64 = 1.0) {
+  using C = Cx<T>;
   const int Nk = op.Nk, N = op.N;
   const long long n = io.n;
   const T* kxT = (const T*)op.kxT;
+  C* V = reinterpret_cast<C*>(io.V);
+  const C* Wv = reinterpret_cast<const C*>(io.w);
+  const C* Rv = reinterpret_cast<const C*>(io.r);
   for (int t = e.b; t < e.ntask; t += e.G) {
     const int k = t / e.R, sub = t - (t / e.R) * e.R;
     const long long off = (long long)k * N;
     if (mode == 1) {
-      combine_rows<T>(io.w, io.V, n, off, N, coef, mm, scale, S.v, nullptr, S, e);
+      combine_rows<T>(Wv, V, n, off, N, coef, mm, scale, S.v, nullptr, S, e);
+      if (pc) pc->mark(EP_COMBINE);
+    } else if (mode == 0) {
+      for (int q = e.tid; q < N; q += blockDim.x) S.v[q] = x_scale<T>(Rv[off + q], scale);
+      __syncthreads();
     } else {
-      const double2* src = mode == 0 ? io.r : io.x;
-      const double sc = mode == 0 ? scale : 1.0;
       for (int q = e.tid; q < N; q += blockDim.x) {
-        const double2 a = src[off + q];
-        S.v[q] = make_double2(a.x * sc, a.y * sc);
+        const double2 a = io.x[off + q];
+        S.v[q] = mk2<T>((T)(a.x * scale64), (T)(a.y * scale64));
       }
       __syncthreads();
     }
     if (mode != 2) {
-      for (int q = e.tid; q < N; q += blockDim.x) {
-        const double2 a = S.v[q];
-        const C h = mk2<T>((T)a.x, (T)a.y);
-        S.vt[q] = h;
-        S.vlo[q] = mk2<T>((T)(a.x - (double)h.x), (T)(a.y - (double)h.y));
-        if (sub == 0) io.V[(long long)jv * n + off + q] = a;
-      }
-      __syncthreads();
+      if (sub == 0)
+        for (int q = e.tid; q < N; q += blockDim.x) V[(long long)jv * n + off + q] = S.v[q];
       precond_row<T>(op, io, k, sub, jv, off, S, e);
+      if (pc) pc->mark(EP_PRECOND);
     } else {
-      for (int q = e.tid; q < N; q += blockDim.x) S.z[q] = mk2<T>((T)S.v[q].x, (T)S.v[q].y);
+      for (int q = e.tid; q < N; q += blockDim.x) S.z[q] = S.v[q];
     }
     __syncthreads();
     const T kk = kxT[k];
@@ -610,9 +630,9 @@ __device__ void phase_prep(const EngineOps& op, const EngineIO& io, int mode, in
           const long long base = (long long)k * Mz + s0 + r;
           const C f0 = S.out[r], f1 = S.out[RCH + r], f2 = S.out[2 * RCH + r], f3 = S.out[3 * RCH + r];
           Fv[base] = f0;
-          Fv[KM + base] = mk2<T>(c1 * f1.x, c1 * f1.y);
+          Fv[KM + base] = x_scale<T>(f1, c1);
           Fv[2 * KM + base] = f2;
-          Fv[3 * KM + base] = mk2<T>(kk * f3.x, kk * f3.y);
+          Fv[3 * KM + base] = x_scale<T>(f3, kk);
         }
       }
     } else {
@@ -635,20 +655,22 @@ __device__ void phase_prep(const EngineOps& op, const EngineIO& io, int mode, in
       }
     }
     __syncthreads();
+    if (pc) pc->mark(EP_CONTRACT);
   }
 }
 
-// post: epilogue rows [p_lo, p_hi) of each row task; the input vector of the
-// operator is zin (FP64: Z_j, or x for a residual).  Arnoldi mode writes w
-// and adds V_i^H w (i < mm) to acc; residual mode writes r = b - A x and adds
-// ||r||^2 to *nacc.
+// post: epilogue rows [p_lo, p_hi) of each row task; the operator's input
+// vector is zin.  Arnoldi mode writes w and adds V_i^H w (i < mm) to acc;
+// residual mode (zin = x, FP64) writes r = b - A x and adds ||r||^2 to *nacc.
 template <class T>
 __device__ void phase_post(const EngineOps& op, const EngineIO& io, bool resid, const double2* zin,
-                           int mm, EngSmem<T>& S, double2* acc, double* nacc, const EngCtx& e) {
-  using C = typename CT2<T>::type;
+                           double zscale, int mm, EngSmem<T>& S, Cx<T>* acc, T* nacc,
+                           const EngCtx& e) {
+  using C = Cx<T>;
   const int Nk = op.Nk, N = op.N;
   const long long n = io.n;
   const T* kxT = (const T*)op.kxT;
+  const C* V = reinterpret_cast<const C*>(io.V);
   for (int t = e.b; t < e.ntask; t += e.G) {
     const int k = t / e.R, sub = t - (t / e.R) * e.R;
     const long long off = (long long)k * N;
@@ -657,6 +679,11 @@ __device__ void phase_post(const EngineOps& op, const EngineIO& io, bool resid, 
     if (p_lo >= p_hi) continue;                 // uniform within the CTA
     const int pe = min(p_hi, N - 2);            // rows above the tau rows
     const T kk = kxT[k];
+    // operator input row in T (the temperature epilogue needs it)
+    for (int q = e.tid; q < N; q += blockDim.x) {
+      const double2 a = zin[off + q];
+      S.v[q] = mk2<T>((T)(a.x * zscale), (T)(a.y * zscale));
+    }
     if (op.kind == 0) {
       const int Mz = op.Mz;
       const C* Hv = (const C*)op.Hv;
@@ -665,7 +692,7 @@ __device__ void phase_post(const EngineOps& op, const EngineIO& io, bool resid, 
       for (int q = e.tid; q < Mz; q += blockDim.x) {
         const long long i0 = (long long)k * Mz + q;
         const C h0 = Hv[i0], h1 = Hv[KM + i0], h2 = Hv[2 * KM + i0], h3 = Hv[3 * KM + i0];
-        S.aux[q] = mk2<T>(h0.x + h1.x, h0.y + h1.y);
+        S.aux[q] = x_add<T>(h0, h1);
         S.aux[Mz + q] = mk2<T>((T)2 * k2 * h2.x - k2 * h0.x, (T)2 * k2 * h2.y - k2 * h0.y);
         S.aux[2 * Mz + q] = h3;
       }
@@ -682,39 +709,33 @@ __device__ void phase_post(const EngineOps& op, const EngineIO& io, bool resid, 
         tgemv_chunk<T, 3>(g, N, p0, nr, Mz, S, e);
         for (int r = e.tid; r < nr; r += blockDim.x) {
           const C a = S.out[r], b = S.out[RCH + r], c = S.out[2 * RCH + r];
-          const T re = a.x + b.x - (T)4 * kk * c.x;
-          const T im = a.y + b.y - (T)4 * kk * c.y;
-          S.w[p0 - p_lo + r] = make_double2((double)re, (double)im);
+          S.w[p0 - p_lo + r] = mk2<T>(a.x + b.x - (T)4 * kk * c.x, a.y + b.y - (T)4 * kk * c.y);
         }
       }
     } else {
       const C* A = (const C*)op.A;
-      for (int q = e.tid; q < N; q += blockDim.x) {
-        const double2 a = zin[off + q];
-        S.v[q] = a;
-        S.z[q] = mk2<T>((T)a.x, (T)a.y);
-        S.aux[q] = A[off + q];
-      }
+      for (int q = e.tid; q < N; q += blockDim.x) S.aux[q] = A[off + q];
       __syncthreads();
       GemvArgs<T, 2> g;
       g.a[0] = (const T*)op.tD2T;
       g.a[1] = (const T*)op.tViT;
-      g.x[0] = S.z;
+      g.x[0] = S.v;
       g.x[1] = S.aux;
-      const double k2 = op.kx[k] * op.kx[k];
+      const T k2 = kk * kk, a0 = (T)op.a0;
       for (int p0 = p_lo; p0 < pe; p0 += RCH) {
         const int nr = min(RCH, pe - p0);
         tgemv_chunk<T, 2>(g, N, p0, nr, N, S, e);
         for (int r = e.tid; r < nr; r += blockDim.x) {
           const C l = S.out[r], a = S.out[RCH + r];
-          const double2 vn = S.v[p0 + r];
-          const double Lr = (double)l.x - k2 * vn.x, Li = (double)l.y - k2 * vn.y;
-          S.w[p0 - p_lo + r] = make_double2((op.a0 * vn.x - Lr) - (double)a.x,
-                                            (op.a0 * vn.y - Li) - (double)a.y);
+          const C vn = S.v[p0 + r];
+          // a0 v - (D2 v - k^2 v) - Vi A
+          S.w[p0 - p_lo + r] = mk2<T>((a0 * vn.x - (l.x - k2 * vn.x)) - a.x,
+                                      (a0 * vn.y - (l.y - k2 * vn.y)) - a.y);
         }
       }
     }
-    // tau rows N-2, N-1 in FP64 from the FP64 input (one warp each)
+    // tau rows N-2, N-1: the boundary values of the input, in FP64 from the
+    // FP64 input (these sums cancel strongly; one warp each)
     for (int p = max(p_lo, N - 2) + e.warp; p < p_hi; p += ENG_WARPS) {
       const double* Vr = op.V64 + (p == N - 2 ? 0 : (long long)(N - 1) * N);
       double sr = 0.0, si = 0.0;
@@ -723,24 +744,26 @@ __device__ void phase_post(const EngineOps& op, const EngineIO& io, bool resid, 
         sr += a.x * Vr[m];
         si += a.y * Vr[m];
       }
-      sr = warp_sum(sr);
-      si = warp_sum(si);
-      if (e.lane == 0) S.w[p - p_lo] = make_double2(sr, si);
+      sr = warp_sum(sr) * zscale;
+      si = warp_sum(si) * zscale;
+      if (e.lane == 0) S.w[p - p_lo] = mk2<T>((T)sr, (T)si);
     }
     __syncthreads();
     const int np = p_hi - p_lo;
     if (!resid) {
-      for (int r = e.tid; r < np; r += blockDim.x) io.w[off + p_lo + r] = S.w[r];
-      dots_acc(io.V, n, off + p_lo, np, S.w, mm, acc, e);
+      C* W = reinterpret_cast<C*>(io.w);
+      for (int r = e.tid; r < np; r += blockDim.x) W[off + p_lo + r] = S.w[r];
+      dots_acc<T>(V, n, off + p_lo, np, S.w, mm, acc, e);
     } else {
+      C* Rv = reinterpret_cast<C*>(io.r);
       for (int r = e.tid; r < np; r += blockDim.x) {
         const double2 bb = io.b[off + p_lo + r];
-        const double2 rr = make_double2(bb.x - S.w[r].x, bb.y - S.w[r].y);
-        io.r[off + p_lo + r] = rr;
+        const C rr = mk2<T>((T)(bb.x * zscale - (double)S.w[r].x), (T)(bb.y * zscale - (double)S.w[r].y));
+        Rv[off + p_lo + r] = rr;
         S.w[r] = rr;
       }
       __syncthreads();
-      norm_acc(S.w, np, nacc, e);
+      norm_acc<T>(S.w, np, nacc, e);
     }
     __syncthreads();
   }
@@ -749,11 +772,13 @@ __device__ void phase_post(const EngineOps& op, const EngineIO& io, bool resid, 
 // update: w' = w - V coef on the owned rows (in place in io.w); then the dots
 // V_i^H w' (i < mm_dots) into acc and ||w'||^2 into *nacc
 template <class T>
-__device__ void phase_update(const EngineOps& op, const EngineIO& io, const double2* coef, int mm,
-                             int mm_dots, EngSmem<T>& S, double2* acc, double* nacc,
-                             const EngCtx& e) {
+__device__ void phase_update(const EngineOps& op, const EngineIO& io, const Cx<T>* coef, int mm,
+                             int mm_dots, EngSmem<T>& S, Cx<T>* acc, T* nacc, const EngCtx& e) {
+  using C = Cx<T>;
   const int N = op.N;
   const long long n = io.n;
+  C* W = reinterpret_cast<C*>(io.w);
+  const C* V = reinterpret_cast<const C*>(io.V);
   for (int t = e.b; t < e.ntask; t += e.G) {
     const int k = t / e.R, sub = t - (t / e.R) * e.R;
     const long long off = (long long)k * N;
@@ -761,9 +786,9 @@ __device__ void phase_update(const EngineOps& op, const EngineIO& io, const doub
     const int p_lo = sub * pc, p_hi = min(N, p_lo + pc);
     if (p_lo >= p_hi) continue;
     const int np = p_hi - p_lo;
-    combine_rows<T>(io.w, io.V, n, off + p_lo, np, coef, mm, 1.0, S.w, io.w, S, e);
-    if (mm_dots > 0) dots_acc(io.V, n, off + p_lo, np, S.w, mm_dots, acc, e);
-    norm_acc(S.w, np, nacc, e);
+    combine_rows<T>(W, V, n, off + p_lo, np, coef, mm, (T)1, S.w, W, S, e);
+    if (mm_dots > 0) dots_acc<T>(V, n, off + p_lo, np, S.w, mm_dots, acc, e);
+    norm_acc<T>(S.w, np, nacc, e);
     __syncthreads();
   }
 }
@@ -771,13 +796,14 @@ __device__ void phase_update(const EngineOps& op, const EngineIO& io, const doub
 // ------------------------------------------------------------- the engine
 template <class T>
 __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(EngineOps op, EngineIO io) {
+  using C = Cx<T>;
   cg::grid_group grid = cg::this_grid();
   extern __shared__ __align__(256) unsigned char smraw[];
-  __shared__ double sh[40];
-  __shared__ double2 s_h1[ENG_MAXM], s_h2[ENG_MAXM], s_hc[ENG_MAXM + 1], s_acc[ENG_MAXM];
-  __shared__ double s_cs[ENG_MAXM];
-  __shared__ double2 s_sn[ENG_MAXM], s_g[ENG_MAXM + 1], s_y[ENG_MAXM];
-  __shared__ double s_nacc;
+  __shared__ T sh[8];
+  __shared__ C s_h1[ENG_MAXM], s_h2[ENG_MAXM], s_hc[ENG_MAXM + 1], s_acc[ENG_MAXM];
+  __shared__ T s_cs[ENG_MAXM];
+  __shared__ C s_sn[ENG_MAXM], s_g[ENG_MAXM + 1], s_y[ENG_MAXM];
+  __shared__ T s_nacc, s_hh;
   __shared__ int s_flag;
   EngCtx e;
   e.G = gridDim.x; e.b = blockIdx.x; e.tid = threadIdx.x; e.lane = e.tid & 31; e.warp = e.tid >> 5;
@@ -790,27 +816,70 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
   const int m = io.restart;
   const long long per = (n + e.G - 1) / e.G;
   const long long lo = (long long)e.b * per, hi = min(n, lo + per);
-  double2* pp1 = io.part;
-  double2* pp2 = io.part + (size_t)(m + 1) * e.G;
+  C* pp1 = reinterpret_cast<C*>(io.part);
+  C* pp2 = pp1 + (size_t)(m + 1) * e.G;
+  T* np1 = reinterpret_cast<T*>(io.npart);       // ||.||^2 partials
+  T* np2 = np1 + e.G;                            // second set (exact norm)
+  double2* Zv = io.Z;
+  C* Rv = reinterpret_cast<C*>(io.r);
+  C* Hm = reinterpret_cast<C*>(io.H);
+  C* Yv = reinterpret_cast<C*>(io.y);
+  // heavy cancellation in ||w'||^2 - ||h2||^2 below this fraction of ||w'||^2
+  // means the Pythagorean norm has lost too many digits
+  const T cancel = std::is_same<T, float>::value ? (T)1e-2 : (T)1e-4;
   PhaseClock pc;
   pc.init(io.phase_cycles, e);
 
-  // x = 0, r = b, beta = ||b||
-  for (long long t = (long long)e.b * blockDim.x + e.tid; t < n; t += (long long)e.G * blockDim.x) {
-    io.x[t] = make_double2(0.0, 0.0);
-    io.r[t] = io.b[t];
+  // x = 0; b64 = ||b|| in FP64; the Krylov process works on r = b / b64 (unit
+  // norm, so nothing in T under- or overflows whatever the problem's scale)
+  // and x is accumulated in units of b64
+  double b64;
+  {
+    double s = 0.0;
+    for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
+      io.x[t] = make_double2(0.0, 0.0);
+      const double2 bb = io.b[t];
+      s += bb.x * bb.x + bb.y * bb.y;
+    }
+    s = warp_sum(s);
+    __shared__ double s_part[ENG_WARPS];
+    if (e.lane == 0) s_part[e.warp] = s;
+    __syncthreads();
+    double* npd = io.npart;
+    if (e.tid == 0) {
+      double a = 0.0;
+      for (int q = 0; q < ENG_WARPS; ++q) a += s_part[q];
+      npd[e.b] = a;
+    }
+    grid.sync();
+    __shared__ double s_b64;
+    if (e.warp == 0) {
+      double a = 0.0;
+#pragma unroll 10
+      for (int g = e.lane; g < e.G; g += 32) a += npd[g];
+      a = warp_sum(a);
+      if (e.lane == 0) s_b64 = sqrt(a);
+    }
+    __syncthreads();
+    b64 = s_b64;
   }
-  double beta = grid_norm(io.b, n, io.npart, e, grid, sh);
-  const double tol = io.rtol * beta;
+  const double inv64 = (b64 > 0.0 && isfinite(b64)) ? 1.0 / b64 : 0.0;
+  for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
+    const double2 bb = io.b[t];
+    Rv[t] = mk2<T>((T)(bb.x * inv64), (T)(bb.y * inv64));
+  }
+  grid.sync();                                  // prep reads whole rows of r
+  T beta = (T)1;
+  const T tol = (T)io.rtol;
   int total = 0, info = 1;
-  if (beta <= tol) info = 0;
-  if (!isfinite(beta)) info = 3;              // non-finite right-hand side
+  if (b64 == 0.0) info = 0;
+  if (!isfinite(b64)) info = 3;               // non-finite right-hand side
   while (info == 1 && total < io.maxiter) {
     // V0 = r / beta, Z0 = M V0 and its z-contraction
-    phase_prep<T>(op, io, 0, 0, 1.0 / beta, nullptr, 0, S, e);
-    for (int i = e.tid; i <= m; i += blockDim.x) s_g[i] = make_double2(0.0, 0.0);
+    phase_prep<T>(op, io, 0, 0, (T)1 / beta, nullptr, 0, S, e);
+    for (int i = e.tid; i <= m; i += blockDim.x) s_g[i] = mk2<T>((T)0, (T)0);
     __syncthreads();
-    if (e.tid == 0) s_g[0] = make_double2(beta, 0.0);
+    if (e.tid == 0) s_g[0] = mk2<T>(beta, (T)0);
     grid.sync();
     pc.mark(EP_START);
     int kc = 0;
@@ -818,89 +887,103 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
       // x-direction convolution of A z_j
       if (op.kind == 0) ph_schur_x<T>(op, smraw, e);
       else ph_theta_x<T>(op, smraw, e);
-      grid.sync();
+      __syncthreads();
       pc.mark(EP_XCONV);
+      grid.sync();
+      pc.mark(EP_XCONV_WAIT);
       // epilogue w = A z_j + first-pass dots
       const int mm = j + 1;
-      for (int i = e.tid; i < mm; i += blockDim.x) s_acc[i] = make_double2(0.0, 0.0);
+      for (int i = e.tid; i < mm; i += blockDim.x) s_acc[i] = mk2<T>((T)0, (T)0);
       __syncthreads();
-      phase_post<T>(op, io, false, io.Z + (long long)j * n, mm, S, s_acc, nullptr, e);
+      phase_post<T>(op, io, false, Zv + (long long)j * n, 1.0, mm, S, s_acc, nullptr, e);
       __syncthreads();
       for (int i = e.tid; i < mm; i += blockDim.x) pp1[(size_t)i * e.G + e.b] = s_acc[i];
-      grid.sync();
-      pc.mark(EP_POST);
-      // h1 = V^H w; w' = w - V h1; second-pass dots and ||w'||^2
-      reduce_parts(pp1, e.G, mm, s_h1, e);
-      for (int i = e.tid; i < mm; i += blockDim.x) s_acc[i] = make_double2(0.0, 0.0);
-      if (e.tid == 0) s_nacc = 0.0;
       __syncthreads();
+      pc.mark(EP_POST);
+      grid.sync();
+      pc.mark(EP_POST_WAIT);
+      // h1 = V^H w; w' = w - V h1; second-pass dots and ||w'||^2
+      reduce_parts<T>(pp1, e.G, mm, s_h1, e);
+      for (int i = e.tid; i < mm; i += blockDim.x) s_acc[i] = mk2<T>((T)0, (T)0);
+      if (e.tid == 0) s_nacc = (T)0;
+      __syncthreads();
+      pc.mark(EP_UPD_RED);
       phase_update<T>(op, io, s_h1, mm, mm, S, s_acc, &s_nacc, e);
       __syncthreads();
       for (int i = e.tid; i < mm; i += blockDim.x) pp2[(size_t)i * e.G + e.b] = s_acc[i];
-      if (e.tid == 0) io.npart[e.b] = s_nacc;
-      grid.sync();
+      if (e.tid == 0) np1[e.b] = s_nacc;
+      __syncthreads();
       pc.mark(EP_UPDATE);
+      grid.sync();
+      pc.mark(EP_UPDATE_WAIT);
       // h2 = V^H w', ||w''||^2 = ||w'||^2 - ||h2||^2
-      reduce_parts(pp2, e.G, mm, s_h2, e);
-      const double wn2 = reduce_scalar(io.npart, e.G, sh, e);    // ends with __syncthreads
-      double hh = 0.0;
-      for (int i = 0; i < mm; ++i) hh += s_h2[i].x * s_h2[i].x + s_h2[i].y * s_h2[i].y;
+      reduce_parts<T>(pp2, e.G, mm, s_h2, e);
+      const T wn2 = reduce_scalar<T>(np1, e.G, sh, e);     // ends with __syncthreads
+      if (e.warp == 0) {
+        T a = (T)0;
+        for (int i = e.lane; i < mm; i += 32) a += s_h2[i].x * s_h2[i].x + s_h2[i].y * s_h2[i].y;
+        a = warp_sum(a);
+        if (e.lane == 0) s_hh = a;
+      }
+      __syncthreads();
+      const T hh = s_hh;
+      pc.mark(EP_NEXT_RED);
       if (!isfinite(wn2) || !isfinite(hh)) {     // non-finite operator output: give up
         info = 3;
         break;
       }
-      double hn2 = wn2 - hh;
+      T hn2 = wn2 - hh;
       bool subtracted = false;
-      if (!(hn2 > 1e-4 * wn2)) {
+      if (!(hn2 > cancel * wn2)) {
         // heavy cancellation: form w'' = w' - V h2 and take its exact norm
-        if (e.tid == 0) s_nacc = 0.0;
+        if (e.tid == 0) s_nacc = (T)0;
         __syncthreads();
         phase_update<T>(op, io, s_h2, mm, 0, S, nullptr, &s_nacc, e);
         __syncthreads();
-        // second partial array: other CTAs may still be reading npart here
-        if (e.tid == 0) io.npart[e.G + e.b] = s_nacc;
+        // second partial array: other CTAs may still be reading np1 here
+        if (e.tid == 0) np2[e.b] = s_nacc;
         grid.sync();
-        hn2 = reduce_scalar(io.npart + e.G, e.G, sh, e);
+        hn2 = reduce_scalar<T>(np2, e.G, sh, e);
         subtracted = true;
         pc.mark(EP_EXACT);
       }
-      const double hn = sqrt(hn2 > 0.0 ? hn2 : 0.0);
+      const T hn = sqrt(hn2 > (T)0 ? hn2 : (T)0);
       // Givens update of column j (every CTA, identical data)
       if (e.tid == 0) {
-        for (int i = 0; i < mm; ++i) s_hc[i] = cadd(s_h1[i], s_h2[i]);
-        s_hc[j + 1] = make_double2(hn, 0.0);
+        for (int i = 0; i < mm; ++i) s_hc[i] = x_add<T>(s_h1[i], s_h2[i]);
+        s_hc[j + 1] = mk2<T>(hn, (T)0);
         for (int i = 0; i < j; ++i) {
-          const double c = s_cs[i];
-          const double2 sv = s_sn[i];
-          const double2 hi0 = s_hc[i], hi1 = s_hc[i + 1];
-          const double2 tt = cadd(cscale(hi0, c), cmul(sv, hi1));
-          s_hc[i + 1] = cadd(cmul(make_double2(-sv.x, sv.y), hi0), cscale(hi1, c));  // -conj(s) h_i + c h_{i+1}
-          s_hc[i] = tt;
+          const T c = s_cs[i];
+          const C sv = s_sn[i];
+          const C hi0 = s_hc[i], hi1 = s_hc[i + 1];
+          s_hc[i] = x_add<T>(x_scale<T>(hi0, c), x_mul<T>(sv, hi1));
+          s_hc[i + 1] = x_add<T>(x_mul<T>(mk2<T>(-sv.x, sv.y), hi0), x_scale<T>(hi1, c));  // -conj(s) h_i + c h_{i+1}
         }
-        const double2 a = s_hc[j], bb = s_hc[j + 1];
-        const double aa = hypot(a.x, a.y), bba = hypot(bb.x, bb.y);
-        double c;
-        double2 sv, rjj;
-        if (bba == 0.0) { c = 1.0; sv = make_double2(0.0, 0.0); rjj = a; }
-        else if (aa == 0.0) { c = 0.0; sv = make_double2(bb.x / bba, -bb.y / bba); rjj = make_double2(bba, 0.0); }
+        const C a = s_hc[j], bb = s_hc[j + 1];
+        const T aa = x_abs<T>(a), bba = x_abs<T>(bb);
+        T c;
+        C sv, rjj;
+        if (bba == (T)0) { c = (T)1; sv = mk2<T>((T)0, (T)0); rjj = a; }
+        else if (aa == (T)0) { c = (T)0; sv = mk2<T>(bb.x / bba, -bb.y / bba); rjj = mk2<T>(bba, (T)0); }
         else {
-          const double den = sqrt(aa * aa + bba * bba);
+          const T den = sqrt(aa * aa + bba * bba);
           c = aa / den;
-          sv = cscale(cdiv(cconj(bb), cconj(a)), c);
-          rjj = cscale(cdiv(make_double2(1.0, 0.0), cconj(a)), c * (aa * aa + bba * bba));
+          sv = x_scale<T>(x_div<T>(x_conj<T>(bb), x_conj<T>(a)), c);
+          rjj = x_scale<T>(x_div<T>(mk2<T>((T)1, (T)0), x_conj<T>(a)), c * (aa * aa + bba * bba));
         }
         s_cs[j] = c;
         s_sn[j] = sv;
         s_hc[j] = rjj;
-        const double2 gj = s_g[j], gj1 = s_g[j + 1];
-        s_g[j] = cadd(cscale(gj, c), cmul(sv, gj1));
-        s_g[j + 1] = cadd(cmul(make_double2(-sv.x, sv.y), gj), cscale(gj1, c));
-        const double rn = hypot(s_g[j + 1].x, s_g[j + 1].y);
-        s_flag = (rn <= tol) ? 1 : ((hn == 0.0) ? 2 : 0);
+        const C gj = s_g[j], gj1 = s_g[j + 1];
+        s_g[j] = x_add<T>(x_scale<T>(gj, c), x_mul<T>(sv, gj1));
+        s_g[j + 1] = x_add<T>(x_mul<T>(mk2<T>(-sv.x, sv.y), gj), x_scale<T>(gj1, c));
+        const T rn = x_abs<T>(s_g[j + 1]);
+        s_flag = (rn <= tol) ? 1 : ((hn == (T)0) ? 2 : 0);
       }
       __syncthreads();
+      pc.mark(EP_GIVENS);
       if (e.b == 0) {
-        double2* Hc = io.H + (size_t)j * (m + 1);     // rotated column j, rows 0..j
+        C* Hc = Hm + (size_t)j * (m + 1);     // rotated column j, rows 0..j
         for (int i = e.tid; i <= j; i += blockDim.x) Hc[i] = s_hc[i];
       }
       const int fl = s_flag;
@@ -908,9 +991,9 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
       kc = j + 1;
       const bool stop = fl != 0 || j + 1 == m || total >= io.maxiter;
       if (!stop)
-        phase_prep<T>(op, io, 1, j + 1, 1.0 / hn, s_h2, subtracted ? 0 : mm, S, e);
+        phase_prep<T>(op, io, 1, j + 1, (T)1 / hn, s_h2, subtracted ? 0 : mm, S, e, &pc);
       grid.sync();
-      pc.mark(EP_NEXT);
+      pc.mark(EP_NEXT_WAIT);
       if (stop) {
         if (fl == 1) info = 0;
         else if (fl == 2) info = 2;
@@ -919,42 +1002,48 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
     }
     if (kc == 0) break;
     // y = H[:k,:k]^{-1} g[:k]: column sweep by CTA 0 (the column of H is
-    // contiguous in the column-major layout), then x += Z y everywhere
+    // contiguous in the column-major layout), then x += Z y everywhere (FP64)
     if (e.b == 0) {
       for (int i = e.tid; i < kc; i += blockDim.x) s_y[i] = s_g[i];
       __syncthreads();
       for (int q = kc - 1; q >= 0; --q) {
-        const double2* Hq = io.H + (size_t)q * (m + 1);
-        if (e.tid == 0) s_y[q] = cdiv(s_y[q], Hq[q]);
+        const C* Hq = Hm + (size_t)q * (m + 1);
+        if (e.tid == 0) s_y[q] = x_div<T>(s_y[q], Hq[q]);
         __syncthreads();
-        const double2 yq = s_y[q];
-        for (int i = e.tid; i < q; i += blockDim.x) s_y[i] = csub(s_y[i], cmul(Hq[i], yq));
+        const C yq = s_y[q];
+        for (int i = e.tid; i < q; i += blockDim.x) s_y[i] = x_sub<T>(s_y[i], x_mul<T>(Hq[i], yq));
         __syncthreads();
       }
-      for (int i = e.tid; i < kc; i += blockDim.x) io.y[i] = s_y[i];
+      for (int i = e.tid; i < kc; i += blockDim.x) Yv[i] = s_y[i];
     }
     grid.sync();
     for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
-      double2 acc = make_double2(0.0, 0.0);
-      for (int q = 0; q < kc; ++q) acc = cadd(acc, cmul(io.y[q], io.Z[(long long)q * n + t]));
-      io.x[t] = cadd(io.x[t], acc);
+      double ar = 0.0, ai = 0.0;
+      for (int q = 0; q < kc; ++q) {
+        const C yq = Yv[q];
+        const double2 z = Zv[(long long)q * n + t];
+        ar += (double)yq.x * z.x - (double)yq.y * z.y;
+        ai += (double)yq.x * z.y + (double)yq.y * z.x;
+      }
+      io.x[t].x += b64 * ar;
+      io.x[t].y += b64 * ai;
     }
     grid.sync();
     pc.mark(EP_LSQ);
     if (info != 1 || total >= io.maxiter) break;
     // true residual at the restart: r = b - A x
-    phase_prep<T>(op, io, 2, 0, 1.0, nullptr, 0, S, e);
+    phase_prep<T>(op, io, 2, 0, (T)1, nullptr, 0, S, e, nullptr, inv64);
     grid.sync();
     if (op.kind == 0) ph_schur_x<T>(op, smraw, e);
     else ph_theta_x<T>(op, smraw, e);
     grid.sync();
-    if (e.tid == 0) s_nacc = 0.0;
+    if (e.tid == 0) s_nacc = (T)0;
     __syncthreads();
-    phase_post<T>(op, io, true, io.x, 0, S, nullptr, &s_nacc, e);
+    phase_post<T>(op, io, true, io.x, inv64, 0, S, nullptr, &s_nacc, e);
     __syncthreads();
-    if (e.tid == 0) io.npart[e.b] = s_nacc;
+    if (e.tid == 0) np1[e.b] = s_nacc;
     grid.sync();
-    beta = sqrt(reduce_scalar(io.npart, e.G, sh, e));
+    beta = sqrt(reduce_scalar<T>(np1, e.G, sh, e));
     pc.mark(EP_RESID);
     if (beta <= tol) { info = 0; break; }
     if (!isfinite(beta)) { info = 3; break; }
@@ -967,7 +1056,7 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
 
 template <class T>
 static size_t engine_smem(const EngineOps& op) {
-  using C = typename CT2<T>::type;
+  using C = Cx<T>;
   const size_t a = (size_t)(op.L + 4 * (op.Nk + op.L)) * sizeof(C);                 // Schur x
   const size_t b = (size_t)(2 * op.Nk + op.Np) * sizeof(C) + op.Np * sizeof(T);     // theta x
   const size_t rows = eng_rows_bytes<T>(op.N, op.kind == 0 ? op.Mz : 0);

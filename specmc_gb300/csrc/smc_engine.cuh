@@ -55,14 +55,25 @@ struct EngineIO {
   long long* phase_cycles = nullptr;
 };
 
-// phases of one Arnoldi step (and of a restart cycle) between grid barriers
+// phases of one Arnoldi step (and of a restart cycle) between grid barriers;
+// the *_WAIT slots hold CTA 0's wait at the grid barrier that ends the phase,
+// the others its own work
 enum EnginePhase {
   EP_START = 0,  // V0 = r / beta, its preconditioned vector and z-contraction
   EP_XCONV,      // x-direction convolution (per z-point / grid column)
+  EP_XCONV_WAIT,
   EP_POST,       // operator epilogue + first-pass orthogonalisation dots
+  EP_POST_WAIT,
+  EP_UPD_RED,    // reduction of the first-pass dots
   EP_UPDATE,     // first-pass update + second-pass dots + ||w'||^2
+  EP_UPDATE_WAIT,
   EP_EXACT,      // exact norm after heavy cancellation (rare)
-  EP_NEXT,       // Givens update + next basis vector, its preconditioned vector, z-contraction
+  EP_NEXT_RED,   // reduction of the second-pass dots and of ||w'||^2
+  EP_GIVENS,     // Givens update of the new Hessenberg column
+  EP_COMBINE,    // next basis row v = (w' - V h2) / h
+  EP_PRECOND,    // its preconditioned row
+  EP_CONTRACT,   // z-contraction slice
+  EP_NEXT_WAIT,
   EP_LSQ,        // triangular solve + x update at the end of a cycle
   EP_RESID,      // true residual at a restart
   ENGINE_PHASES

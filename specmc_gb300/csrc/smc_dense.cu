@@ -463,8 +463,11 @@ void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work) {
   for (int p0 = 0; p0 < n; p0 += ZNB) {
     int nbp = std::min(ZNB, n - p0);
     void* args[] = {&A, &n, &p0, &nbp, &piv, &part, &done, &pv};
-    SMC_CUDA(cudaLaunchCooperativeKernel((void*)smc_zlu_panel_kernel, dim3(G), dim3(256), args, 0, c.s));
-    SMC_LAUNCH_CHECK(c);
+    {
+      CoopGuard guard(c.s);
+      SMC_CUDA(cudaLaunchCooperativeKernel((void*)smc_zlu_panel_kernel, dim3(G), dim3(256), args, 0, c.s));
+      SMC_LAUNCH_CHECK(c);
+    }
     smc_zlu_laswp_kernel<<<ceil_div(n, LASWP_WARPS), 32 * LASWP_WARPS, 0, c.s>>>(A, n, pv + ZNB);
     SMC_LAUNCH_CHECK(c);
     int rest = n - p0 - nbp;
@@ -621,6 +624,7 @@ void zlu_dense_solve(const Ctx& c, const double2* LU, const double2* invL, const
   double2* y = work;
   void* args[] = {(void*)&LU, (void*)&invL, (void*)&invU, (void*)&perm, (void*)&b,
                   (void*)&x, (void*)&y, (void*)&n};
+  CoopGuard guard(c.s);
   SMC_CUDA(cudaLaunchCooperativeKernel((void*)smc_zlu_solve_kernel, dim3(G), dim3(256), args, 0, c.s));
   SMC_LAUNCH_CHECK(c);
 }

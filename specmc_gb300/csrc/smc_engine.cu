@@ -1075,11 +1075,13 @@ static void engine_launch(const Ctx& c, const EngineOps& op, const EngineIO& io)
   int per_sm = 0;
   SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ENG_THREADS, sm));
   if (per_sm < 1) throw std::runtime_error("fgmres engine: kernel cannot be co-resident");
-  const int G = c.num_sms * (per_sm >= 2 ? 2 : 1);
+  int G = c.num_sms * (per_sm >= 2 ? 2 : 1);
+  if (io.grid_cap > 0 && io.grid_cap < G) G = io.grid_cap;
   if (G > io.max_grid) throw std::runtime_error("fgmres engine: partial buffers too small");
   EngineOps o = op;
   EngineIO i = io;
   void* args[] = {(void*)&o, (void*)&i};
+  CoopGuard guard(c.s);
   SMC_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(G), dim3(ENG_THREADS), args, sm, c.s));
   SMC_LAUNCH_CHECK(c);
 }

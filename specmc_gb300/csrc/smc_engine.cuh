@@ -50,6 +50,7 @@ struct EngineIO {
   int* flag = nullptr;
   int* result = nullptr;     // {info, iterations}
   int max_grid = 0;
+  int grid_cap = 0;          // > 0: at most this many CTAs (handles sharing the GPU)
   // optional: SM cycles CTA 0 spent between consecutive grid barriers, summed
   // per phase (ENGINE_PHASES slots, names in engine_phase_names); null = off
   long long* phase_cycles = nullptr;

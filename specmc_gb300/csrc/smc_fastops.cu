@@ -491,6 +491,7 @@ void cgs2(const Ctx& c, const double2* V, int j, long long n, double2* w, double
   if (j + 1 > 96) throw std::runtime_error("cgs2: restart above 95");
   int G = c.num_sms;
   void* args[] = {(void*)&V, (void*)&j, (void*)&n, (void*)&w, (void*)&hout, (void*)&part};
+  CoopGuard guard(c.s);
   SMC_CUDA(cudaLaunchCooperativeKernel((void*)smc_cgs2_kernel, dim3(G), dim3(256), args, 0, c.s));
   SMC_LAUNCH_CHECK(c);
 }

@@ -7,6 +7,7 @@
 //                                       (column-major, used by LU factors)
 //   dense Schur LU    (n, n) complex    column-major, n = Nk * Nz
 #pragma once
+#include <mutex>
 
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -95,6 +96,20 @@ struct ProfScope {
   } while (0)
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Cooperative grids (grid-wide barriers) of different handles never overlap:
+// a cooperative kernel needs all of its CTAs resident at once, and two of
+// them each holding SMs while waiting for the rest of their own CTAs would
+// never finish.  The guard holds a process-wide lock from the launch until
+// the kernel has completed on its stream; ordinary kernels of other streams
+// keep running beside it.
+std::mutex& coop_mutex();
+struct CoopGuard {
+  cudaStream_t s;
+  std::unique_lock<std::mutex> lk;
+  explicit CoopGuard(cudaStream_t s_) : s(s_), lk(coop_mutex()) {}
+  ~CoopGuard() { cudaStreamSynchronize(s); }
+};
 
 // ------------------------------------------------------- complex helpers
 __host__ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {

@@ -111,21 +111,26 @@ struct HostBasis {
 };
 
 // ------------------------------------------------------------ device memory
+// Every buffer is zeroed and every upload made on the handle's own stream:
+// that stream is non-blocking, so work on the legacy default stream would not
+// be ordered before the handle's kernels.
 struct DevMem {
   std::vector<void*> ptrs;
+  cudaStream_t s = nullptr;
   template <class T>
   T* alloc(size_t count) {
     void* p = nullptr;
     if (count == 0) count = 1;
     SMC_CUDA(cudaMalloc(&p, count * sizeof(T)));
-    SMC_CUDA(cudaMemset(p, 0, count * sizeof(T)));
+    SMC_CUDA(cudaMemsetAsync(p, 0, count * sizeof(T), s));
     ptrs.push_back(p);
     return static_cast<T*>(p);
   }
   template <class T>
   T* upload(const std::vector<T>& h) {
     T* p = alloc<T>(h.size());
-    SMC_CUDA(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    SMC_CUDA(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    SMC_CUDA(cudaStreamSynchronize(s));     // h may go out of scope
     return p;
   }
   ~DevMem() {
@@ -149,6 +154,11 @@ struct FgmresResult {
 };
 
 using Op = std::function<void(const double2*, double2*)>;
+
+std::mutex& coop_mutex() {
+  static std::mutex mu;
+  return mu;
+}
 
 // ---------------------------------------------------------------- profiler
 int Profiler::tag_of(const char* name) {
@@ -321,6 +331,7 @@ struct Model {
   float* dKx32 = nullptr;
   int* dEngInt = nullptr;
   bool eng_phase = false;            // per-phase cycle counts of engine solves into the profiler
+  int eng_ctas = 0;                  // > 0: cap on the engine's CTAs (handles sharing the GPU)
   long long* dEngPhase = nullptr;    // ENGINE_PHASES accumulators
   double sm_khz = 0.0;               // peak SM clock (cycles -> ms)
 
@@ -404,6 +415,7 @@ struct Model {
     SMC_CUDA(cudaSetDevice(cfg.device));
     device = cfg.device;
     SMC_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    mem.s = stream;
     int sms = 0;
     SMC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     ctx.s = stream; ctx.nlaunch = &nlaunch; ctx.num_sms = sms; ctx.prof = &prof;
@@ -540,7 +552,8 @@ struct Model {
       dEtaPadZ = mem.alloc<double>((size_t)Np * N);
       {
         std::vector<double> ez(N);
-        SMC_CUDA(cudaMemcpy(ez.data(), dEz, N * sizeof(double), cudaMemcpyDeviceToHost));
+        SMC_CUDA(cudaMemcpyAsync(ez.data(), dEz, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        SMC_CUDA(cudaStreamSynchronize(stream));
         std::vector<double> tiled((size_t)Nx * N);
         for (int i = 0; i < Nx; ++i)
           for (int j = 0; j < N; ++j) tiled[(size_t)i * N + j] = ez[j];
@@ -553,10 +566,12 @@ struct Model {
         double2* dEzIn = mem.alloc<double2>(N);
         {
           std::vector<double> ez(N);
-          SMC_CUDA(cudaMemcpy(ez.data(), dEz, N * sizeof(double), cudaMemcpyDeviceToHost));
+          SMC_CUDA(cudaMemcpyAsync(ez.data(), dEz, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+          SMC_CUDA(cudaStreamSynchronize(stream));
           std::vector<double2> ec(N);
           for (int j = 0; j < N; ++j) ec[j] = make_double2(ez[j], 0.0);
-          SMC_CUDA(cudaMemcpy(dEzIn, ec.data(), N * sizeof(double2), cudaMemcpyHostToDevice));
+          SMC_CUDA(cudaMemcpyAsync(dEzIn, ec.data(), N * sizeof(double2), cudaMemcpyHostToDevice, stream));
+          SMC_CUDA(cudaStreamSynchronize(stream));
         }
         ZJob j; j.Z = dVi; j.X = dEzIn; j.Y = dEzc;
         zmat_apply(ctx, &j, 1, 1, N, dkx);
@@ -568,16 +583,14 @@ struct Model {
         dLastEta = mem.alloc<double>((size_t)Nx * N);
         dEtaP = mem.alloc<double>((size_t)Np * N);
         dEtaC = mem.alloc<double2>(n);
-        dMd = mem.alloc<double2>((size_t)(2 * Nk - 1) * NN);
-        dAsmWork = mem.alloc<double2>((size_t)4 * (2 * Nk - 1) * NN);
-        dSchur = mem.alloc<double2>((size_t)n * n);
-        dSchurPiv = mem.alloc<int>(n);
-        dSchurPerm = mem.alloc<int>(n);
+        // the dense Schur route (legacy solve, rescue) is allocated on first
+        // use: its factor is (Nk N)^2 complex entries
         {
-          long long nblk = (n + 63) / 64;
-          dSchurInvL = mem.alloc<double2>((size_t)nblk * 64 * 64);
-          dSchurInvU = mem.alloc<double2>((size_t)nblk * 64 * 64);
+          size_t free_b = 0, total_b = 0;
+          SMC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+          dense_cap_bytes = 0.5 * (double)free_b;
         }
+        if (!fast && cfg.precond != SMC_PRECOND_BFBT) ensure_dense();
         dSb = mem.alloc<double2>(n); dSx = mem.alloc<double2>(n); dSr = mem.alloc<double2>(n);
         dSdx = mem.alloc<double2>(n); dSAx = mem.alloc<double2>(n); dSw = mem.alloc<double2>(n);
         dSf2 = mem.alloc<double2>(n); dSf3 = mem.alloc<double2>(n); dSf4 = mem.alloc<double2>(n);
@@ -782,10 +795,36 @@ struct Model {
     }
   }
 
+  // Algorithmic bytes of an engine solve of `its` Arnoldi steps: per step the
+  // operator's matrices are read once (z-contraction, epilogue, x-direction
+  // weights), the block preconditioner once, the x-direction scratch written
+  // and read, and the Krylov vectors touched four times per basis vector held
+  // (first-pass dots, update, second-pass dots, next-vector combination) plus
+  // the new V and Z rows written.
+  double engine_bytes(int kind, bool fp32, int its, int restart) const {
+    const double t = fp32 ? 4.0 : 8.0, cx = 2.0 * t, n8 = (double)n;
+    double mats, scratch;
+    if (kind == 0) {
+      const double Mz = psplan.Mz, L = psplan.L;
+      mats = t * Mz * N * (1.0 + 3.0 * Nk) + t * 3.0 * Mz * N + t * L * Mz;
+      scratch = cx * 4.0 * Nk * Mz * 3.0;
+    } else {
+      mats = t * 4.0 * N * N + t * 2.0 * Np * N;
+      scratch = cx * (2.0 * Nk * N * 2.0 + Nk * N * 2.0);
+    }
+    const double prec = (fp32 ? 8.0 : 8.0) * Nk * (double)NN;
+    double vec = 0.0;
+    for (int j = 0; j < its; ++j) {
+      const int held = (restart > 0 ? j % restart : j) + 1;
+      vec += cx * n8 * (4.0 * held + 2.0) + 16.0 * n8;
+    }
+    return its * (mats + scratch + prec) + vec;
+  }
+
   // one FGMRES solve in the persistent engine; kind 0 = Schur, 1 = theta
   FgmresResult engine_solve(int kind, bool fp32, const double2* b, double2* x, double rtol,
                             int restart, int maxiter, const void* GpT, double palpha) {
-    ProfScope ps(ctx, kind == 0 ? "engine_stokes" : "engine_theta");
+    ProfScope ps(ctx, kind == 0 ? "engine_stokes" : "engine_theta", 0.0, 1);
     const EngMats& em = fp32 ? em32 : em64;
     EngineOps op;
     op.kind = kind; op.Nk = Nk; op.N = N; op.kx = dkx; op.V64 = dV;
@@ -809,6 +848,7 @@ struct Model {
     io.b = b; io.x = x; io.rtol = rtol; io.n = n;
     io.restart = std::max(1, std::min(restart, mmax));
     io.maxiter = maxiter;
+    io.grid_cap = eng_ctas;
     const bool phases = eng_phase && prof.enabled;
     if (phases) {
       SMC_CUDA(cudaMemsetAsync(dEngPhase, 0, ENGINE_PHASES * sizeof(long long), stream));
@@ -827,6 +867,7 @@ struct Model {
     FgmresResult fr;
     fr.info = res[0];
     fr.iters = res[1];
+    ps.work = engine_bytes(kind, fp32, fr.iters, io.restart);
     return fr;
   }
 
@@ -927,9 +968,45 @@ struct Model {
   // grid from the current dEta: eta_c = coeffs(eta)
   void eta_operator() {
     analyze(dEta, Nx, dEtaC, sp[2]);
-    build_mult_mats(ctx, dEtaC, dMd, Nk, N);
+    md_stale = true;
+    if (dMd && (!fast || use_dense_mult)) md_current();
     ps_eta_grid(ctx, psplan, dEtaC, dPsFv, dPsE);
     if (fast) to_float(ctx, dPsE, dE32, (long long)psplan.L * psplan.Mz);
+  }
+
+  // ------------------------------------------------ dense Schur route storage
+  bool md_stale = true;
+  double dense_cap_bytes = 0.0;
+  // bytes of the dense route: Md, assembly/LU workspace, factor, inverses
+  double dense_bytes() const {
+    const double blk = (double)(2 * Nk - 1) * NN * 16.0;
+    const long long nblk = (n + 63) / 64;
+    return 5.0 * blk + (double)n * n * 16.0 + 2.0 * nblk * 64 * 64 * 16.0 + 8.0 * n;
+  }
+  bool dense_feasible() const { return dSchur || dense_bytes() <= dense_cap_bytes; }
+  void ensure_dense() {
+    if (dSchur) return;
+    if (!dense_feasible())
+      throw std::runtime_error("dense Schur route: the factor of (Nk Nz)^2 = " +
+                               std::to_string((double)n * n) +
+                               " complex entries does not fit in device memory; use the "
+                               "BFBT route (precond = SMC_PRECOND_BFBT)");
+    if (!dMd) dMd = mem.alloc<double2>((size_t)(2 * Nk - 1) * NN);
+    dAsmWork = mem.alloc<double2>((size_t)4 * (2 * Nk - 1) * NN);
+    dSchur = mem.alloc<double2>((size_t)n * n);
+    dSchurPiv = mem.alloc<int>(n);
+    dSchurPerm = mem.alloc<int>(n);
+    const long long nblk = (n + 63) / 64;
+    dSchurInvL = mem.alloc<double2>((size_t)nblk * 64 * 64);
+    dSchurInvU = mem.alloc<double2>((size_t)nblk * 64 * 64);
+  }
+  // Md of the current eta (the dense mult_eta blocks)
+  void md_current() {
+    if (!dMd) dMd = mem.alloc<double2>((size_t)(2 * Nk - 1) * NN);
+    if (md_stale) {
+      build_mult_mats(ctx, dEtaC, dMd, Nk, N);
+      md_stale = false;
+    }
   }
 
   // FreeSchurOperator.matvec at the current Md (lagged_stokes.py:202-220)
@@ -944,6 +1021,7 @@ struct Model {
     KFactor f4; f4.kpow = 1;                                // k (D w)
     zop(dD, 0, dSw, dSf4, f4);
     if (use_dense_mult) {
+      md_current();
       smc::mult_eta(ctx, dMd, v, dSt[0], Nk, N, -1.0, nullptr);
       smc::mult_eta(ctx, dMd, dSf2, dSt[1], Nk, N, -1.0, nullptr);
       smc::mult_eta(ctx, dMd, dSf3, dSt[2], Nk, N, -1.0, nullptr);
@@ -965,6 +1043,8 @@ struct Model {
   }
 
   void refresh() {
+    ensure_dense();
+    md_current();
     {
       ProfScope ps(ctx, "schur_assembly");
       assemble_schur(ctx, dMd, dD, dD2, dG, dV, dkx, dSchur, Nk, N, dAsmWork);
@@ -1134,7 +1214,29 @@ struct Model {
     ctr.n_bfbt_iters += fr.iters;
     ctr.last_bfbt_true_res = res;
     ctr.last_K = 0;
-    if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
+    if (fr.info != 0 && !(res <= cfg.stokes_rtol) && !dense_feasible()) {
+      // rescue without the dense route (its factor does not fit): rebuild the
+      // BFBT blocks for the current eta and solve in FP64 with four times the
+      // iteration budget; counted as a weak rescue
+      ctr.n_bfbt_rescue++;
+      bfbt_age = 1 << 30;
+      bfbt_prof_h.clear();
+      bfbt_build();
+      Op A64 = [&](const double2* v, double2* o) {
+        if (fast) schur_matvec_fast(v, o, false);
+        else schur_matvec(v, o);
+      };
+      Op M64 = [&](const double2* r, double2* z) {
+        if (fast) kgemv(ctx, dRedG, r, z, Nk, N, 1.0);
+        else lu_small_solve(ctx, dRedLU, dRedPiv, NN, r, z, N, Nk, 1.0, 1, nullptr);
+      };
+      FgmresResult f2 = fgmres(A64, M64, dSb, x, cfg.stokes_rtol, cfg.stokes_restart,
+                               4 * cfg.stokes_maxiter);
+      ctr.n_bfbt_iters += f2.iters;
+      ctr.n_bfbt_rescue_weak++;
+      res = schur_true_res(dSb, x);
+      ctr.last_bfbt_true_res = res;
+    } else if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
       // rescue chain (coupled_model.py:613-654)
       ctr.n_bfbt_rescue++;
       refresh();
@@ -1861,6 +1963,9 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
     } else if (k == "inner_rtol_floor") {
       if (!(value > 0.0 && value < 1.0)) throw std::runtime_error("inner_rtol_floor must be in (0, 1)");
       h->m.inner_floor = value;
+    } else if (k == "engine_ctas") {
+      if (!(value >= 0.0 && value <= 1e6)) throw std::runtime_error("engine_ctas must be >= 0");
+      h->m.eng_ctas = (int)value;
     } else if (k == "engine_phase_profile") {
       h->m.eng_phase = value != 0.0;
     } else throw std::runtime_error("unknown option " + k);

@@ -1,0 +1,136 @@
+"""Ensembles of independent runs on one GPU (the batched workload).
+
+Each run is its own model handle with its own CUDA stream; a pool of host
+threads drives them (the native calls release the GIL), so the kernels of
+different runs overlap on the GPU.  The persistent Krylov engine of a handle
+normally spreads over every SM; in an ensemble each handle's engine is capped
+at its share of the SMs so that the concurrent runs fit side by side.
+
+The runs are independent -- nothing is exchanged between them while they
+step -- so an ensemble shards across GPUs by partitioning the run list
+(replicas of this driver, one per GPU).
+
+``ensemble_configs`` draws the seeded mixed workload of 256 runs: grid from
+{32x24, 64x48, 64x96, 128x96}, Ra log-uniform in [1e4, 1e6], deta_T
+log-uniform in [1, 1e4], viscosity model uniform over const / eta_z / eta_T,
+perturbation amplitude uniform in [1e-2, 5e-2] with modes m, n in 1..4.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+from . import _lib, api
+from . import _numerics as NUM
+from .config import ConvectionConfig
+
+__all__ = ["GRIDS", "MODELS", "ensemble_configs", "march_ensemble", "device_sms"]
+
+GRIDS = ((32, 24), (64, 48), (64, 96), (128, 96))
+MODELS = ("const", "eta_z", "eta_T")
+
+
+def ensemble_configs(nruns=256, seed=0):
+    """The seeded list of runs: dicts with ``cfg`` (ConvectionConfig) and the
+    perturbation ``amp``, ``m``, ``n`` (drawn in this order per run)."""
+    rng = np.random.default_rng(seed)
+    runs = []
+    for _ in range(int(nruns)):
+        Nx, Nz = GRIDS[int(rng.integers(len(GRIDS)))]
+        Ra = float(10.0 ** rng.uniform(4.0, 6.0))
+        deta = float(10.0 ** rng.uniform(0.0, 4.0))
+        vm = MODELS[int(rng.integers(len(MODELS)))]
+        amp = float(rng.uniform(1e-2, 5e-2))
+        m = int(rng.integers(1, 5))
+        n = int(rng.integers(1, 5))
+        cfg = ConvectionConfig(viscosity_model=vm, Nx=Nx, Nz=Nz, Ra=Ra, deta_T=deta)
+        runs.append(dict(cfg=cfg, amp=amp, m=m, n=n))
+    return runs
+
+
+def device_sms(device=0):
+    """Streaming multiprocessors of ``device``."""
+    import torch
+    return int(torch.cuda.get_device_properties(device).multi_processor_count)
+
+
+def _march_one(run, nsteps, form, device, cap, safety, dtmax, chunk, max_wall):
+    """One run: CFL-limited steps in chunks of ``chunk``; after each chunk the
+    state is checked.  The run is flagged when max|theta| on the grid exceeds
+    AMP_LIMIT x its initial value (the reference driver's abort threshold,
+    specmc/_numerics.py:139-140; the ensemble keeps marching such a run and
+    reports it), and it stops, flagged, when the state is non-finite, the
+    march stalls, or it has used ``max_wall`` seconds."""
+    t0 = time.perf_counter()
+    model = api.build_model(run["cfg"], form=form, device=device)
+    try:
+        lib, h = model._lib, model._h
+        if cap > 0:
+            _lib.check(lib.smc_set_option(h, b"engine_ctas", float(cap)))
+        th = np.ascontiguousarray(model.seed(amp=run["amp"], m=run["m"], n=run["n"]))
+        amp0 = float(np.abs(model.grid(th)).max())
+        _lib.check(lib.smc_set_state(h, th.ctypes.data_as(ctypes.c_void_p), _lib.SMC_HOST))
+        t1 = time.perf_counter()
+        info = _lib.SmcMarchInfo()
+        s = np.empty_like(th)
+        steps, status = 0, "ok"
+        while steps < nsteps:
+            k = min(int(chunk), int(nsteps) - steps)
+            _lib.check(lib.smc_advance(h, 1e300, k, float(safety), float(dtmax), ctypes.byref(info)))
+            steps += int(info.steps)
+            _lib.check(lib.smc_get_state(h, s.ctypes.data_as(ctypes.c_void_p), _lib.SMC_HOST))
+            if not np.all(np.isfinite(s)) or not np.isfinite(info.t):
+                status = "non-finite"
+                break
+            if status == "ok" and float(np.abs(model.grid(s)).max()) > NUM.AMP_LIMIT * max(amp0, 1e-300):
+                status = "amplitude"
+            if info.steps < k:
+                status = "stalled"
+                break
+            if max_wall and time.perf_counter() - t1 > max_wall:
+                status = "time"
+                break
+        t2 = time.perf_counter()
+        finite = bool(np.all(np.isfinite(s)))
+        diag = model.diagnostics(s) if finite else {}
+        return dict(steps=steps, t=float(info.t), dt=float(info.dt), build_s=t1 - t0,
+                    march_s=t2 - t1, state=s, diag=diag, finite=finite,
+                    flagged=status != "ok", status=status, counters=model.counters())
+    finally:
+        model.close()
+
+
+def march_ensemble(runs, nsteps=100, form="mixed", concurrency=8, safety=None, dtmax=None,
+                   device=0, engine_ctas=None, chunk=5, max_wall=None, on_done=None):
+    """March every run of ``runs`` for ``nsteps`` CFL-limited steps, up to
+    ``concurrency`` at a time.  Returns one result dict per run (steps, t,
+    build and march seconds, final state, diagnostics, status and flag,
+    counters); flagged runs stop early and are kept in the list.
+
+    ``engine_ctas`` caps each handle's Krylov engine; the default gives each
+    concurrent run an equal share of two CTAs per SM.  ``on_done(i, result)``
+    is called as each run finishes."""
+    safety = NUM.CFL_SAFETY if safety is None else float(safety)
+    dtmax = NUM.DTMAX if dtmax is None else float(dtmax)
+    concurrency = max(1, int(concurrency))
+    if engine_ctas is None:
+        engine_ctas = max(1, (2 * device_sms(device)) // concurrency) if concurrency > 1 else 0
+    out = [None] * len(runs)
+
+    def work(i):
+        out[i] = _march_one(runs[i], nsteps, form, device, int(engine_ctas), safety, dtmax,
+                            chunk, max_wall)
+        if on_done is not None:
+            on_done(i, out[i])
+
+    if concurrency == 1:
+        for i in range(len(runs)):
+            work(i)
+    else:
+        with ThreadPoolExecutor(max_workers=concurrency) as ex:
+            for f in [ex.submit(work, i) for i in range(len(runs))]:
+                f.result()
+    return out

@@ -117,6 +117,9 @@ class GpuModel:
             t = that.to(torch.complex128).contiguous()
             if tuple(t.shape) != (self.Nk, self.Nz):
                 raise ValueError("state must be (Nk, Nz) = (%d, %d)" % (self.Nk, self.Nz))
+            # the library reads it on the handle's own stream: finish the
+            # producer's work on the current torch stream first
+            torch.cuda.current_stream(t.device).synchronize()
             return ctypes.c_void_p(t.data_ptr()), _lib.SMC_DEVICE, t
         a = np.ascontiguousarray(np.asarray(that), dtype=np.complex128)
         if a.shape != (self.Nk, self.Nz):

@@ -87,11 +87,85 @@ __global__ void smc_lu_small_kernel(double* __restrict__ A, int* __restrict__ pi
   if (tid == 0 && info) info[blockIdx.x] = inf;
 }
 
+// The same factorisation for matrices too large for shared memory (Nz of a
+// few hundred): one CTA per matrix working in place in global memory (the
+// matrix stays in L2 while its CTA factors it); the pivot column and the
+// pivot row of each step are staged in shared memory for the rank-1 update.
+__global__ void __launch_bounds__(512) smc_lu_medium_kernel(double* __restrict__ A, int* __restrict__ piv,
+                                                            int* __restrict__ info, int N) {
+  extern __shared__ double stage[];               // column c (N) + row c (N)
+  double* colc = stage;
+  double* rowc = stage + N;
+  __shared__ double rv[32];
+  __shared__ int ri[32];
+  __shared__ int s_p;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  double* a = A + (long long)blockIdx.x * N * N;
+  int inf = 0;
+  for (int c = 0; c < N; ++c) {
+    double best = -1.0;
+    int bi = N;
+    for (int r = c + tid; r < N; r += nt) {
+      double v = fabs(a[r + (long long)c * N]);
+      if (v > best) { best = v; bi = r; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double ov = __shfl_xor_sync(0xffffffffu, best, o);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    if ((tid & 31) == 0) { rv[tid >> 5] = best; ri[tid >> 5] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      double b = rv[0];
+      int p = ri[0];
+      for (int w = 1; w < (nt >> 5); ++w)
+        if (rv[w] > b || (rv[w] == b && ri[w] < p)) { b = rv[w]; p = ri[w]; }
+      if (p >= N) p = c;
+      s_p = p;
+      piv[(long long)blockIdx.x * N + c] = p;
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p != c)
+      for (int col = tid; col < N; col += nt) {
+        double t = a[c + (long long)col * N];
+        a[c + (long long)col * N] = a[p + (long long)col * N];
+        a[p + (long long)col * N] = t;
+      }
+    __syncthreads();
+    const double pv = a[c + (long long)c * N];
+    if (pv != 0.0) {
+      const double rinv = 1.0 / pv;
+      for (int r = c + 1 + tid; r < N; r += nt) {
+        const double l = a[r + (long long)c * N] * rinv;
+        a[r + (long long)c * N] = l;
+        colc[r] = l;
+      }
+    } else {
+      if (!inf) inf = c + 1;
+      for (int r = c + 1 + tid; r < N; r += nt) colc[r] = a[r + (long long)c * N];
+    }
+    for (int col = c + 1 + tid; col < N; col += nt) rowc[col] = a[c + (long long)col * N];
+    __syncthreads();
+    const int m = N - c - 1;
+    for (int t = tid; t < m * m; t += nt) {
+      const int r = c + 1 + t % m, col = c + 1 + t / m;
+      a[r + (long long)col * N] -= colc[r] * rowc[col];
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && info) info[blockIdx.x] = inf;
+}
+
 void lu_small_batched(const Ctx& c, double* A, int* piv, int* info, int N, int count) {
   size_t smem = (size_t)N * N * sizeof(double);
-  if (smem > 200 * 1024) throw std::runtime_error("lu_small_batched: Nz too large for the shared-memory LU");
-  SMC_CUDA(cudaFuncSetAttribute(smc_lu_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
+  if (smem > 200 * 1024) {
+    smc_lu_medium_kernel<<<count, 512, 2 * N * sizeof(double), c.s>>>(A, piv, info, N);
+    SMC_LAUNCH_CHECK(c);
+    return;
+  }
+  allow_max_smem((const void*)smc_lu_small_kernel);
   smc_lu_small_kernel<<<count, 256, smem, c.s>>>(A, piv, info, N);
   SMC_LAUNCH_CHECK(c);
 }
@@ -451,8 +525,7 @@ __global__ void __launch_bounds__(256) smc_zlu_gemm_kernel(double2* __restrict__
 
 void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work) {
   const size_t gsm = (size_t)2 * ZNB * GT * sizeof(double2);
-  SMC_CUDA(cudaFuncSetAttribute(smc_zlu_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)gsm));
+  allow_max_smem((const void*)smc_zlu_gemm_kernel);
   int G = c.num_sms;
   int maxb = 0;
   SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, smc_zlu_panel_kernel, 256, 0));
@@ -609,8 +682,7 @@ __global__ void __launch_bounds__(256) smc_zlu_solve_kernel(const double2* __res
 void zlu_diag_inverses(const Ctx& c, const double2* LU, int n, double2* invL, double2* invU) {
   const int nblk = (n + SB - 1) / SB;
   const size_t sm = (size_t)2 * SB * SB * sizeof(double2);
-  SMC_CUDA(cudaFuncSetAttribute(smc_zlu_diag_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sm));
+  allow_max_smem((const void*)smc_zlu_diag_inv_kernel);
   smc_zlu_diag_inv_kernel<<<dim3(nblk, 2), 64, sm, c.s>>>(LU, n, invL, invU);
   SMC_LAUNCH_CHECK(c);
 }

@@ -1070,11 +1070,20 @@ template <class T>
 static void engine_launch(const Ctx& c, const EngineOps& op, const EngineIO& io) {
   const size_t sm = engine_smem<T>(op);
   auto kern = smc_fgmres_engine_kernel<T>;
-  if (sm > 48 * 1024)
-    SMC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  allow_max_smem((const void*)kern);
   int per_sm = 0;
   SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ENG_THREADS, sm));
-  if (per_sm < 1) throw std::runtime_error("fgmres engine: kernel cannot be co-resident");
+  if (per_sm < 1) {
+    cudaFuncAttributes fa;
+    cudaFuncGetAttributes(&fa, (const void*)kern);
+    throw std::runtime_error("fgmres engine: kernel cannot be co-resident (kind " +
+                             std::to_string(op.kind) + ", N " + std::to_string(op.N) + ", Mz " +
+                             std::to_string(op.Mz) + ", L " + std::to_string(op.L) + ", Np " +
+                             std::to_string(op.Np) + ", dynamic smem " + std::to_string(sm) +
+                             ", static smem " + std::to_string(fa.sharedSizeBytes) + ", max dynamic " +
+                             std::to_string(fa.maxDynamicSharedSizeBytes) + ", regs " +
+                             std::to_string(fa.numRegs) + ")");
+  }
   int G = c.num_sms * (per_sm >= 2 ? 2 : 1);
   if (io.grid_cap > 0 && io.grid_cap < G) G = io.grid_cap;
   if (G > io.max_grid) throw std::runtime_error("fgmres engine: partial buffers too small");

@@ -221,6 +221,7 @@ void fused_schur_matvec_t(const Ctx& c, const FusedSchur<T>& op, const T* E, con
   SMC_LAUNCH_CHECK(c);
   dim3 g2(op.Mz, 4);
   size_t sm = (size_t)(op.Nk + 2 * op.L) * sizeof(CT);
+  allow_max_smem((const void*)smc_fs_x_kernel<T>);
   smc_fs_x_kernel<T><<<g2, 128, sm, c.s>>>((const CT*)Fv, E, op.Nk, op.Mz, op.L, (const CT*)op.tw,
                                           (CT*)Hv);
   SMC_LAUNCH_CHECK(c);
@@ -386,6 +387,7 @@ void fused_theta_matvec_t(const Ctx& c, const FusedTheta<T>& op, const T* ux, co
   smc_ft_zsynth_kernel<T><<<ceil_div(no, 8), 256, 0, c.s>>>(v, op.V, op.VD, op.kx, op.Nk, op.N, (CT*)X);
   SMC_LAUNCH_CHECK(c);
   size_t sm = (size_t)(2 * op.Nk + op.Np) * sizeof(CT) + op.Np * sizeof(T);
+  allow_max_smem((const void*)smc_ft_x_kernel<T>);
   smc_ft_x_kernel<T><<<op.N, 128, sm, c.s>>>((const CT*)X, ux, uz, (const CT*)op.tw, op.Nk, op.N,
                                             op.Np, (CT*)A);
   SMC_LAUNCH_CHECK(c);

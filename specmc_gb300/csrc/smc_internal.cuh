@@ -104,6 +104,12 @@ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 // the kernel has completed on its stream; ordinary kernels of other streams
 // keep running beside it.
 std::mutex& coop_mutex();
+
+// Let kernel `f` use up to the device's opt-in maximum of dynamic shared
+// memory.  The attribute is global to the process, so every caller sets the
+// same value (a smaller per-launch value set by one handle could otherwise
+// undercut another handle's launch in between).
+void allow_max_smem(const void* f);
 struct CoopGuard {
   cudaStream_t s;
   std::unique_lock<std::mutex> lk;

@@ -127,6 +127,7 @@ void ps_mult_eta(const Ctx& c, const PsPlan& pl, const double* E, const PsJobs& 
   SMC_LAUNCH_CHECK(c);
   dim3 g2(pl.Mz, nb);
   size_t sm = (size_t)(pl.Nk + pl.L) * sizeof(double2);
+  allow_max_smem((const void*)smc_ps_x_kernel);
   smc_ps_x_kernel<<<g2, 128, sm, c.s>>>(Fv, E, jobs, pl.Nk, pl.Mz, pl.L, pl.tw, Hv);
   SMC_LAUNCH_CHECK(c);
   dim3 g3(ceil_div(pl.N, 128), pl.Nk, nb);

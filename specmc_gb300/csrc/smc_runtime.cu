@@ -18,6 +18,7 @@
 #include <string>
 #include <type_traits>
 #include <vector>
+#include <set>
 
 #include "../../include/specmc_gb300.h"
 #include "smc_internal.cuh"
@@ -158,6 +159,22 @@ using Op = std::function<void(const double2*, double2*)>;
 std::mutex& coop_mutex() {
   static std::mutex mu;
   return mu;
+}
+
+void allow_max_smem(const void* f) {
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  int dev = 0;
+  SMC_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.count({f, dev})) return;
+  int mx = 0;
+  SMC_CUDA(cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  SMC_CUDA(cudaFuncGetAttributes(&fa, f));
+  SMC_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                mx - (int)fa.sharedSizeBytes));
+  done.insert({f, dev});
 }
 
 // ---------------------------------------------------------------- profiler
@@ -326,6 +343,7 @@ struct Model {
   double theta_lag = 0.1;    // fast form: relative a0 change before the theta preconditioner is rebuilt
   long long n_theta_lag_hits = 0;
   long long n_fp64_fallback = 0;     // fast form: inner FP32 solves redone in FP64
+  int stokes_fp64_solves = 0;        // fast form: Stokes solves left in FP64 after a fallback
   bool use_engine = true;   // fast form: Krylov solves in the persistent on-device engine
   EngineIO eio;
   float* dKx32 = nullptr;
@@ -421,8 +439,6 @@ struct Model {
     ctx.s = stream; ctx.nlaunch = &nlaunch; ctx.num_sms = sms; ctx.prof = &prof;
     SMC_CUDA(cudaMallocHost(&hbuf, 4096 * sizeof(double)));
     if (N < 4 || Nx < 4) throw std::runtime_error("Nx and Nz must be >= 4");
-    if ((size_t)N * N * sizeof(double) > 200 * 1024)
-      throw std::runtime_error("Nz > 160 needs the global-memory small LU (not built)");
 
     hb.reset(new HostBasis(N));
     kx_h.resize(Nk);
@@ -1175,8 +1191,21 @@ struct Model {
     return norm(dSAx) / bn;
   }
 
+  // fast form: after a dense rescue the BFBT blocks have just failed for this
+  // eta field and the lagged dense factor is fresh, so the next solves use
+  // the lagged-LU defect route (the reference's legacy route,
+  // coupled_model.py:524-586) until its lag expires, then BFBT is tried again
+  int legacy_after_rescue = 0;
+  long long n_legacy_after_rescue = 0;
+
   void bfbt_solve(const double2* th, double2* x) {
     rhs_schur(th, dSb);
+    if (fast && legacy_after_rescue > 0 && dSchur) {
+      --legacy_after_rescue;
+      ++n_legacy_after_rescue;
+      legacy_solve(th, x);
+      return;
+    }
     bfbt_build();
     Op A = [&](const double2* v, double2* o) { schur_matvec(v, o); };
     Op M = [&](const double2* r, double2* z) {
@@ -1189,13 +1218,31 @@ struct Model {
     if (fast) {
       Op A64 = [&](const double2* v, double2* o) { schur_matvec_fast(v, o, false); };
       Op A32 = [&](const double2* v, double2* o) { schur_matvec_fast(v, o, true); };
-      if (inner_fp32) {
+      const bool fp32_now = inner_fp32 && stokes_fp64_solves == 0;
+      if (!fp32_now && stokes_fp64_solves > 0) --stokes_fp64_solves;
+      if (fp32_now) {
         InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
           if (use_engine)
             return engine_solve(0, true, r, e, tol, cfg.stokes_restart, mi, dRedGT32, 1.0);
           return fgmres(A32, M, r, e, tol, cfg.stokes_restart, mi);
         };
         fr = fgmres_refined(A64, inner, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, &res);
+        if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
+          // the FP32 operator cannot resolve this system (viscosity contrast
+          // too large for its rounding): solve it in FP64 and stay in FP64
+          // for the next solves
+          ctr.n_bfbt_iters += fr.iters;
+          ++n_fp64_fallback;
+          stokes_fp64_solves = 16;
+          if (use_engine)
+            fr = engine_solve(0, false, dSb, x, cfg.stokes_rtol, cfg.stokes_restart,
+                              cfg.stokes_maxiter, dRedGT64, 1.0);
+          else
+            fr = fgmres(A64, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
+          schur_matvec_fast(x, dSAx, false);
+          vec_axpby(ctx, dSAx, make_double2(1.0, 0.0), dSb, make_double2(-1.0, 0.0), n);
+          res = norm(dSAx) / std::max(norm(dSb), 1e-300);
+        }
       } else {
         if (use_engine)
           fr = engine_solve(0, false, dSb, x, cfg.stokes_rtol, cfg.stokes_restart,
@@ -1239,6 +1286,7 @@ struct Model {
     } else if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
       // rescue chain (coupled_model.py:613-654)
       ctr.n_bfbt_rescue++;
+      if (fast) legacy_after_rescue = cfg.lag;
       refresh();
       defect_solve(th, x);
       if (last_failed) {

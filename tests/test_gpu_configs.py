@@ -1,0 +1,134 @@
+"""Parity of the larger workloads on the GPU: the batched ensemble of
+independent runs and the internally heated 2:1 box, mixed form against the
+FP64 plain form (the oracle for these sizes is the plain GPU path, whose
+parity with the reference is pinned by the golden-vector tests)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def ens():
+    from specmc_gb300 import ensemble
+    runs = ensemble.ensemble_configs(256, seed=0)
+    # one run of each viscosity model on three of the grids
+    pick, seen = [], set()
+    for i, r in enumerate(runs):
+        key = (r["cfg"].viscosity_model, r["cfg"].Nx)
+        if key not in seen and r["cfg"].Nx <= 64:
+            seen.add(key)
+            pick.append(i)
+    return ensemble, [runs[i] for i in pick[:6]]
+
+
+def test_ensemble_concurrent_equals_sequential(ens):
+    """Handles marched concurrently (own streams, host threads) give the same
+    bits as the same handles marched one after another."""
+    ensemble, runs = ens
+    a = ensemble.march_ensemble(runs, nsteps=10, concurrency=1, engine_ctas=64)
+    b = ensemble.march_ensemble(runs, nsteps=10, concurrency=3, engine_ctas=64)
+    for x, y in zip(a, b):
+        assert x["steps"] == y["steps"]
+        assert np.array_equal(x["state"], y["state"])
+
+
+def test_ensemble_mixed_matches_plain(ens):
+    """Each run of the ensemble: the mixed form agrees with the FP64 plain
+    form to 1e-6 relative in Nu_top and Vrms after 10 steps."""
+    ensemble, runs = ens
+    m = ensemble.march_ensemble(runs, nsteps=10, form="mixed", concurrency=3)
+    p = ensemble.march_ensemble(runs, nsteps=10, form="plain", concurrency=3)
+    for run, x, y in zip(runs, m, p):
+        assert x["finite"] and y["finite"], run["cfg"]
+        assert x["steps"] == y["steps"] == 10
+        for key in ("Nu_top", "urms"):
+            assert _rel(x["diag"][key], y["diag"][key]) <= 1e-6, (run["cfg"], key)
+
+
+def _heated_ic(model, H=1.5, seed=7, amp=1e-2, modes=8):
+    """Conductive profile with internal heating H (physics/heating.py:168-171)
+    plus seeded Fourier-Chebyshev noise in modes m, n <= 8 scaled to max 1e-2,
+    mirror-symmetric and zero at the walls."""
+    rng = np.random.default_rng(seed)
+    X, Z = np.meshgrid(model.x, model.z, indexing="ij")
+    noise = np.zeros_like(X)
+    for m in range(1, modes + 1):
+        for n in range(1, modes + 1):
+            noise += rng.uniform(-1.0, 1.0) * np.cos(m * np.pi * X * 2.0 / model.Lx) * np.sin(n * np.pi * Z)
+    noise *= amp / np.abs(noise).max()
+    g = 0.5 * H * Z * (1.0 - Z) + noise
+    return np.ascontiguousarray(model.coeffs(g))
+
+
+def test_heated_2to1_64x96_mixed_matches_plain():
+    """Internally heated 2:1 box (Ra 1.25e4, H 1.5, eta_T deta 1e3, 64x96,
+    Lx = 4 for the physical 2:1 box on the mirror-doubled carrier): 15 CFL
+    steps, mixed vs plain, Nu_top / Nu_energy / Vrms within 1e-6."""
+    import specmc_gb300.api as api
+    from specmc_gb300.config import ConvectionConfig
+    cfg = ConvectionConfig(viscosity_model="eta_T", deta_T=1000.0, Ra=1.25e4, internal_heating=1.5,
+                           Nx=64, Nz=96, Lx=4.0)
+    out = {}
+    for form in ("mixed", "plain"):
+        m = api.build_model(cfg, form=form)
+        s = _heated_ic(m)
+        for _ in range(15):
+            s = m.step(s, api.production_dt(m, s))
+        out[form] = m.diagnostics(s)
+        m.close()
+    for key in ("Nu_top", "Nu_energy", "urms"):
+        assert _rel(out["mixed"][key], out["plain"][key]) <= 1e-6, key
+
+
+def test_large_nz_lu_matches_oracle():
+    """Nz = 168 puts the per-k tau-operator LUs past the shared-memory kernel
+    (N^2 doubles > 200 KB) onto the global-memory batched LU; the const-route
+    march must still equal the CPU oracle to round-off."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from oracle import specmc_oracle as O
+    import specmc_gb300.api as api
+    from specmc_gb300.config import ConvectionConfig
+    cfg = ConvectionConfig(viscosity_model="const", Ra=1e4, Nx=16, Nz=168)
+    m = api.build_model(cfg)
+    o = O.build(cfg)
+    s_gpu = m.seed(amp=3e-2, m=1, n=1)
+    s_cpu = o.seed(amp=3e-2, m=1, n=1)
+    for _ in range(3):
+        s_gpu = m.step(s_gpu, 2e-5)
+        s_cpu = o.step(s_cpu, 2e-5)
+    err = np.abs(np.asarray(s_gpu) - s_cpu).max() / np.abs(s_cpu).max()
+    assert err < 1e-10, err
+    m.close()
+
+
+def test_large_arrhenius_1024x513_mixed_matches_plain():
+    """The large run (1024 x 513, Ra 1e7, Arrhenius law calibrated to
+    deta_T = 1e5 with the eta window [1e-5, 1], Di 0.5, H 1, BFBT route): no
+    CPU oracle is feasible at this size, so the mixed form is checked against
+    the FP64 plain form over two CFL steps.  The viscosity contrast is beyond
+    what the FP32 inner operator resolves: the mixed form must notice and
+    finish its Stokes solves in FP64."""
+    import specmc_gb300.api as api
+    from specmc_gb300.config import ConvectionConfig
+    cfg = ConvectionConfig(viscosity_model="arrhenius", Nx=1024, Nz=513, Ra=1e7, deta_T=1e5,
+                           eta_min=1e-5, eta_max=1.0, dissipation_number=0.5, internal_heating=1.0,
+                           arrhenius_Ts=1.0, precond="bfbt")
+    out = {}
+    for form in ("mixed", "plain"):
+        m = api.build_model(cfg, form=form)
+        s = _heated_ic(m, H=1.0, seed=5, amp=1e-3, modes=32)
+        for _ in range(2):
+            s = m.step(s, api.production_dt(m, s))
+        assert np.all(np.isfinite(s))
+        out[form] = (np.asarray(s), m.diagnostics(s))
+        m.close()
+    err = np.abs(out["mixed"][0] - out["plain"][0]).max() / np.abs(out["plain"][0]).max()
+    assert err < 1e-6, err
+    for key in ("Nu_top", "urms"):
+        assert _rel(out["mixed"][1][key], out["plain"][1][key]) <= 1e-6, key

@@ -189,7 +189,7 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
  * "inner_rtol_floor" (0 < f < 1, default 1e-4): smallest relative tolerance
  * asked of an FP32 inner solve of the mixed form (its operator's rounding
  * limits what a tighter inner solve could gain).
- * "theta_precond_lag" (0 <= f < 1, default 0.1): the mixed form reuses the
+ * "theta_precond_lag" (0 <= f < 1, default 0.3): the mixed form reuses the
  * temperature preconditioner while a0 stays within this relative distance
  * of the a0 it was built for (0: rebuild for every new a0, as the reference).
  * "engine_ctas" (>= 0, default 0 = one or two CTAs per SM): cap on the CTAs of

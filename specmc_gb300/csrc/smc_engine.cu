@@ -40,6 +40,7 @@
 
 #include "smc_internal.cuh"
 #include "smc_engine.cuh"
+#include "smc_fft.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -341,70 +342,50 @@ __device__ void norm_acc(const Cx<T>* y, int nr, T* acc, const EngCtx& e) {
 }
 
 // ----------------------------------------------------- x-direction phases
-// Schur x-convolution: CTA per z-point s; the four fields are handled by
-// four groups of blockDim/4 threads with their own shared-memory slices
+// Schur x-convolution: CTA per z-point s; the four fields are handled by four
+// groups of blockDim/4 threads, each with its own length-L shared-memory row.
+// G = sum_j F_j e^{+i th} + sgn sum_{j>=1} F_j e^{-i th} (modes at +j and,
+// times sgn, at L - j; one FFT), P = E G, H_i = (1/L) sum_l P e^{-i th_i}
+// (one FFT, first Nk modes).  sgn = -1 for the first three fields, +1 for the
+// fourth (the flipped cross term).
 template <class T>
 __device__ void ph_schur_x(const EngineOps& op, unsigned char* smraw, const EngCtx& e) {
   using C = typename CT2<T>::type;
   const int Nk = op.Nk, Mz = op.Mz, L = op.L;
+  const int logL = ilog2_pow2(L);
   const int gsz = blockDim.x / 4, grp = e.tid / gsz, gt = e.tid % gsz;
-  C* W = reinterpret_cast<C*>(smraw);           // L twiddles
-  C* F = W + L + grp * (Nk + L);                 // this group's field
-  C* P = F + Nk;
+  C* W = reinterpret_cast<C*>(smraw);           // L/2 twiddles
+  C* P = W + (L >> 1) + grp * L;                 // this group's row
   const C* tw = (const C*)op.twS;
   const T* E = (const T*)op.E;
   const C* Fv = (const C*)op.Fv;
   C* Hv = (C*)op.Hv;
-  for (int t = e.tid; t < L; t += blockDim.x) W[t] = tw[t];
+  for (int t = e.tid; t < (L >> 1); t += blockDim.x) W[t] = tw[t];
   const T sgn = (grp == 3) ? (T)1 : (T)-1;
-  const T ap = (T)1 + sgn, am = (T)1 - sgn;
   const T invL = (T)1 / (T)L;
   for (int s = e.b; s < Mz; s += e.G) {
     __syncthreads();
-    for (int j = gt; j < Nk; j += gsz) F[j] = Fv[((long long)grp * Nk + j) * Mz + s];
+    for (int i = gt; i < L; i += gsz) { P[i].x = (T)0; P[i].y = (T)0; }
     __syncthreads();
-    for (int l = gt; l < L; l += gsz) {
-      T gr = F[0].x, gi = F[0].y;
-      int idx = 0;
-      for (int j = 1; j < Nk; ++j) {
-        idx += l;
-        if (idx >= L) idx -= L;
-        const C t = W[idx];
-        const C f = F[j];
-        gr += ap * (f.x * t.x) - am * (f.y * t.y);
-        gi += ap * (f.y * t.x) + am * (f.x * t.y);
-      }
-      const T ev = E[(long long)l * Mz + s];
-      P[l].x = ev * gr;
-      P[l].y = ev * gi;
+    for (int j = gt; j < Nk; j += gsz) {
+      const C f = Fv[((long long)grp * Nk + j) * Mz + s];
+      P[j] = f;
+      if (j > 0) { P[L - j].x = sgn * f.x; P[L - j].y = sgn * f.y; }
     }
     __syncthreads();
-    // 4 consecutive threads per output mode i (groups are warp-aligned)
-    for (int base = 0; base < Nk; base += gsz / 4) {
-      const int i = base + gt / 4, part = gt & 3;
-      T hr = 0, hi = 0;
-      if (i < Nk) {
-        int idx = (int)(((long long)i * part) % L);
-        const int step = (int)(((long long)i * 4) % L);
-        for (int l = part; l < L; l += 4) {
-          const C t = W[idx];
-          const C p = P[l];
-          hr += p.x * t.x + p.y * t.y;
-          hi += p.y * t.x - p.x * t.y;
-          idx += step;
-          if (idx >= L) idx -= L;
-        }
-      }
-      hr += __shfl_xor_sync(0xffffffffu, hr, 1);
-      hi += __shfl_xor_sync(0xffffffffu, hi, 1);
-      hr += __shfl_xor_sync(0xffffffffu, hr, 2);
-      hi += __shfl_xor_sync(0xffffffffu, hi, 2);
-      if (i < Nk && part == 0) {
-        C o;
-        o.x = hr * invL;
-        o.y = hi * invL;
-        Hv[((long long)grp * Nk + i) * Mz + s] = o;
-      }
+    cta_fft(P, L, logL, W, +1, gt, gsz);
+    for (int l = gt; l < L; l += gsz) {
+      const T ev = E[(long long)l * Mz + s];
+      P[l].x *= ev;
+      P[l].y *= ev;
+    }
+    __syncthreads();
+    cta_fft(P, L, logL, W, -1, gt, gsz);
+    for (int i = gt; i < Nk; i += gsz) {
+      C o;
+      o.x = P[i].x * invL;
+      o.y = P[i].y * invL;
+      Hv[((long long)grp * Nk + i) * Mz + s] = o;
     }
   }
 }
@@ -1057,7 +1038,7 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
 template <class T>
 static size_t engine_smem(const EngineOps& op) {
   using C = Cx<T>;
-  const size_t a = (size_t)(op.L + 4 * (op.Nk + op.L)) * sizeof(C);                 // Schur x
+  const size_t a = (size_t)(op.L / 2 + 4 * op.L) * sizeof(C);                       // Schur x
   const size_t b = (size_t)(2 * op.Nk + op.Np) * sizeof(C) + op.Np * sizeof(T);     // theta x
   const size_t rows = eng_rows_bytes<T>(op.N, op.kind == 0 ? op.Mz : 0);
   size_t s = rows;

@@ -20,6 +20,7 @@
 
 #include "smc_internal.cuh"
 #include "smc_fastops.cuh"
+#include "smc_fft.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -71,65 +72,43 @@ __global__ void smc_fs_fwd_kernel(const typename C2<T>::type* __restrict__ v, co
 }
 
 // per (s, b): G(l) = sum_j F_j e^{+i th} + sgn_b sum_{j>=1} F_j e^{-i th},
-// P = E G, H_i = (1/L) sum_l P(l) e^{-i th_i}; sgn = -1 except b = 3 (+1)
+// P = E G, H_i = (1/L) sum_l P(l) e^{-i th_i}; sgn = -1 except b = 3 (+1).
+// Both transforms are radix-2 FFTs of length L (a power of two) in shared
+// memory: the modes are placed at +j and (times sgn) at L - j.
 template <class T>
 __global__ void smc_fs_x_kernel(const typename C2<T>::type* __restrict__ Fv, const T* __restrict__ E,
                                 int Nk, int Mz, int L, const typename C2<T>::type* __restrict__ tw,
                                 typename C2<T>::type* __restrict__ Hv) {
   using CT = typename C2<T>::type;
   extern __shared__ unsigned char smraw[];
-  CT* F = reinterpret_cast<CT*>(smraw);   // Nk
-  CT* P = F + Nk;                          // L
-  CT* W = P + L;                           // L twiddles
+  CT* P = reinterpret_cast<CT*>(smraw);    // L
+  CT* W = P + L;                           // L/2 twiddles
   const int s = blockIdx.x, b = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const T sgn = (b == 3) ? (T)1 : (T)-1;
-  const T ap = (T)1 + sgn, am = (T)1 - sgn;
-  for (int j = tid; j < Nk; j += nt) F[j] = Fv[((long long)b * Nk + j) * Mz + s];
-  for (int l = tid; l < L; l += nt) W[l] = tw[l];
+  const int logL = ilog2_pow2(L);
+  for (int i = tid; i < (L >> 1); i += nt) W[i] = tw[i];
+  for (int i = tid; i < L; i += nt) { P[i].x = (T)0; P[i].y = (T)0; }
   __syncthreads();
-  for (int l = tid; l < L; l += nt) {
-    T gr = F[0].x, gi = F[0].y;
-    int idx = 0;
-    for (int j = 1; j < Nk; ++j) {
-      idx += l;
-      if (idx >= L) idx -= L;
-      const CT t = W[idx];
-      const CT f = F[j];
-      gr += ap * (f.x * t.x) - am * (f.y * t.y);
-      gi += ap * (f.y * t.x) + am * (f.x * t.y);
-    }
-    const T e = E[(long long)l * Mz + s];
-    P[l].x = e * gr;
-    P[l].y = e * gi;
+  for (int j = tid; j < Nk; j += nt) {
+    const CT f = Fv[((long long)b * Nk + j) * Mz + s];
+    P[j] = f;
+    if (j > 0) { P[L - j].x = sgn * f.x; P[L - j].y = sgn * f.y; }
   }
   __syncthreads();
+  cta_fft(P, L, logL, W, +1, tid, nt);
+  for (int l = tid; l < L; l += nt) {
+    const T e = E[(long long)l * Mz + s];
+    P[l].x *= e;
+    P[l].y *= e;
+  }
+  __syncthreads();
+  cta_fft(P, L, logL, W, -1, tid, nt);
   const T invL = (T)1 / (T)L;
-  // 4 consecutive lanes per output mode i, each summing every 4th point
-  for (int base = 0; base < Nk; base += nt / 4) {
-    const int i = base + tid / 4, part = tid & 3;
-    T hr = 0, hi = 0;
-    if (i < Nk) {
-      int idx = (int)(((long long)i * part) % L);
-      const int step = (int)(((long long)i * 4) % L);
-      for (int l = part; l < L; l += 4) {
-        const CT t = W[idx];
-        const CT p = P[l];
-        hr += p.x * t.x + p.y * t.y;
-        hi += p.y * t.x - p.x * t.y;
-        idx += step;
-        if (idx >= L) idx -= L;
-      }
-    }
-    hr += __shfl_xor_sync(0xffffffffu, hr, 1);
-    hi += __shfl_xor_sync(0xffffffffu, hi, 1);
-    hr += __shfl_xor_sync(0xffffffffu, hr, 2);
-    hi += __shfl_xor_sync(0xffffffffu, hi, 2);
-    if (i < Nk && part == 0) {
-      CT o;
-      o.x = hr * invL;
-      o.y = hi * invL;
-      Hv[((long long)b * Nk + i) * Mz + s] = o;
-    }
+  for (int i = tid; i < Nk; i += nt) {
+    CT o;
+    o.x = P[i].x * invL;
+    o.y = P[i].y * invL;
+    Hv[((long long)b * Nk + i) * Mz + s] = o;
   }
 }
 
@@ -220,7 +199,7 @@ void fused_schur_matvec_t(const Ctx& c, const FusedSchur<T>& op, const T* E, con
                                                         op.N, op.Mz, (CT*)Fv);
   SMC_LAUNCH_CHECK(c);
   dim3 g2(op.Mz, 4);
-  size_t sm = (size_t)(op.Nk + 2 * op.L) * sizeof(CT);
+  size_t sm = (size_t)(op.L + op.L / 2) * sizeof(CT);
   allow_max_smem((const void*)smc_fs_x_kernel<T>);
   smc_fs_x_kernel<T><<<g2, 128, sm, c.s>>>((const CT*)Fv, E, op.Nk, op.Mz, op.L, (const CT*)op.tw,
                                           (CT*)Hv);

@@ -16,6 +16,7 @@
 // MACs instead of ~1.5 Nk^2 N^2.
 #include "smc_internal.cuh"
 #include "smc_pseudo.cuh"
+#include "smc_fft.cuh"
 
 namespace smc {
 
@@ -43,38 +44,33 @@ __global__ void smc_ps_x_kernel(const double2* __restrict__ Fv, const double* __
                                 PsJobs jobs, int Nk, int Mz, int L, const double2* __restrict__ tw,
                                 double2* __restrict__ Hv) {
   extern __shared__ double2 sm[];
-  double2* F = sm;          // Nk
-  double2* P = sm + Nk;     // L
+  double2* P = sm;          // L
+  double2* W = sm + L;      // L/2 twiddles
   const int s = blockIdx.x, b = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const double sgn = jobs.sgn[b];
-  for (int j = tid; j < Nk; j += nt) F[j] = Fv[((long long)b * Nk + j) * Mz + s];
+  const int logL = ilog2_pow2(L);
+  for (int i = tid; i < (L >> 1); i += nt) W[i] = tw[i];
+  for (int i = tid; i < L; i += nt) P[i] = make_double2(0.0, 0.0);
   __syncthreads();
+  // G(l) = sum_j F_j e^{+i th} + sgn sum_{j>=1} F_j e^{-i th}: the modes at
+  // +j and (the partner sign times) at L - j, then one inverse-direction FFT
+  for (int j = tid; j < Nk; j += nt) {
+    const double2 f = Fv[((long long)b * Nk + j) * Mz + s];
+    P[j] = f;
+    if (j > 0) P[L - j] = make_double2(sgn * f.x, sgn * f.y);
+  }
+  __syncthreads();
+  cta_fft(P, L, logL, W, +1, tid, nt);
   for (int l = tid; l < L; l += nt) {
-    double gr = F[0].x, gi = F[0].y;
-    for (int j = 1; j < Nk; ++j) {
-      double2 t = tw[(long long)(j * l) % L];          // e^{+i theta}
-      double2 f = F[j];
-      // f e^{i th} + sgn f e^{-i th}
-      double cr = f.x * t.x, ci = f.y * t.x;            // f cos
-      double sr = -f.y * t.y, si = f.x * t.y;           // i f sin
-      gr += (1.0 + sgn) * cr + (1.0 - sgn) * sr;
-      gi += (1.0 + sgn) * ci + (1.0 - sgn) * si;
-    }
-    double e = E[(long long)l * Mz + s];
-    P[l] = make_double2(e * gr, e * gi);
+    const double e = E[(long long)l * Mz + s];
+    P[l] = make_double2(e * P[l].x, e * P[l].y);
   }
   __syncthreads();
+  // H_i = (1/L) sum_l P(l) e^{-i th}, i < Nk
+  cta_fft(P, L, logL, W, -1, tid, nt);
   const double invL = 1.0 / L;
-  for (int i = tid; i < Nk; i += nt) {
-    double hr = 0.0, hi = 0.0;
-    for (int l = 0; l < L; ++l) {
-      double2 t = tw[(long long)(i * l) % L];
-      double2 p = P[l];
-      hr += p.x * t.x + p.y * t.y;                      // p e^{-i th}
-      hi += p.y * t.x - p.x * t.y;
-    }
-    Hv[((long long)b * Nk + i) * Mz + s] = make_double2(hr * invL, hi * invL);
-  }
+  for (int i = tid; i < Nk; i += nt)
+    Hv[((long long)b * Nk + i) * Mz + s] = make_double2(P[i].x * invL, P[i].y * invL);
 }
 
 // out_b[i][p] = sum_s Zi[p][s] Hv[b][i][s]
@@ -126,7 +122,7 @@ void ps_mult_eta(const Ctx& c, const PsPlan& pl, const double* E, const PsJobs& 
   smc_ps_zfwd_kernel<<<g1, 128, 0, c.s>>>(jobs, pl.Zf, pl.Nk, pl.N, pl.Mz, Fv);
   SMC_LAUNCH_CHECK(c);
   dim3 g2(pl.Mz, nb);
-  size_t sm = (size_t)(pl.Nk + pl.L) * sizeof(double2);
+  size_t sm = (size_t)(pl.L + pl.L / 2) * sizeof(double2);
   allow_max_smem((const void*)smc_ps_x_kernel);
   smc_ps_x_kernel<<<g2, 128, sm, c.s>>>(Fv, E, jobs, pl.Nk, pl.Mz, pl.L, pl.tw, Hv);
   SMC_LAUNCH_CHECK(c);

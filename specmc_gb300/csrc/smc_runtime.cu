@@ -340,7 +340,7 @@ struct Model {
   int matvec_variant = 0;   // smc_schur_matvec: 0 plain, 1 fused FP64, 2 fused FP32
   bool inner_fp32 = true;   // fast form: FP32 inner Krylov operators + FP64 refinement
   double inner_floor = 1e-4; // smallest relative tolerance asked of an FP32 inner solve
-  double theta_lag = 0.1;    // fast form: relative a0 change before the theta preconditioner is rebuilt
+  double theta_lag = 0.3;    // fast form: relative a0 change before the theta preconditioner is rebuilt
   long long n_theta_lag_hits = 0;
   long long n_fp64_fallback = 0;     // fast form: inner FP32 solves redone in FP64
   int stokes_fp64_solves = 0;        // fast form: Stokes solves left in FP64 after a fallback
@@ -614,7 +614,11 @@ struct Model {
         dSolveWork = mem.alloc<double2>(n);
         dBfbtHw = mem.alloc<double>(2 * N);
         // pseudo-spectral plan: L >= 3 Nk - 2 x-points, Mz = 2N - 1 CGL points
-        psplan.Nk = Nk; psplan.N = N; psplan.Mz = 2 * N - 1; psplan.L = 3 * Nk - 2;
+        // L: the first power of two >= 3 Nk - 2 (alias-free products of two
+        // Nk-mode fields; a power of two for the radix-2 FFTs)
+        psplan.Nk = Nk; psplan.N = N; psplan.Mz = 2 * N - 1;
+        psplan.L = 1;
+        while (psplan.L < 3 * Nk - 2) psplan.L <<= 1;
         {
           const int Mz = psplan.Mz, L = psplan.L;
           std::vector<double> Zf((size_t)Mz * N), Zi((size_t)N * Mz);

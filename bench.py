@@ -36,10 +36,11 @@ METRIC = "steps/sec, mixed-precision vs FP64 GPU path at <=1e-6 rel Nu/Vrms erro
 WORKLOAD = dict(viscosity_model="eta_T", deta_T=1000.0, Ra=1e4, Nx=64, Nz=96)
 SEED = dict(amp=3e-2, m=1, n=1)
 L2_BYTES = 129 * 1024 * 1024
-# DRAM bytes (read + write) per launch of the dominant kernels, from one ncu
-# capture of this workload (dram__bytes_read.sum + dram__bytes_write.sum); the
-# capture and its command are summarised in profiles/engine_64x96.md
-DRAM_BYTES_PER_LAUNCH = {}
+# DRAM bytes (read + write) per launch of the dominant kernels, from ncu
+# captures of this workload (dram__bytes_read.sum + dram__bytes_write.sum,
+# mean over the captured launches); the captures and their commands are
+# summarised in profiles/engine_64x96.md
+DRAM_BYTES_PER_LAUNCH = {"engine_stokes": 10.29e6, "engine_theta": 2.87e6}
 
 
 def _peaks():
@@ -196,6 +197,8 @@ def run_ours(args, rank, world):
             torch.distributed.barrier()
         c0 = m.counters()["n_kernel_launches"]
         if profile:
+            if args.phases and form == "mixed":
+                _lib.check(lib.smc_set_option(m._h, b"engine_phase_profile", 1.0))
             _lib.check(lib.smc_profile(m._h, 1))
         evs = []
         torch.cuda.synchronize()
@@ -331,6 +334,8 @@ def main():
     ap.add_argument("--ref-warmup", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--phases", action="store_true",
+                    help="add the Krylov engine's per-phase times to kernel_regions")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -134,3 +134,40 @@ def march_ensemble(runs, nsteps=100, form="mixed", concurrency=8, safety=None, d
             for f in [ex.submit(work, i) for i in range(len(runs))]:
                 f.result()
     return out
+
+
+def _main(argv=None):
+    """python -m specmc_gb300.ensemble [--runs 256] [--steps 100] ...: march the
+    seeded ensemble and print one JSON summary line."""
+    import argparse
+    import collections
+    import json
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--runs", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--form", default="mixed", choices=("mixed", "plain"))
+    ap.add_argument("--concurrency", type=int, default=8)
+    ap.add_argument("--engine-ctas", type=int, default=None)
+    ap.add_argument("--max-wall", type=float, default=None,
+                    help="seconds after which a run stops, flagged 'time'")
+    a = ap.parse_args(argv)
+    runs = ensemble_configs(a.runs, a.seed)
+    t0 = time.perf_counter()
+    res = march_ensemble(runs, nsteps=a.steps, form=a.form, concurrency=a.concurrency,
+                         engine_ctas=a.engine_ctas, max_wall=a.max_wall)
+    wall = time.perf_counter() - t0
+    steps = sum(r["steps"] for r in res)
+    by = collections.defaultdict(list)
+    for run, r in zip(runs, res):
+        by["%dx%d %s" % (run["cfg"].Nx, run["cfg"].Nz, run["cfg"].viscosity_model)].append(
+            1e3 * r["march_s"] / max(r["steps"], 1))
+    print(json.dumps(dict(
+        runs=len(runs), steps=steps, wall_s=wall, steps_per_s=steps / wall, form=a.form,
+        concurrency=a.concurrency, build_s=sum(r["build_s"] for r in res),
+        status=dict(collections.Counter(r["status"] for r in res)),
+        median_ms_per_step={k: float(np.median(v)) for k, v in sorted(by.items())})))
+
+
+if __name__ == "__main__":
+    _main()

@@ -203,6 +203,17 @@ int smc_set_option(smc_handle* h, const char* key, double value);
 /* RBCImplicitTheta.reset_history (implicit_theta.py:601-606). */
 int smc_reset_history(smc_handle* h);
 
+/* The BDF2 history of the temperature step (implicit_theta.py:596-599,
+ * 616-619): the previous (projected) state, the previous stream function,
+ * the previous dt and whether it exists.  The reference does not save it;
+ * with it a checkpointed march resumes with the same BDF2 step instead of a
+ * backward-Euler restart.  (Nk, Nz) complex buffers; the const model keeps
+ * no history (have_prev = 0). */
+int smc_get_history(smc_handle* h, double* prev_out, double* psi_prev_out, int mem,
+                    double* dt_prev, int* have_prev);
+int smc_set_history(smc_handle* h, const double* prev, const double* psi_prev, int mem,
+                    double dt_prev, int have_prev);
+
 int smc_counters_get(smc_handle* h, smc_counters* out);
 
 /* Sizes of the handle's arrays: Nk, Nx, Nz, Np (= 2 Nx). */

@@ -87,11 +87,10 @@ def production_dt(model, that):
 
 
 def load_checkpoint(path):
-    """(theta coefficients, meta) from a driver checkpoint .npz (specmc/io/checkpoint.py:80-103)."""
-    with np.load(path, allow_pickle=False) as z:
-        that = np.array(z["that"])
-        meta = {k: z[k].item() for k in ("t", "n", "fac") if k in z.files}
-    return that, meta
+    """(theta coefficients, meta) from a driver checkpoint .npz; delegates to
+    :func:`specmc_gb300.checkpoint.load` (specmc/api.py -> io/checkpoint.py:80-103)."""
+    from . import checkpoint
+    return checkpoint.load(path)
 
 
 def march(model, that, dt, nsteps, keep_states=False, on_step=None):

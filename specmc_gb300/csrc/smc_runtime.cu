@@ -2028,6 +2028,35 @@ int smc_reset_history(smc_handle* h) {
   SMC_GUARD(h, { h->m.have_prev = false; })
 }
 
+int smc_get_history(smc_handle* h, double* prev_out, double* psi_prev_out, int mem,
+                    double* dt_prev, int* have_prev) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    if (!prev_out || !psi_prev_out || !dt_prev || !have_prev)
+      throw std::runtime_error("smc_get_history: null pointer");
+    copy_out(m, prev_out, m.dPrev, mem, m.n * sizeof(double2));
+    copy_out(m, psi_prev_out, m.dPsiPrev, mem, m.n * sizeof(double2));
+    *dt_prev = m.dt_prev;
+    *have_prev = m.have_prev ? 1 : 0;
+  })
+}
+
+int smc_set_history(smc_handle* h, const double* prev, const double* psi_prev, int mem,
+                    double dt_prev, int have_prev) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    if (have_prev) {
+      if (!prev || !psi_prev) throw std::runtime_error("smc_set_history: null pointer");
+      if (!(dt_prev > 0.0)) throw std::runtime_error("smc_set_history: dt_prev must be > 0");
+      copy_in(m, m.dPrev, prev, mem, m.n);
+      copy_in(m, m.dPsiPrev, psi_prev, mem, m.n);
+      SMC_CUDA(cudaStreamSynchronize(m.stream));
+    }
+    m.dt_prev = have_prev ? dt_prev : 0.0;
+    m.have_prev = have_prev != 0 && m.cfg.model != SMC_MODEL_CONST;
+  })
+}
+
 int smc_counters_get(smc_handle* h, smc_counters* out) {
   SMC_GUARD(h, {
     *out = h->m.ctr;

@@ -181,6 +181,31 @@ class GpuModel:
     def reset_history(self):
         _lib.check(self._lib.smc_reset_history(self._h))
 
+    def get_history(self):
+        """-> dict(prev, psi_prev, dt_prev, have_prev): the BDF2 history of the
+        temperature step (NumPy arrays)."""
+        prev = np.empty((self.Nk, self.Nz), dtype=np.complex128)
+        psi = np.empty_like(prev)
+        dtp = ctypes.c_double()
+        have = ctypes.c_int()
+        _lib.check(self._lib.smc_get_history(self._h, prev.ctypes.data_as(ctypes.c_void_p),
+                                             psi.ctypes.data_as(ctypes.c_void_p), _lib.SMC_HOST,
+                                             ctypes.byref(dtp), ctypes.byref(have)))
+        return dict(prev=prev, psi_prev=psi, dt_prev=float(dtp.value), have_prev=bool(have.value))
+
+    def set_history(self, prev=None, psi_prev=None, dt_prev=0.0, have_prev=False):
+        """Install a BDF2 history (as returned by :meth:`get_history`)."""
+        if have_prev:
+            a = np.ascontiguousarray(prev, dtype=np.complex128)
+            b = np.ascontiguousarray(psi_prev, dtype=np.complex128)
+            if a.shape != (self.Nk, self.Nz) or b.shape != (self.Nk, self.Nz):
+                raise ValueError("history arrays must be (Nk, Nz) = (%d, %d)" % (self.Nk, self.Nz))
+            _lib.check(self._lib.smc_set_history(self._h, a.ctypes.data_as(ctypes.c_void_p),
+                                                 b.ctypes.data_as(ctypes.c_void_p), _lib.SMC_HOST,
+                                                 float(dt_prev), 1))
+        else:
+            _lib.check(self._lib.smc_set_history(self._h, None, None, _lib.SMC_HOST, 0.0, 0))
+
     # ---------------------------------------------------------- physics
     def stokes(self, that):
         p, mem, keep = self._spec_in(that)

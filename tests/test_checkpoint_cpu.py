@@ -1,0 +1,44 @@
+"""Checkpoint files (no GPU): the reference's layout and loader contract."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+from specmc_gb300 import checkpoint as ck  # noqa: E402
+
+
+def test_roundtrip_and_names(tmp_path):
+    that = (np.arange(12.0) + 1j * np.arange(12.0)[::-1]).reshape(3, 4)
+    p = ck.save(str(tmp_path), that, 0.125, n=7, fac=40.0)
+    assert os.path.basename(p) == "state_0.125000.npz"
+    assert not any(f.endswith(".tmp.npz") for f in os.listdir(tmp_path))
+    s, meta = ck.load(p)
+    assert np.array_equal(s, that)
+    assert meta["t"] == 0.125 and meta["n"] == 7 and meta["fac"] == 40.0
+    assert meta["keys"] == ["fac", "n", "t", "that"] and meta["history"] is None
+    ck.save(str(tmp_path), that, 0.5)
+    assert [t for t, _ in ck.list_(str(tmp_path))] == [0.125, 0.5]
+    assert ck.latest(str(tmp_path))[0] == 0.5
+    s2, m2 = ck.load(ck.latest(str(tmp_path))[1])
+    assert m2["n"] is None and m2["fac"] is None
+
+
+def test_loader_errors(tmp_path):
+    with pytest.raises(FileNotFoundError):
+        ck.load(str(tmp_path / "missing.npz"))
+    bad = tmp_path / "bad.npz"
+    np.savez(bad, x=np.zeros(3))
+    with pytest.raises(ValueError):
+        ck.load(str(bad))
+
+
+def test_files_of_the_reference_layout_load(tmp_path):
+    # a file written the way specmc/io/checkpoint.py:49-56 writes it
+    that = np.ones((2, 3), complex)
+    fn = tmp_path / "state_0.010000.npz"
+    np.savez_compressed(fn, that=that, t=0.01, n=None, fac=None)
+    s, meta = ck.load(str(fn))
+    assert np.array_equal(s, that) and meta["t"] == 0.01 and meta["n"] is None

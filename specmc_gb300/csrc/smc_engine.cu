@@ -64,7 +64,7 @@ struct EngCtx {
 #define SMC_PHASE_NAMES(P)                                                                   \
   {P ".start", P ".xconv", P ".xconv_wait", P ".post", P ".post_wait", P ".update_reduce",      \
    P ".update", P ".update_wait", P ".exact_norm", P ".next_reduce", P ".givens", P ".combine", \
-   P ".precond", P ".contract", P ".next_wait", P ".lsq", P ".resid"}
+   P ".precond", P ".contract", P ".next_wait", P ".lsq", P ".resid", P ".refine_residual"}
 const char* const engine_phase_names[2][ENGINE_PHASES] = {SMC_PHASE_NAMES("engine_stokes"),
                                                           SMC_PHASE_NAMES("engine_theta")};
 #undef SMC_PHASE_NAMES
@@ -775,23 +775,45 @@ __device__ void phase_update(const EngineOps& op, const EngineIO& io, const Cx<T
 }
 
 // ------------------------------------------------------------- the engine
+// Per-CTA shared state of one solve (every CTA holds identical values).
 template <class T>
-__global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(EngineOps op, EngineIO io) {
-  using C = Cx<T>;
-  cg::grid_group grid = cg::this_grid();
-  extern __shared__ __align__(256) unsigned char smraw[];
-  __shared__ T sh[8];
-  __shared__ C s_h1[ENG_MAXM], s_h2[ENG_MAXM], s_hc[ENG_MAXM + 1], s_acc[ENG_MAXM];
-  __shared__ T s_cs[ENG_MAXM];
-  __shared__ C s_sn[ENG_MAXM], s_g[ENG_MAXM + 1], s_y[ENG_MAXM];
-  __shared__ T s_nacc, s_hh;
-  __shared__ int s_flag;
+struct EngShared {
+  T sh[8];
+  Cx<T> h1[ENG_MAXM], h2[ENG_MAXM], hc[ENG_MAXM + 1], acc[ENG_MAXM];
+  T cs[ENG_MAXM];
+  Cx<T> sn[ENG_MAXM], g[ENG_MAXM + 1], y[ENG_MAXM];
+  T nacc, hh;
+  int flag;
+  double part[ENG_WARPS];
+  double b64;
+};
+
+__device__ __forceinline__ EngCtx eng_ctx(const EngineOps& op) {
   EngCtx e;
   e.G = gridDim.x; e.b = blockIdx.x; e.tid = threadIdx.x; e.lane = e.tid & 31; e.warp = e.tid >> 5;
   e.gw = e.b * ENG_WARPS + e.warp;
   e.nw = e.G * ENG_WARPS;
   e.R = op.Nk <= e.G ? e.G / op.Nk : 1;
   e.ntask = op.Nk * e.R;
+  return e;
+}
+
+// One right-preconditioned FGMRES solve of A x = io.b (x -> io.x, FP64) to
+// the relative tolerance io.rtol within io.maxiter Arnoldi steps; every CTA
+// of the cooperative grid calls it.  -> info (0 converged, 1 not, 2
+// breakdown, 3 non-finite data) and the Arnoldi steps taken.
+template <class T>
+__device__ void fgmres_solve(const EngineOps& op, const EngineIO& io, EngShared<T>& Q,
+                             unsigned char* smraw, const EngCtx& e, cg::grid_group& grid,
+                             PhaseClock& pc, int& info_out, int& total_out) {
+  using C = Cx<T>;
+  T* sh = Q.sh;
+  C *s_h1 = Q.h1, *s_h2 = Q.h2, *s_hc = Q.hc, *s_acc = Q.acc;
+  T* s_cs = Q.cs;
+  C *s_sn = Q.sn, *s_g = Q.g, *s_y = Q.y;
+  T& s_nacc = Q.nacc;
+  T& s_hh = Q.hh;
+  int& s_flag = Q.flag;
   EngSmem<T> S = eng_carve<T>(smraw, op.N, op.Mz);
   const long long n = io.n;
   const int m = io.restart;
@@ -808,8 +830,6 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
   // heavy cancellation in ||w'||^2 - ||h2||^2 below this fraction of ||w'||^2
   // means the Pythagorean norm has lost too many digits
   const T cancel = std::is_same<T, float>::value ? (T)1e-2 : (T)1e-4;
-  PhaseClock pc;
-  pc.init(io.phase_cycles, e);
 
   // x = 0; b64 = ||b|| in FP64; the Krylov process works on r = b / b64 (unit
   // norm, so nothing in T under- or overflows whatever the problem's scale)
@@ -823,26 +843,24 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
       s += bb.x * bb.x + bb.y * bb.y;
     }
     s = warp_sum(s);
-    __shared__ double s_part[ENG_WARPS];
-    if (e.lane == 0) s_part[e.warp] = s;
+    if (e.lane == 0) Q.part[e.warp] = s;
     __syncthreads();
     double* npd = io.npart;
     if (e.tid == 0) {
       double a = 0.0;
-      for (int q = 0; q < ENG_WARPS; ++q) a += s_part[q];
+      for (int q = 0; q < ENG_WARPS; ++q) a += Q.part[q];
       npd[e.b] = a;
     }
     grid.sync();
-    __shared__ double s_b64;
     if (e.warp == 0) {
       double a = 0.0;
 #pragma unroll 10
       for (int g = e.lane; g < e.G; g += 32) a += npd[g];
       a = warp_sum(a);
-      if (e.lane == 0) s_b64 = sqrt(a);
+      if (e.lane == 0) Q.b64 = sqrt(a);
     }
     __syncthreads();
-    b64 = s_b64;
+    b64 = Q.b64;
   }
   const double inv64 = (b64 > 0.0 && isfinite(b64)) ? 1.0 / b64 : 0.0;
   for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
@@ -1029,9 +1047,114 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
     if (beta <= tol) { info = 0; break; }
     if (!isfinite(beta)) { info = 3; break; }
   }
+  info_out = info;
+  total_out = total;
+}
+
+template <class T>
+__global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(EngineOps op, EngineIO io) {
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ __align__(256) unsigned char smraw[];
+  __shared__ EngShared<T> Q;
+  const EngCtx e = eng_ctx(op);
+  PhaseClock pc;
+  pc.init(io.phase_cycles, e);
+  int info = 1, total = 0;
+  fgmres_solve<T>(op, io, Q, smraw, e, grid, pc, info, total);
   if (e.b == 0 && e.tid == 0) {
     io.result[0] = info;
     io.result[1] = total;
+  }
+}
+
+// Iterative refinement in one launch: FP64 outer residuals r = b - A64 x
+// (the FP64 operator phases), FP32 inner FGMRES solves of A32 e = r to
+// max(0.3 tol / ||r||, floor), x += e, until ||r|| <= rtol ||b||, at most 12
+// outer passes and maxiter inner Arnoldi steps in all.
+__global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_engine_kernel(EngineOps op32, EngineOps op64,
+                                                                           EngineIO io, RefineIO rf) {
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ __align__(256) unsigned char smraw[];
+  __shared__ EngShared<float> Q;
+  __shared__ double s_red[8];
+  __shared__ double s_part[ENG_WARPS];
+  __shared__ double s_nacc64;
+  const EngCtx e = eng_ctx(op32);
+  PhaseClock pc;
+  pc.init(io.phase_cycles, e);
+  const long long n = io.n;
+  const long long per = (n + e.G - 1) / e.G;
+  const long long lo = (long long)e.b * per, hi = min(n, lo + per);
+  double* npr = io.npart + e.G;           // the inner solve uses io.npart[0, G)
+  // x = 0, r = b, ||b||
+  {
+    double s = 0.0;
+    for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
+      const double2 bb = rf.b[t];
+      rf.x[t] = make_double2(0.0, 0.0);
+      rf.r[t] = bb;
+      s += bb.x * bb.x + bb.y * bb.y;
+    }
+    s = warp_sum(s);
+    if (e.lane == 0) s_part[e.warp] = s;
+    __syncthreads();
+    if (e.tid == 0) {
+      double a = 0.0;
+      for (int q = 0; q < ENG_WARPS; ++q) a += s_part[q];
+      npr[e.b] = a;
+    }
+    grid.sync();
+  }
+  const double bn = sqrt(reduce_scalar<double>(npr, e.G, s_red, e));
+  const double tol = rf.rtol * bn;
+  double beta = bn;
+  int total = 0, outer = 0, info = 1;
+  EngSmem<double> S64 = eng_carve<double>(smraw, op64.N, op64.Mz);
+  EngineIO o64 = io;
+  o64.b = rf.b;
+  o64.x = rf.x;
+  o64.r = rf.r;
+  while (outer < 12) {
+    if (beta <= tol) { info = 0; break; }
+    if (!isfinite(beta)) { info = 3; break; }
+    if (total >= rf.maxiter) break;
+    EngineIO in = io;
+    in.b = rf.r;
+    in.x = rf.e;
+    in.rtol = fmax(0.3 * tol / beta, rf.floor);
+    in.maxiter = rf.maxiter - total;
+    int inf = 1, its = 0;
+    fgmres_solve<float>(op32, in, Q, smraw, e, grid, pc, inf, its);
+    total += its;
+    if (inf == 3) { info = 3; break; }
+    for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
+      const double2 a = rf.x[t], d = rf.e[t];
+      rf.x[t] = make_double2(a.x + d.x, a.y + d.y);
+    }
+    grid.sync();
+    // r = b - A64 x
+    phase_prep<double>(op64, o64, 2, 0, 1.0, nullptr, 0, S64, e, nullptr, 1.0);
+    grid.sync();
+    if (op64.kind == 0) ph_schur_x<double>(op64, smraw, e);
+    else ph_theta_x<double>(op64, smraw, e);
+    grid.sync();
+    if (e.tid == 0) s_nacc64 = 0.0;
+    __syncthreads();
+    phase_post<double>(op64, o64, true, rf.x, 1.0, 0, S64, nullptr, &s_nacc64, e);
+    __syncthreads();
+    if (e.tid == 0) npr[e.b] = s_nacc64;
+    grid.sync();
+    beta = sqrt(reduce_scalar<double>(npr, e.G, s_red, e));
+    ++outer;
+    pc.mark(EP_REFINE);
+    if (its == 0 && beta > tol) break;             // no progress possible
+  }
+  if (beta <= tol && info != 3) info = 0;
+  if (e.b == 0 && e.tid == 0) {
+    io.result[0] = info;
+    io.result[1] = total;
+    io.result[2] = outer;
+    rf.res[0] = beta / fmax(bn, 1e-300);
   }
 }
 
@@ -1071,6 +1194,28 @@ static void engine_launch(const Ctx& c, const EngineOps& op, const EngineIO& io)
   EngineOps o = op;
   EngineIO i = io;
   void* args[] = {(void*)&o, (void*)&i};
+  CoopGuard guard(c.s);
+  SMC_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(G), dim3(ENG_THREADS), args, sm, c.s));
+  SMC_LAUNCH_CHECK(c);
+}
+
+void fgmres_refine_engine(const Ctx& c, const EngineOps& op32, const EngineOps& op64,
+                          const EngineIO& io, const RefineIO& rf) {
+  if (io.restart + 1 > ENG_MAXM) throw std::runtime_error("fgmres engine: restart above 99");
+  const size_t s32 = engine_smem<float>(op32), s64 = engine_smem<double>(op64);
+  const size_t sm = s32 > s64 ? s32 : s64;
+  auto kern = smc_refine_engine_kernel;
+  allow_max_smem((const void*)kern);
+  int per_sm = 0;
+  SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ENG_THREADS, sm));
+  if (per_sm < 1) throw std::runtime_error("refinement engine: kernel cannot be co-resident");
+  int G = c.num_sms * (per_sm >= 2 ? 2 : 1);
+  if (io.grid_cap > 0 && io.grid_cap < G) G = io.grid_cap;
+  if (G > io.max_grid) throw std::runtime_error("refinement engine: partial buffers too small");
+  EngineOps a = op32, b = op64;
+  EngineIO i = io;
+  RefineIO r = rf;
+  void* args[] = {(void*)&a, (void*)&b, (void*)&i, (void*)&r};
   CoopGuard guard(c.s);
   SMC_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(G), dim3(ENG_THREADS), args, sm, c.s));
   SMC_LAUNCH_CHECK(c);

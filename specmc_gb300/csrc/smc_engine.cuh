@@ -77,11 +77,27 @@ enum EnginePhase {
   EP_NEXT_WAIT,
   EP_LSQ,        // triangular solve + x update at the end of a cycle
   EP_RESID,      // true residual at a restart
+  EP_REFINE,     // FP64 residual of an outer refinement pass (refinement engine)
   ENGINE_PHASES
 };
 extern const char* const engine_phase_names[2][ENGINE_PHASES];
 
 void fgmres_engine(const Ctx& c, const EngineOps& op, const EngineIO& io, bool fp32);
+
+// The outer loop of FP32-inner / FP64-outer iterative refinement, on the device
+struct RefineIO {
+  const double2* b = nullptr;   // right-hand side (FP64)
+  double2* x = nullptr;         // solution (FP64)
+  double2* r = nullptr;         // outer residual scratch (FP64, n)
+  double2* e = nullptr;         // inner correction scratch (FP64, n)
+  double rtol = 1e-8;           // outer relative tolerance
+  double floor = 1e-4;          // smallest inner relative tolerance
+  int maxiter = 800;            // inner Arnoldi steps in all
+  double* res = nullptr;        // -> final relative residual (device)
+};
+// io: the engine workspace; io.result -> {info, inner steps, outer passes}
+void fgmres_refine_engine(const Ctx& c, const EngineOps& op32, const EngineOps& op64,
+                          const EngineIO& io, const RefineIO& rf);
 
 // out[b][c][r] = (To) in[b][r][c] for batch matrices of rows x cols
 void transpose_as(const Ctx& c, const double* in, float* out, long long rows, long long cols, int batch);

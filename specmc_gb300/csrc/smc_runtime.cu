@@ -351,6 +351,7 @@ struct Model {
   bool eng_phase = false;            // per-phase cycle counts of engine solves into the profiler
   int eng_ctas = 0;                  // > 0: cap on the engine's CTAs (handles sharing the GPU)
   long long* dEngPhase = nullptr;    // ENGINE_PHASES accumulators
+  double* dEngRes = nullptr;         // final relative residual of a refinement launch
   double sm_khz = 0.0;               // peak SM clock (cycles -> ms)
 
   // ------------------------------------------------------------ utilities
@@ -539,6 +540,7 @@ struct Model {
         eio.result = dEngInt + 4;
         eio.V = dKV; eio.Z = dKZ; eio.w = dKw; eio.r = dKr;
         dEngPhase = mem.alloc<long long>(ENGINE_PHASES);
+        dEngRes = mem.alloc<double>(2);
         {
           int khz = 0;
           SMC_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, device));
@@ -842,9 +844,7 @@ struct Model {
   }
 
   // one FGMRES solve in the persistent engine; kind 0 = Schur, 1 = theta
-  FgmresResult engine_solve(int kind, bool fp32, const double2* b, double2* x, double rtol,
-                            int restart, int maxiter, const void* GpT, double palpha) {
-    ProfScope ps(ctx, kind == 0 ? "engine_stokes" : "engine_theta", 0.0, 1);
+  EngineOps engine_ops(int kind, bool fp32, const void* GpT, double palpha) const {
     const EngMats& em = fp32 ? em32 : em64;
     EngineOps op;
     op.kind = kind; op.Nk = Nk; op.N = N; op.kx = dkx; op.V64 = dV;
@@ -864,6 +864,13 @@ struct Model {
       else { op.twT = ft64.tw; op.ux = gr[0]; op.uz = gr[1]; }
       op.X = dFtX; op.A = dFtA;
     }
+    return op;
+  }
+
+  FgmresResult engine_solve(int kind, bool fp32, const double2* b, double2* x, double rtol,
+                            int restart, int maxiter, const void* GpT, double palpha) {
+    ProfScope ps(ctx, kind == 0 ? "engine_stokes" : "engine_theta", 0.0, 1);
+    const EngineOps op = engine_ops(kind, fp32, GpT, palpha);
     EngineIO io = eio;
     io.b = b; io.x = x; io.rtol = rtol; io.n = n;
     io.restart = std::max(1, std::min(restart, mmax));
@@ -888,6 +895,50 @@ struct Model {
     fr.info = res[0];
     fr.iters = res[1];
     ps.work = engine_bytes(kind, fp32, fr.iters, io.restart);
+    return fr;
+  }
+
+  // The whole FP32-inner / FP64-outer refinement in one engine launch (the
+  // device runs the outer loop of fgmres_refined below); -> (info, inner
+  // Arnoldi steps), *true_res = final relative FP64 residual.
+  FgmresResult engine_refine(int kind, const double2* b, double2* x, double rtol, int maxiter,
+                             int restart, const void* GpT32, const void* GpT64, double palpha,
+                             double* true_res) {
+    ProfScope ps(ctx, kind == 0 ? "engine_stokes" : "engine_theta", 0.0, 1);
+    const EngineOps op32 = engine_ops(kind, true, GpT32, palpha);
+    const EngineOps op64 = engine_ops(kind, false, GpT64, palpha);
+    EngineIO io = eio;
+    io.n = n;
+    io.restart = std::max(1, std::min(restart, mmax));
+    io.grid_cap = eng_ctas;
+    RefineIO rf;
+    rf.b = b; rf.x = x; rf.r = dRefR; rf.e = dRefE;
+    rf.rtol = rtol; rf.floor = inner_floor; rf.maxiter = maxiter; rf.res = dEngRes;
+    const bool phases = eng_phase && prof.enabled;
+    if (phases) {
+      SMC_CUDA(cudaMemsetAsync(dEngPhase, 0, ENGINE_PHASES * sizeof(long long), stream));
+      io.phase_cycles = dEngPhase;
+    }
+    fgmres_refine_engine(ctx, op32, op64, io, rf);
+    int res[3];
+    double rel = 0.0;
+    long long cyc[ENGINE_PHASES];
+    SMC_CUDA(cudaMemcpyAsync(res, eio.result, sizeof(res), cudaMemcpyDeviceToHost, stream));
+    SMC_CUDA(cudaMemcpyAsync(&rel, dEngRes, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (phases)
+      SMC_CUDA(cudaMemcpyAsync(cyc, dEngPhase, sizeof(cyc), cudaMemcpyDeviceToHost, stream));
+    SMC_CUDA(cudaStreamSynchronize(stream));
+    if (phases)
+      for (int q = 0; q < ENGINE_PHASES; ++q)
+        prof.add(engine_phase_names[kind][q], (double)cyc[q] / sm_khz, 1);
+    FgmresResult fr;
+    fr.info = res[0];
+    fr.iters = res[1];
+    n_outer += res[2];
+    if (true_res) *true_res = rel;
+    // inner solves plus one FP64 operator application per outer pass
+    ps.work = engine_bytes(kind, true, fr.iters, io.restart) +
+              res[2] * 2.0 * engine_bytes(kind, true, 1, io.restart);
     return fr;
   }
 
@@ -1225,12 +1276,15 @@ struct Model {
       const bool fp32_now = inner_fp32 && stokes_fp64_solves == 0;
       if (!fp32_now && stokes_fp64_solves > 0) --stokes_fp64_solves;
       if (fp32_now) {
-        InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
-          if (use_engine)
-            return engine_solve(0, true, r, e, tol, cfg.stokes_restart, mi, dRedGT32, 1.0);
-          return fgmres(A32, M, r, e, tol, cfg.stokes_restart, mi);
-        };
-        fr = fgmres_refined(A64, inner, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, &res);
+        if (use_engine) {
+          fr = engine_refine(0, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, cfg.stokes_restart,
+                             dRedGT32, dRedGT64, 1.0, &res);
+        } else {
+          InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
+            return fgmres(A32, M, r, e, tol, cfg.stokes_restart, mi);
+          };
+          fr = fgmres_refined(A64, inner, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, &res);
+        }
         if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
           // the FP32 operator cannot resolve this system (viscosity contrast
           // too large for its rounding): solve it in FP64 and stay in FP64
@@ -1507,12 +1561,15 @@ struct Model {
       Op A32 = [&](const double2* v, double2* o) { theta_matvec_fast(v, o, true); };
       double tr = 0.0;
       if (inner_fp32) {
-        InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
-          if (use_engine)
-            return engine_solve(1, true, r, e, tol, cfg.theta_restart, mi, Lp->GinvT32, -1.0);
-          return fgmres(A32, M, r, e, tol, cfg.theta_restart, mi);
-        };
-        fr = fgmres_refined(A64, inner, dKb, dRhs, cfg.theta_rtol, cfg.theta_maxiter, &tr);
+        if (use_engine) {
+          fr = engine_refine(1, dKb, dRhs, cfg.theta_rtol, cfg.theta_maxiter, cfg.theta_restart,
+                             Lp->GinvT32, Lp->GinvT64, -1.0, &tr);
+        } else {
+          InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
+            return fgmres(A32, M, r, e, tol, cfg.theta_restart, mi);
+          };
+          fr = fgmres_refined(A64, inner, dKb, dRhs, cfg.theta_rtol, cfg.theta_maxiter, &tr);
+        }
         if (fr.info == 3) {
           // non-finite values in the FP32 inner solves: redo the solve in FP64
           ++n_fp64_fallback;

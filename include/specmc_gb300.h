@@ -186,14 +186,20 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
  * "krylov_engine" (0/1, SMC_MIXED handles, default 1): run each of those
  * FGMRES solves in one persistent cooperative kernel on the device (1) or
  * with host-side control per iteration (0).
- * "inner_rtol_floor" (0 < f < 1, default 1e-4): smallest relative tolerance
- * asked of an FP32 inner solve of the mixed form (its operator's rounding
- * limits what a tighter inner solve could gain).
+ * "inner_rtol_floor" (0 < f < 1): smallest relative tolerance asked of an
+ * FP32 inner solve of the mixed form, for the Stokes and the temperature
+ * solves; "stokes_inner_rtol_floor" (default 1e-3) and
+ * "theta_inner_rtol_floor" (default 1e-4) set one of them.  The FP32
+ * operator's rounding limits what an outer pass gains (about 2e-2 for the
+ * Stokes operator at a 1e3 viscosity contrast), so a tighter inner solve
+ * only adds Arnoldi steps.
  * "theta_precond_lag" (0 <= f < 1, default 0.3): the mixed form reuses the
  * temperature preconditioner while a0 stays within this relative distance
  * of the a0 it was built for (0: rebuild for every new a0, as the reference).
- * "engine_ctas" (>= 0, default 0 = one or two CTAs per SM): cap on the CTAs of
- * the persistent Krylov engine, for handles that share the GPU concurrently.
+ * "engine_ctas" (>= 0): the CTAs of the persistent Krylov engine, for handles
+ * that share the GPU concurrently; default 0 = Nk R CTAs, R the smallest
+ * count that leaves at most two z-points of the x-direction phase to a CTA,
+ * capped at the co-resident maximum (one or two CTAs per SM).
  * "engine_phase_profile" (0/1, default 0): while the profiler is on, add the
  * engine's time between grid barriers, per phase, as profile regions named
  * "engine_stokes.<phase>" / "engine_theta.<phase>" (SM cycles of one CTA at

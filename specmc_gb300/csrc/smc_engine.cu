@@ -64,7 +64,8 @@ struct EngCtx {
 #define SMC_PHASE_NAMES(P)                                                                   \
   {P ".start", P ".xconv", P ".xconv_wait", P ".post", P ".post_wait", P ".update_reduce",      \
    P ".update", P ".update_wait", P ".exact_norm", P ".next_reduce", P ".givens", P ".combine", \
-   P ".precond", P ".contract", P ".next_wait", P ".lsq", P ".resid", P ".refine_residual"}
+   P ".precond", P ".contract", P ".next_wait", P ".lsq", P ".resid", P ".refine_xupdate",     \
+   P ".refine_contract", P ".refine_xconv", P ".refine_post", P ".refine_norm"}
 const char* const engine_phase_names[2][ENGINE_PHASES] = {SMC_PHASE_NAMES("engine_stokes"),
                                                           SMC_PHASE_NAMES("engine_theta")};
 #undef SMC_PHASE_NAMES
@@ -1132,18 +1133,22 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_engine_kernel(Engin
       rf.x[t] = make_double2(a.x + d.x, a.y + d.y);
     }
     grid.sync();
+    pc.mark(EP_REF_XUPD);
     // r = b - A64 x
     phase_prep<double>(op64, o64, 2, 0, 1.0, nullptr, 0, S64, e, nullptr, 1.0);
     grid.sync();
+    pc.mark(EP_REF_PREP);
     if (op64.kind == 0) ph_schur_x<double>(op64, smraw, e);
     else ph_theta_x<double>(op64, smraw, e);
     grid.sync();
+    pc.mark(EP_REF_XCONV);
     if (e.tid == 0) s_nacc64 = 0.0;
     __syncthreads();
     phase_post<double>(op64, o64, true, rf.x, 1.0, 0, S64, nullptr, &s_nacc64, e);
     __syncthreads();
     if (e.tid == 0) npr[e.b] = s_nacc64;
     grid.sync();
+    pc.mark(EP_REF_POST);
     beta = sqrt(reduce_scalar<double>(npr, e.G, s_red, e));
     ++outer;
     pc.mark(EP_REFINE);

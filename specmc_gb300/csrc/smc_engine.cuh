@@ -77,7 +77,13 @@ enum EnginePhase {
   EP_NEXT_WAIT,
   EP_LSQ,        // triangular solve + x update at the end of a cycle
   EP_RESID,      // true residual at a restart
-  EP_REFINE,     // FP64 residual of an outer refinement pass (refinement engine)
+  // outer pass of the refinement engine: x += e, then r = b - A64 x in the
+  // FP64 operator phases, then ||r||
+  EP_REF_XUPD,
+  EP_REF_PREP,   // FP64 z-contraction of x
+  EP_REF_XCONV,  // FP64 x-direction convolution
+  EP_REF_POST,   // FP64 epilogue r = b - A x and ||r||^2 partials
+  EP_REFINE,     // ||r|| reduction
   ENGINE_PHASES
 };
 extern const char* const engine_phase_names[2][ENGINE_PHASES];

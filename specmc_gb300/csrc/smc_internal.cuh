@@ -34,7 +34,7 @@ struct CudaError : std::runtime_error {
 // the kernels of a tag with CUDA events on the handle's stream; elapsed
 // times are resolved (and the events recycled) by Profiler::resolve.
 struct Profiler {
-  static constexpr int MAXTAG = 48;
+  static constexpr int MAXTAG = 64;
   bool enabled = false;
   const char* names[MAXTAG] = {nullptr};
   double ms[MAXTAG] = {0};

@@ -339,7 +339,8 @@ struct Model {
   long long n_outer = 0;
   int matvec_variant = 0;   // smc_schur_matvec: 0 plain, 1 fused FP64, 2 fused FP32
   bool inner_fp32 = true;   // fast form: FP32 inner Krylov operators + FP64 refinement
-  double inner_floor = 1e-4; // smallest relative tolerance asked of an FP32 inner solve
+  // smallest relative tolerance asked of an FP32 inner solve: Stokes, temperature
+  double inner_floor[2] = {1e-3, 1e-4};
   double theta_lag = 0.3;    // fast form: relative a0 change before the theta preconditioner is rebuilt
   long long n_theta_lag_hits = 0;
   long long n_fp64_fallback = 0;     // fast form: inner FP32 solves redone in FP64
@@ -350,6 +351,7 @@ struct Model {
   int* dEngInt = nullptr;
   bool eng_phase = false;            // per-phase cycle counts of engine solves into the profiler
   int eng_ctas = 0;                  // > 0: cap on the engine's CTAs (handles sharing the GPU)
+  int eng_auto_ctas = 0;             // the engine's grid when eng_ctas is 0 (set in setup)
   long long* dEngPhase = nullptr;    // ENGINE_PHASES accumulators
   double* dEngRes = nullptr;         // final relative residual of a refinement launch
   double sm_khz = 0.0;               // peak SM clock (cycles -> ms)
@@ -621,6 +623,13 @@ struct Model {
         psplan.Nk = Nk; psplan.N = N; psplan.Mz = 2 * N - 1;
         psplan.L = 1;
         while (psplan.L < 3 * Nk - 2) psplan.L <<= 1;
+        // default engine grid: R CTAs per Fourier row, R the smallest count
+        // that leaves at most two of the Mz z-points of the x-direction phase
+        // to a CTA.  A small problem then runs on fewer CTAs than the GPU
+        // holds, which makes its grid barriers and partial-sum reductions
+        // cheaper (64x96: 99 CTAs, 17% less time per step than 304); the
+        // launch caps it at the co-resident maximum.
+        eng_auto_ctas = Nk * std::max(1, (psplan.Mz + 2 * Nk - 1) / (2 * Nk));
         {
           const int Mz = psplan.Mz, L = psplan.L;
           std::vector<double> Zf((size_t)Mz * N), Zi((size_t)N * Mz);
@@ -875,7 +884,7 @@ struct Model {
     io.b = b; io.x = x; io.rtol = rtol; io.n = n;
     io.restart = std::max(1, std::min(restart, mmax));
     io.maxiter = maxiter;
-    io.grid_cap = eng_ctas;
+    io.grid_cap = eng_ctas > 0 ? eng_ctas : eng_auto_ctas;
     const bool phases = eng_phase && prof.enabled;
     if (phases) {
       SMC_CUDA(cudaMemsetAsync(dEngPhase, 0, ENGINE_PHASES * sizeof(long long), stream));
@@ -910,10 +919,10 @@ struct Model {
     EngineIO io = eio;
     io.n = n;
     io.restart = std::max(1, std::min(restart, mmax));
-    io.grid_cap = eng_ctas;
+    io.grid_cap = eng_ctas > 0 ? eng_ctas : eng_auto_ctas;
     RefineIO rf;
     rf.b = b; rf.x = x; rf.r = dRefR; rf.e = dRefE;
-    rf.rtol = rtol; rf.floor = inner_floor; rf.maxiter = maxiter; rf.res = dEngRes;
+    rf.rtol = rtol; rf.floor = inner_floor[kind]; rf.maxiter = maxiter; rf.res = dEngRes;
     const bool phases = eng_phase && prof.enabled;
     if (phases) {
       SMC_CUDA(cudaMemsetAsync(dEngPhase, 0, ENGINE_PHASES * sizeof(long long), stream));
@@ -928,9 +937,10 @@ struct Model {
     if (phases)
       SMC_CUDA(cudaMemcpyAsync(cyc, dEngPhase, sizeof(cyc), cudaMemcpyDeviceToHost, stream));
     SMC_CUDA(cudaStreamSynchronize(stream));
-    if (phases)
+    if (phases)       // the refinement slots count outer passes
       for (int q = 0; q < ENGINE_PHASES; ++q)
-        prof.add(engine_phase_names[kind][q], (double)cyc[q] / sm_khz, 1);
+        prof.add(engine_phase_names[kind][q], (double)cyc[q] / sm_khz,
+                 q >= EP_REF_XUPD ? res[2] : 1);
     FgmresResult fr;
     fr.info = res[0];
     fr.iters = res[1];
@@ -947,7 +957,7 @@ struct Model {
   // (info, inner iterations) and the final true relative residual.
   using InnerSolve = std::function<FgmresResult(const double2*, double2*, double, int)>;
   FgmresResult fgmres_refined(const Op& A64, const InnerSolve& inner, const double2* b,
-                              double2* x, double rtol, int maxiter, double* true_res) {
+                              double2* x, double rtol, int maxiter, double floor, double* true_res) {
     FgmresResult res;
     vec_zero(ctx, x, n * sizeof(double2));
     const double bn = norm(b);
@@ -959,7 +969,7 @@ struct Model {
     for (int outer = 0; outer < 12; ++outer) {
       if (beta <= tol) { res.info = 0; break; }
       if (total >= maxiter) break;
-      const double inner_rtol = std::max(0.3 * tol / beta, inner_floor);
+      const double inner_rtol = std::max(0.3 * tol / beta, floor);
       FgmresResult fr = inner(dRefR, dRefE, inner_rtol, maxiter - total);
       total += fr.iters;
       if (fr.info == 3) { res.info = 3; break; }   // non-finite data in the inner solve
@@ -1283,7 +1293,8 @@ struct Model {
           InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
             return fgmres(A32, M, r, e, tol, cfg.stokes_restart, mi);
           };
-          fr = fgmres_refined(A64, inner, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, &res);
+          fr = fgmres_refined(A64, inner, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, inner_floor[0],
+                              &res);
         }
         if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
           // the FP32 operator cannot resolve this system (viscosity contrast
@@ -1568,7 +1579,8 @@ struct Model {
           InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
             return fgmres(A32, M, r, e, tol, cfg.theta_restart, mi);
           };
-          fr = fgmres_refined(A64, inner, dKb, dRhs, cfg.theta_rtol, cfg.theta_maxiter, &tr);
+          fr = fgmres_refined(A64, inner, dKb, dRhs, cfg.theta_rtol, cfg.theta_maxiter, inner_floor[1],
+                              &tr);
         }
         if (fr.info == 3) {
           // non-finite values in the FP32 inner solves: redo the solve in FP64
@@ -2069,9 +2081,11 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
     } else if (k == "theta_precond_lag") {
       if (!(value >= 0.0 && value < 1.0)) throw std::runtime_error("theta_precond_lag must be in [0, 1)");
       h->m.theta_lag = value;
-    } else if (k == "inner_rtol_floor") {
-      if (!(value > 0.0 && value < 1.0)) throw std::runtime_error("inner_rtol_floor must be in (0, 1)");
-      h->m.inner_floor = value;
+    } else if (k == "inner_rtol_floor" || k == "stokes_inner_rtol_floor" ||
+               k == "theta_inner_rtol_floor") {
+      if (!(value > 0.0 && value < 1.0)) throw std::runtime_error(k + " must be in (0, 1)");
+      if (k[0] != 't') h->m.inner_floor[0] = value;
+      if (k[0] != 's') h->m.inner_floor[1] = value;
     } else if (k == "engine_ctas") {
       if (!(value >= 0.0 && value <= 1e6)) throw std::runtime_error("engine_ctas must be >= 0");
       h->m.eng_ctas = (int)value;

@@ -138,7 +138,10 @@ int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety,
 /* Kernel-region timing with CUDA events on the handle's stream (no
  * reference counterpart; the reference keeps wall-clock accumulators
  * t_stokes/t_refresh, coupled_model.py:329-330).  smc_profile(h, 1) resets
- * and enables; smc_profile_get returns slot `slot` (name NULL past the last):
+ * and enables every region, smc_profile(h, 2) only the Krylov engine regions
+ * ("engine_stokes", "engine_theta": two events per solve, so a timed march
+ * is not perturbed), smc_profile(h, 0) disables; smc_profile_get returns slot
+ * `slot` (name NULL past the last):
  * total ms, launches, and the algorithmic work counted for those launches
  * (flops, or bytes when *work_is_bytes). */
 int smc_profile(smc_handle* h, int enable);

@@ -76,10 +76,14 @@ __global__ void smc_lu_small_kernel(double* __restrict__ A, int* __restrict__ pi
       inf = c + 1;
     }
     __syncthreads();
-    const int m = N - c - 1;
-    for (int t = tid; t < m * m; t += nt) {
-      int r = c + 1 + t % m, col = c + 1 + t / m;
-      a[r + col * N] -= a[r + c * N] * a[c + col * N];
+    // rank-1 update of the trailing block: lanes over rows, the CTA's warps
+    // over columns (each element gets the same single update per step)
+    {
+      const int nw = nt >> 5, lane = tid & 31;
+      for (int col = c + 1 + (tid >> 5); col < N; col += nw) {
+        const double u = a[c + col * N];
+        for (int r = c + 1 + lane; r < N; r += 32) a[r + col * N] -= a[r + c * N] * u;
+      }
     }
     __syncthreads();
   }
@@ -246,9 +250,60 @@ __global__ void smc_green_kernel(const double* __restrict__ LU, const int* __res
   for (int p = tid; p < N; p += blockDim.x) Gk[(long long)p * N + q] = xs[p].x;
 }
 
+// The same columns, GREEN_COLS per CTA, one thread per column: each thread
+// runs the row permutation and the two substitutions of lu_real_solve_smem on
+// its own column (the same operations in the same order, hence the same
+// values) without any barrier; all lanes read the same LU entry at a time
+// (a broadcast).  The per-column CTAs above wait at 2N barriers per column.
+static constexpr int GREEN_COLS = 32;
+static constexpr int GREEN_COLS_MAXN = 160;      // N x 32 doubles of shared memory <= 40 KB
+__global__ void __launch_bounds__(GREEN_COLS) smc_green_cols_kernel(const double* __restrict__ LU,
+                                                                   const int* __restrict__ piv,
+                                                                   double* __restrict__ G, int N) {
+  extern __shared__ double xcol[];       // row r of lane l's column at xcol[r * GREEN_COLS + l]
+  const int k = blockIdx.x, lane = threadIdx.x;
+  const int q = blockIdx.y * GREEN_COLS + lane;
+  if (q >= N) return;
+  double* Gk = G + (long long)k * N * N;
+  if (q >= N - 2) {
+    for (int p = 0; p < N; ++p) Gk[(long long)p * N + q] = 0.0;
+    return;
+  }
+  const double* L = LU + (long long)k * N * N;
+  const int* pv = piv + (long long)k * N;
+  double* x = xcol + lane;
+  for (int i = 0; i < N; ++i) x[i * GREEN_COLS] = (i == q) ? 1.0 : 0.0;
+  for (int i = 0; i < N; ++i) {
+    const int p = pv[i];
+    if (p != i) {
+      const double t = x[i * GREEN_COLS];
+      x[i * GREEN_COLS] = x[p * GREEN_COLS];
+      x[p * GREEN_COLS] = t;
+    }
+  }
+  for (int c = 0; c < N; ++c) {          // unit lower
+    const double xc = x[c * GREEN_COLS];
+    const double* Lc = L + (long long)c * N;
+    for (int r = c + 1; r < N; ++r) x[r * GREEN_COLS] -= Lc[r] * xc;
+  }
+  for (int c = N - 1; c >= 0; --c) {     // upper
+    const double* Lc = L + (long long)c * N;
+    x[c * GREEN_COLS] /= Lc[c];
+    const double xc = x[c * GREEN_COLS];
+    for (int r = 0; r < c; ++r) x[r * GREEN_COLS] -= Lc[r] * xc;
+  }
+  for (int p = 0; p < N; ++p) Gk[(long long)p * N + q] = x[p * GREEN_COLS];
+}
+
 void green_from_lu(const Ctx& c, const double* LUcm, const int* piv, double* G, int N, int Nk) {
-  dim3 grd(Nk, N);
-  smc_green_kernel<<<grd, 128, N * sizeof(double2), c.s>>>(LUcm, piv, G, N);
+  if (N <= GREEN_COLS_MAXN) {
+    dim3 grd(Nk, (N + GREEN_COLS - 1) / GREEN_COLS);
+    smc_green_cols_kernel<<<grd, GREEN_COLS, (size_t)N * GREEN_COLS * sizeof(double), c.s>>>(LUcm, piv,
+                                                                                         G, N);
+  } else {
+    dim3 grd(Nk, N);
+    smc_green_kernel<<<grd, 128, N * sizeof(double2), c.s>>>(LUcm, piv, G, N);
+  }
   SMC_LAUNCH_CHECK(c);
 }
 

@@ -7,6 +7,7 @@
 //                                       (column-major, used by LU factors)
 //   dense Schur LU    (n, n) complex    column-major, n = Nk * Nz
 #pragma once
+#include <cstring>
 #include <mutex>
 
 #include <cuda_runtime.h>
@@ -36,6 +37,10 @@ struct CudaError : std::runtime_error {
 struct Profiler {
   static constexpr int MAXTAG = 64;
   bool enabled = false;
+  bool engine_only = false;       // time only the Krylov engine regions ("engine_*")
+  bool wants(const char* name) const {
+    return enabled && (!engine_only || std::strncmp(name, "engine_", 7) == 0);
+  }
   const char* names[MAXTAG] = {nullptr};
   double ms[MAXTAG] = {0};
   long long launches[MAXTAG] = {0};
@@ -75,7 +80,7 @@ struct ProfScope {
   int is_bytes;
   ProfScope(const Ctx& c_, const char* name, double work_ = 0.0, int is_bytes_ = 0)
       : c(c_), work(work_), is_bytes(is_bytes_) {
-    if (c.prof && c.prof->enabled) {
+    if (c.prof && c.prof->wants(name)) {
       tag = c.prof->tag_of(name);
       c.prof->begin(c.s, tag, &a);
     }

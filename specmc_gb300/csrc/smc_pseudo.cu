@@ -97,9 +97,12 @@ __global__ void smc_ps_eta_grid_kernel(const double2* __restrict__ Av, int Nk, i
   const int l = blockIdx.y;
   if (s >= Mz) return;
   double acc = 0.0;
+  int idx = 0;                           // d l mod L, stepped (l < L)
   for (int d = 1; d < Nk; ++d) {
+    idx += l;
+    if (idx >= L) idx -= L;
     double2 a = Av[(long long)d * Mz + s];
-    double2 t = tw[(long long)(d * l) % L];
+    double2 t = tw[idx];
     acc += a.x * t.x - a.y * t.y;
   }
   E[(long long)l * Mz + s] = Av[s].x + 2.0 * acc;
@@ -108,8 +111,10 @@ __global__ void smc_ps_eta_grid_kernel(const double2* __restrict__ Av, int Nk, i
 void ps_eta_grid(const Ctx& c, const PsPlan& pl, const double2* eta_c, double2* work, double* E) {
   PsJobs j{};
   j.f[0] = eta_c;
-  dim3 g1(ceil_div(pl.Mz, 128), pl.Nk, 1);
-  smc_ps_zfwd_kernel<<<g1, 128, 0, c.s>>>(j, pl.Zf, pl.Nk, pl.N, pl.Mz, work);
+  // 32-thread CTAs: each thread keeps its serial dot product, the Nk Mz outputs
+  // spread over more SMs (FP64 latency bound)
+  dim3 g1(ceil_div(pl.Mz, 32), pl.Nk, 1);
+  smc_ps_zfwd_kernel<<<g1, 32, 0, c.s>>>(j, pl.Zf, pl.Nk, pl.N, pl.Mz, work);
   SMC_LAUNCH_CHECK(c);
   dim3 g2(ceil_div(pl.Mz, 128), pl.L);
   smc_ps_eta_grid_kernel<<<g2, 128, 0, c.s>>>(work, pl.Nk, pl.Mz, pl.L, pl.tw, E);

@@ -111,6 +111,36 @@ struct HostBasis {
   }
 };
 
+// inverse of a dense row-major n x n matrix by Gauss-Jordan elimination with
+// partial pivoting (set-up only)
+static std::vector<double> invert_dense(std::vector<double> A, int n) {
+  std::vector<double> X((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) X[(size_t)i * n + i] = 1.0;
+  for (int c = 0; c < n; ++c) {
+    int p = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(A[(size_t)r * n + c]) > std::fabs(A[(size_t)p * n + c])) p = r;
+    if (!(std::fabs(A[(size_t)p * n + c]) > 0.0)) throw std::runtime_error("invert_dense: singular matrix");
+    if (p != c)
+      for (int q = 0; q < n; ++q) {
+        std::swap(A[(size_t)p * n + q], A[(size_t)c * n + q]);
+        std::swap(X[(size_t)p * n + q], X[(size_t)c * n + q]);
+      }
+    const double inv = 1.0 / A[(size_t)c * n + c];
+    for (int q = 0; q < n; ++q) { A[(size_t)c * n + q] *= inv; X[(size_t)c * n + q] *= inv; }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = A[(size_t)r * n + c];
+      if (f == 0.0) continue;
+      for (int q = 0; q < n; ++q) {
+        A[(size_t)r * n + q] -= f * A[(size_t)c * n + q];
+        X[(size_t)r * n + q] -= f * X[(size_t)c * n + q];
+      }
+    }
+  }
+  return X;
+}
+
 // ------------------------------------------------------------ device memory
 // Every buffer is zeroed and every upload made on the handle's own stream:
 // that stream is non-blocking, so work on the legacy default stream would not
@@ -255,6 +285,8 @@ struct Model {
   bool resident_cur0 = true;
   DevMem mem;
   double* hbuf = nullptr;     // pinned scalars
+  unsigned char* hpin = nullptr;   // pinned: engine results (first 1 KB), BFBT profile
+  static_assert(64 + ENGINE_PHASES * sizeof(long long) <= 512, "engine phase slots overlap");
   smc_counters ctr{};
 
   std::unique_ptr<HostBasis> hb;
@@ -275,6 +307,7 @@ struct Model {
   double *dM0, *dDM0, *dT1, *dT2, *dT3, *dComm, *dCommG, *dPcm;
   double* dMpLU = nullptr;
   int* dMpPiv = nullptr;
+  double* dMpInv = nullptr;          // mixed form: explicit inverse, row-major
   // viscosity
   EtaLaw law;
   double *dEta = nullptr, *dEtaLag = nullptr, *dLastEta = nullptr, *dEtaP = nullptr,
@@ -441,6 +474,7 @@ struct Model {
     SMC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     ctx.s = stream; ctx.nlaunch = &nlaunch; ctx.num_sms = sms; ctx.prof = &prof;
     SMC_CUDA(cudaMallocHost(&hbuf, 4096 * sizeof(double)));
+    SMC_CUDA(cudaMallocHost(&hpin, 1024 + (size_t)N * sizeof(double2)));
     if (N < 4 || Nx < 4) throw std::runtime_error("Nx and Nz must be >= 4");
 
     hb.reset(new HostBasis(N));
@@ -678,6 +712,15 @@ struct Model {
         dMpLU = mem.upload(Mp);
         dMpPiv = mem.alloc<int>(N);
         lu_small_batched(ctx, dMpLU, dMpPiv, nullptr, N, 1);
+        // the mixed form applies M^{-1} as a GEMV (the profile only feeds the
+        // BFBT preconditioner there; a one-CTA triangular solve of N = 96
+        // costs ~200 us of serial FP64 latency per Stokes solve)
+        if (fast) {
+          std::vector<double> Mr(NN);
+          for (int a = 0; a < N; ++a)
+            for (int b = 0; b < N; ++b) Mr[(size_t)a * N + b] = Mp[(size_t)b * N + a];
+          dMpInv = mem.upload(invert_dense(Mr, N));
+        }
       }
     }
     SMC_CUDA(cudaStreamSynchronize(stream));
@@ -891,11 +934,12 @@ struct Model {
       io.phase_cycles = dEngPhase;
     }
     fgmres_engine(ctx, op, io, fp32);
-    int res[2];
-    long long cyc[ENGINE_PHASES];
-    SMC_CUDA(cudaMemcpyAsync(res, eio.result, sizeof(res), cudaMemcpyDeviceToHost, stream));
+    int* res = reinterpret_cast<int*>(hpin);                     // pinned: no staged copies
+    long long* cyc = reinterpret_cast<long long*>(hpin + 64);
+    SMC_CUDA(cudaMemcpyAsync(res, eio.result, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
     if (phases)
-      SMC_CUDA(cudaMemcpyAsync(cyc, dEngPhase, sizeof(cyc), cudaMemcpyDeviceToHost, stream));
+      SMC_CUDA(cudaMemcpyAsync(cyc, dEngPhase, ENGINE_PHASES * sizeof(long long),
+                               cudaMemcpyDeviceToHost, stream));
     SMC_CUDA(cudaStreamSynchronize(stream));
     if (phases)
       for (int q = 0; q < ENGINE_PHASES; ++q)
@@ -929,13 +973,14 @@ struct Model {
       io.phase_cycles = dEngPhase;
     }
     fgmres_refine_engine(ctx, op32, op64, io, rf);
-    int res[3];
-    double rel = 0.0;
-    long long cyc[ENGINE_PHASES];
-    SMC_CUDA(cudaMemcpyAsync(res, eio.result, sizeof(res), cudaMemcpyDeviceToHost, stream));
-    SMC_CUDA(cudaMemcpyAsync(&rel, dEngRes, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    int* res = reinterpret_cast<int*>(hpin);                     // pinned: no staged copies
+    long long* cyc = reinterpret_cast<long long*>(hpin + 64);
+    double* relp = reinterpret_cast<double*>(hpin + 512);
+    SMC_CUDA(cudaMemcpyAsync(res, eio.result, 3 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    SMC_CUDA(cudaMemcpyAsync(relp, dEngRes, sizeof(double), cudaMemcpyDeviceToHost, stream));
     if (phases)
-      SMC_CUDA(cudaMemcpyAsync(cyc, dEngPhase, sizeof(cyc), cudaMemcpyDeviceToHost, stream));
+      SMC_CUDA(cudaMemcpyAsync(cyc, dEngPhase, ENGINE_PHASES * sizeof(long long),
+                               cudaMemcpyDeviceToHost, stream));
     SMC_CUDA(cudaStreamSynchronize(stream));
     if (phases)       // the refinement slots count outer passes
       for (int q = 0; q < ENGINE_PHASES; ++q)
@@ -945,7 +990,7 @@ struct Model {
     fr.info = res[0];
     fr.iters = res[1];
     n_outer += res[2];
-    if (true_res) *true_res = rel;
+    if (true_res) *true_res = *relp;
     // inner solves plus one FP64 operator application per outer pass
     ps.work = engine_bytes(kind, true, fr.iters, io.restart) +
               res[2] * 2.0 * engine_bytes(kind, true, 1, io.restart);
@@ -1048,6 +1093,7 @@ struct Model {
   // Md (dense blocks, for the Schur assembly) and the pseudo-spectral eta
   // grid from the current dEta: eta_c = coeffs(eta)
   void eta_operator() {
+    ProfScope ps(ctx, "eta_operator");
     analyze(dEta, Nx, dEtaC, sp[2]);
     md_stale = true;
     if (dMd && (!fast || use_dense_mult)) md_current();
@@ -1215,16 +1261,18 @@ struct Model {
   int bfbt_age = 1 << 30;
   long long n_bfbt_builds = 0;
   void bfbt_build() {
+    ProfScope psp(ctx, "bfbt_profile");
     harm_profile_rhs(ctx, dEta, Nx, N, dwq, dBfbtHw);
     to_complex(dBfbtHw, dBfbtRhs, N);
     ZJob j; j.Z = dVT; j.X = dBfbtRhs; j.Y = dBfbtProfC;     // V^T (w g)
     zmat_apply(ctx, &j, 1, 1, N, dkx);
-    lu_small_solve(ctx, dMpLU, dMpPiv, NN, dBfbtProfC, dBfbtRhs, N, 1, 1.0, 0, nullptr);
+    if (fast) kgemv(ctx, dMpInv, dBfbtProfC, dBfbtRhs, 1, N, 1.0);
+    else lu_small_solve(ctx, dMpLU, dMpPiv, NN, dBfbtProfC, dBfbtRhs, N, 1, 1.0, 0, nullptr);
     if (fast) {
-      bfbt_prof_new.resize(2 * N);
-      SMC_CUDA(cudaMemcpyAsync(bfbt_prof_new.data(), dBfbtRhs, N * sizeof(double2),
-                               cudaMemcpyDeviceToHost, stream));
+      double* hp = reinterpret_cast<double*>(hpin + 1024);      // pinned
+      SMC_CUDA(cudaMemcpyAsync(hp, dBfbtRhs, N * sizeof(double2), cudaMemcpyDeviceToHost, stream));
       SMC_CUDA(cudaStreamSynchronize(stream));
+      bfbt_prof_new.assign(hp, hp + 2 * N);
       bool reuse = !bfbt_prof_h.empty() && bfbt_age < 16;
       if (reuse) {
         double mx = 0.0, md = 0.0;
@@ -1427,6 +1475,7 @@ struct Model {
 
   double cfl_dt(const double2* th, double safety, double dtmax, double dtmin) {
     stokes(th, dPsi, dOm);
+    ProfScope ps(ctx, "cfl_velocity");
     velocity(dPsi, gr[0], gr[1]);
     reduce_maxabs2(ctx, gr[0], gr[1], (long long)Nx * N, dScal, dRed);
     sync_read(dScal, 1);
@@ -1723,6 +1772,7 @@ struct Model {
   ~Model() {
     if (stream) { cudaStreamSynchronize(stream); cudaStreamDestroy(stream); }
     if (hbuf) cudaFreeHost(hbuf);
+    if (hpin) cudaFreeHost(hpin);
   }
 };
 
@@ -1937,8 +1987,10 @@ int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety,
 
 int smc_profile(smc_handle* h, int enable) {
   SMC_GUARD(h, {
+    if (enable < 0 || enable > 2) throw std::runtime_error("smc_profile: enable must be 0, 1 or 2");
     h->m.prof.reset();
     h->m.prof.enabled = enable != 0;
+    h->m.prof.engine_only = enable == 2;
   })
 }
 

@@ -323,16 +323,26 @@ __global__ void smc_eta_law_kernel(const double* __restrict__ th, const double* 
   }
 }
 
+// one warp: lanes stride over the per-CTA partials (maxima, and counts that
+// are exact in any summation order)
 __global__ void smc_eta_stats_final_kernel(const double* part, int np, double* dst) {
-  if (threadIdx.x != 0) return;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) return;
   double a0 = -INFINITY, a1 = -INFINITY, a[4] = {0, 0, 0, 0};
-  for (int b = 0; b < np; ++b) {
+  for (int b = lane; b < np; b += 32) {
     const double* o = part + 6LL * b;
     a0 = fmax(a0, o[0]); a1 = fmax(a1, o[1]);
     for (int t = 0; t < 4; ++t) a[t] += o[2 + t];
   }
-  dst[0] = -a0; dst[1] = a1;
-  for (int t = 0; t < 4; ++t) dst[2 + t] = a[t];
+  for (int d = 16; d > 0; d >>= 1) {
+    a0 = fmax(a0, __shfl_xor_sync(0xffffffffu, a0, d));
+    a1 = fmax(a1, __shfl_xor_sync(0xffffffffu, a1, d));
+    for (int t = 0; t < 4; ++t) a[t] += __shfl_xor_sync(0xffffffffu, a[t], d);
+  }
+  if (lane == 0) {
+    dst[0] = -a0; dst[1] = a1;
+    for (int t = 0; t < 4; ++t) dst[2 + t] = a[t];
+  }
 }
 
 void eta_law(const Ctx& c, const double* th, const double* z, int N, long long npts,
@@ -434,18 +444,27 @@ __global__ void smc_min_drift_kernel(const double* __restrict__ eta, const doubl
   }
 }
 
+// one warp: min and max over the per-CTA partials, NaN if any partial is NaN
 __global__ void smc_min_drift_final_kernel(const double* part, int np, double* dst) {
-  if (threadIdx.x != 0) return;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) return;
   double a = INFINITY, b = 0.0;
   bool nan_seen = false;
-  for (int i = 0; i < np; ++i) {
+  for (int i = lane; i < np; i += 32) {
     double x = part[2 * i], y = part[2 * i + 1];
     if (x != x || y != y) nan_seen = true;
     a = fmin(a, x);
     b = fmax(b, y);
   }
-  dst[0] = nan_seen ? NAN : a;
-  dst[1] = nan_seen ? NAN : b;
+  for (int d = 16; d > 0; d >>= 1) {
+    a = fmin(a, __shfl_xor_sync(0xffffffffu, a, d));
+    b = fmax(b, __shfl_xor_sync(0xffffffffu, b, d));
+  }
+  nan_seen = __any_sync(0xffffffffu, nan_seen);
+  if (lane == 0) {
+    dst[0] = nan_seen ? NAN : a;
+    dst[1] = nan_seen ? NAN : b;
+  }
 }
 
 void min_and_drift(const Ctx& c, const double* eta, const double* lag, long long n, double* dst,
@@ -459,19 +478,31 @@ void min_and_drift(const Ctx& c, const double* eta, const double* lag, long long
 }
 
 // harmonic mean over x of the (Nx, N) field: g_j = 1 / mean_i(1/eta[i][j])
+// out_j = w_j / mean_i(1 / eta[i][j]); one CTA per column j: the reciprocals
+// (FP64 divisions, the expensive part) in parallel, then the column sum by
+// one thread in the order i = 0, 1, ..., in chunks of HP_CHUNK.  The sum
+// order is that of a row-by-row reduction over axis 0 whatever the launch
+// shape, and the FP64 divisions are spread over N SMs instead of one.
+static constexpr int HP_CHUNK = 1024;
 __global__ void smc_harm_profile_kernel(const double* __restrict__ eta, int Nx, int N,
                                         const double* __restrict__ wq, double* __restrict__ out) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= N) return;
+  __shared__ double rcp[HP_CHUNK];
+  const int j = blockIdx.x;
   double s = 0.0;
-  for (int i = 0; i < Nx; ++i) s += 1.0 / eta[(long long)i * N + j];
-  double g = 1.0 / (s / Nx);
-  out[j] = wq[j] * g;      // the weighted right-hand side entry w_j g_j
+  for (int base = 0; base < Nx; base += HP_CHUNK) {
+    const int cnt = min(HP_CHUNK, Nx - base);
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) rcp[i] = 1.0 / eta[(long long)(base + i) * N + j];
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int i = 0; i < cnt; ++i) s += rcp[i];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[j] = wq[j] * (1.0 / (s / Nx));
 }
 
 void harm_profile_rhs(const Ctx& c, const double* eta, int Nx, int N, const double* wq,
                       double* out) {
-  smc_harm_profile_kernel<<<ceil_div(N, 128), 128, 0, c.s>>>(eta, Nx, N, wq, out);
+  smc_harm_profile_kernel<<<N, 128, 0, c.s>>>(eta, Nx, N, wq, out);
   SMC_LAUNCH_CHECK(c);
 }
 

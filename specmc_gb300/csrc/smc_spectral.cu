@@ -49,7 +49,10 @@ void zmat_apply(const Ctx& c, const ZJob* jobs, int njobs, int Nk, int N, const 
   if (njobs < 1 || njobs > 4) throw std::runtime_error("zmat_apply: 1..4 jobs");
   ZJobs4 js;
   for (int i = 0; i < njobs; ++i) js.j[i] = jobs[i];
-  dim3 blk(128), grd(ceil_div(N, 128), Nk, njobs);
+  // one warp per 32 output rows: each thread keeps its serial dot product (the
+  // same sum order), and the Nk N rows spread over Nk ceil(N / 32) CTAs
+  // instead of Nk (FP64 latency and the FP64 pipe of an SM bound a CTA)
+  dim3 blk(32), grd(ceil_div(N, 32), Nk, njobs);
   smc_zmat_kernel<<<grd, blk, 0, c.s>>>(js, Nk, N, kx);
   SMC_LAUNCH_CHECK(c);
 }
@@ -65,9 +68,12 @@ __global__ void smc_synth_x_kernel(SynthJobs4 jobs, int Nk, int N, int Ng,
   int i = blockIdx.y;
   if (j >= N || i >= Ng) return;
   double acc = jb.X[j].x;
+  int idx = 0;                           // k i mod Ng, stepped (i < Ng)
   for (int k = 1; k < Nk; ++k) {
+    idx += i;
+    if (idx >= Ng) idx -= Ng;
     double2 x = jb.X[(long long)k * N + j];
-    double2 t = tw[(long long)(k * i) % Ng];
+    double2 t = tw[idx];
     double v = x.x * t.x - x.y * t.y;
     acc += (2 * k == Ng) ? v : 2.0 * v;
   }
@@ -92,9 +98,12 @@ __global__ void smc_analysis_x_kernel(AnaJobs4 jobs, int Nk, int N, int Ng,
   int k = blockIdx.y;
   if (j >= N || k >= Nk) return;
   double sr = 0.0, si = 0.0;
+  int idx = 0;                           // k i mod Ng, stepped (k < Ng)
   for (int i = 0; i < Ng; ++i) {
     double g = jb.g[(long long)i * N + j];
-    double2 t = tw[(long long)(k * i) % Ng];
+    double2 t = tw[idx];
+    idx += k;
+    if (idx >= Ng) idx -= Ng;
     sr += g * t.x;
     si -= g * t.y;
   }
@@ -106,7 +115,7 @@ void analysis_x(const Ctx& c, const AnaJob* jobs, int njobs, int Nk, int N, int 
   if (njobs < 1 || njobs > 4) throw std::runtime_error("analysis_x: 1..4 jobs");
   AnaJobs4 js;
   for (int i = 0; i < njobs; ++i) js.j[i] = jobs[i];
-  dim3 blk(128), grd(ceil_div(N, 128), Nk, njobs);
+  dim3 blk(32), grd(ceil_div(N, 32), Nk, njobs);       // as zmat_apply
   smc_analysis_x_kernel<<<grd, blk, 0, c.s>>>(js, Nk, N, Ng, tw, scale);
   SMC_LAUNCH_CHECK(c);
 }
@@ -292,17 +301,26 @@ __global__ void smc_memo_kernel(const double2* th, const double2* cth, const dou
   }
 }
 
+// one warp: maxima over the per-CTA partials
 __global__ void smc_memo_final_kernel(const double* part, int np, double* dst) {
-  if (threadIdx.x != 0) return;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) return;
   double a = 0.0, b = 0.0, cc = 0.0;
-  for (int i = 0; i < np; ++i) {
+  for (int i = lane; i < np; i += 32) {
     a = fmax(a, part[3 * i]);
     b = fmax(b, part[3 * i + 1]);
     cc = fmax(cc, part[3 * i + 2]);
   }
-  dst[0] = (a == 0.0) ? 1.0 : 0.0;
-  dst[1] = b;
-  dst[2] = cc;
+  for (int d = 16; d > 0; d >>= 1) {
+    a = fmax(a, __shfl_xor_sync(0xffffffffu, a, d));
+    b = fmax(b, __shfl_xor_sync(0xffffffffu, b, d));
+    cc = fmax(cc, __shfl_xor_sync(0xffffffffu, cc, d));
+  }
+  if (lane == 0) {
+    dst[0] = (a == 0.0) ? 1.0 : 0.0;
+    dst[1] = b;
+    dst[2] = cc;
+  }
 }
 
 void memo_compare(const Ctx& c, const double2* that, const double2* cthat, const double2* X,

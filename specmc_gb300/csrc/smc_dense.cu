@@ -250,56 +250,71 @@ __global__ void smc_green_kernel(const double* __restrict__ LU, const int* __res
   for (int p = tid; p < N; p += blockDim.x) Gk[(long long)p * N + q] = xs[p].x;
 }
 
-// The same columns, GREEN_COLS per CTA, one thread per column: each thread
-// runs the row permutation and the two substitutions of lu_real_solve_smem on
-// its own column (the same operations in the same order, hence the same
-// values) without any barrier; all lanes read the same LU entry at a time
-// (a broadcast).  The per-column CTAs above wait at 2N barriers per column.
+// The same columns, GREEN_COLS per 128-thread CTA and ZSPLIT lanes per
+// column: lane s of a column's group updates the rows r = s (mod 4) at every
+// substitution step, and the warp (8 groups) meets at __syncwarp before the
+// next step reads the finished entry.  Every entry receives the updates of
+// lu_real_solve_smem in the same order (the same values); the FP64 work
+// spreads over 4x more warps than one thread per column, and no CTA-wide
+// barrier is needed (the per-column CTAs above wait at 2N of them).
 static constexpr int GREEN_COLS = 32;
-static constexpr int GREEN_COLS_MAXN = 160;      // N x 32 doubles of shared memory <= 40 KB
-__global__ void __launch_bounds__(GREEN_COLS) smc_green_cols_kernel(const double* __restrict__ LU,
-                                                                   const int* __restrict__ piv,
-                                                                   double* __restrict__ G, int N) {
-  extern __shared__ double xcol[];       // row r of lane l's column at xcol[r * GREEN_COLS + l]
-  const int k = blockIdx.x, lane = threadIdx.x;
-  const int q = blockIdx.y * GREEN_COLS + lane;
-  if (q >= N) return;
-  double* Gk = G + (long long)k * N * N;
-  if (q >= N - 2) {
-    for (int p = 0; p < N; ++p) Gk[(long long)p * N + q] = 0.0;
-    return;
-  }
+static constexpr int GREEN_LD = GREEN_COLS + 1;       // padded row of the column block
+static constexpr int GREEN_COLS_MAXN = 160;           // N x 33 doubles of shared memory <= 42 KB
+__global__ void __launch_bounds__(GREEN_COLS * ZSPLIT) smc_green_cols_kernel(const double* __restrict__ LU,
+                                                                            const int* __restrict__ piv,
+                                                                            double* __restrict__ G, int N) {
+  extern __shared__ double xcol[];       // row r of column cc at xcol[r * GREEN_LD + cc]
+  const int k = blockIdx.x;
+  const int cc = threadIdx.x / ZSPLIT, sub = threadIdx.x % ZSPLIT;
+  const int q = blockIdx.y * GREEN_COLS + cc;
+  const bool act = q < N - 2;            // the tau columns (and columns past N) are not solved
   const double* L = LU + (long long)k * N * N;
   const int* pv = piv + (long long)k * N;
-  double* x = xcol + lane;
-  for (int i = 0; i < N; ++i) x[i * GREEN_COLS] = (i == q) ? 1.0 : 0.0;
-  for (int i = 0; i < N; ++i) {
-    const int p = pv[i];
-    if (p != i) {
-      const double t = x[i * GREEN_COLS];
-      x[i * GREEN_COLS] = x[p * GREEN_COLS];
-      x[p * GREEN_COLS] = t;
+  double* x = xcol + cc;
+  // every lane runs every step loop (the __syncwarp calls need the whole warp)
+  if (act)
+    for (int i = sub; i < N; i += ZSPLIT) x[i * GREEN_LD] = (i == q) ? 1.0 : 0.0;
+  __syncwarp();
+  if (act && sub == 0)
+    for (int i = 0; i < N; ++i) {
+      const int p = pv[i];
+      if (p != i) {
+        const double t = x[i * GREEN_LD];
+        x[i * GREEN_LD] = x[p * GREEN_LD];
+        x[p * GREEN_LD] = t;
+      }
     }
-  }
+  __syncwarp();
   for (int c = 0; c < N; ++c) {          // unit lower
-    const double xc = x[c * GREEN_COLS];
-    const double* Lc = L + (long long)c * N;
-    for (int r = c + 1; r < N; ++r) x[r * GREEN_COLS] -= Lc[r] * xc;
+    if (act) {
+      const double xc = x[c * GREEN_LD];
+      const double* Lc = L + (long long)c * N;
+      for (int r = c + 1 + ((sub - c - 1) & (ZSPLIT - 1)); r < N; r += ZSPLIT)
+        x[r * GREEN_LD] -= Lc[r] * xc;
+    }
+    __syncwarp();
   }
   for (int c = N - 1; c >= 0; --c) {     // upper
     const double* Lc = L + (long long)c * N;
-    x[c * GREEN_COLS] /= Lc[c];
-    const double xc = x[c * GREEN_COLS];
-    for (int r = 0; r < c; ++r) x[r * GREEN_COLS] -= Lc[r] * xc;
+    if (act && sub == (c & (ZSPLIT - 1))) x[c * GREEN_LD] /= Lc[c];
+    __syncwarp();
+    if (act) {
+      const double xc = x[c * GREEN_LD];
+      for (int r = sub; r < c; r += ZSPLIT) x[r * GREEN_LD] -= Lc[r] * xc;
+    }
+    __syncwarp();
   }
-  for (int p = 0; p < N; ++p) Gk[(long long)p * N + q] = x[p * GREEN_COLS];
+  if (q < N) {
+    double* Gk = G + (long long)k * N * N;
+    for (int p = sub; p < N; p += ZSPLIT) Gk[(long long)p * N + q] = act ? x[p * GREEN_LD] : 0.0;
+  }
 }
 
 void green_from_lu(const Ctx& c, const double* LUcm, const int* piv, double* G, int N, int Nk) {
   if (N <= GREEN_COLS_MAXN) {
     dim3 grd(Nk, (N + GREEN_COLS - 1) / GREEN_COLS);
-    smc_green_cols_kernel<<<grd, GREEN_COLS, (size_t)N * GREEN_COLS * sizeof(double), c.s>>>(LUcm, piv,
-                                                                                         G, N);
+    smc_green_cols_kernel<<<grd, GREEN_COLS * ZSPLIT, (size_t)N * GREEN_LD * sizeof(double), c.s>>>(
+        LUcm, piv, G, N);
   } else {
     dim3 grd(Nk, N);
     smc_green_kernel<<<grd, 128, N * sizeof(double2), c.s>>>(LUcm, piv, G, N);

@@ -354,16 +354,49 @@ __device__ void ph_schur_x(const EngineOps& op, unsigned char* smraw, const EngC
   using C = typename CT2<T>::type;
   const int Nk = op.Nk, Mz = op.Mz, L = op.L;
   const int logL = ilog2_pow2(L);
-  const int gsz = blockDim.x / 4, grp = e.tid / gsz, gt = e.tid % gsz;
   C* W = reinterpret_cast<C*>(smraw);           // L/2 twiddles
-  C* P = W + (L >> 1) + grp * L;                 // this group's row
   const C* tw = (const C*)op.twS;
   const T* E = (const T*)op.E;
   const C* Fv = (const C*)op.Fv;
   C* Hv = (C*)op.Hv;
   for (int t = e.tid; t < (L >> 1); t += blockDim.x) W[t] = tw[t];
-  const T sgn = (grp == 3) ? (T)1 : (T)-1;
   const T invL = (T)1 / (T)L;
+  if (schur_x_by_warp(L, (int)sizeof(C))) {
+    // warp w: field w % 4 of the z-points b + (w / 4) G, b + (w / 4 + 2) G, ...
+    __syncthreads();
+    const int grp = e.warp & 3, nzs = ENG_WARPS / 4;
+    C* P = W + (L >> 1) + e.warp * L;            // this warp's row
+    const T sgn = (grp == 3) ? (T)1 : (T)-1;
+    for (int s = e.b + (e.warp >> 2) * e.G; s < Mz; s += nzs * e.G) {
+      for (int i = e.lane; i < L; i += 32) { P[i].x = (T)0; P[i].y = (T)0; }
+      __syncwarp();
+      for (int j = e.lane; j < Nk; j += 32) {
+        const C f = Fv[((long long)grp * Nk + j) * Mz + s];
+        P[j] = f;
+        if (j > 0) { P[L - j].x = sgn * f.x; P[L - j].y = sgn * f.y; }
+      }
+      __syncwarp();
+      warp_fft(P, L, logL, W, +1, e.lane);
+      for (int l = e.lane; l < L; l += 32) {
+        const T ev = E[(long long)l * Mz + s];
+        P[l].x *= ev;
+        P[l].y *= ev;
+      }
+      __syncwarp();
+      warp_fft(P, L, logL, W, -1, e.lane);
+      for (int i = e.lane; i < Nk; i += 32) {
+        C o;
+        o.x = P[i].x * invL;
+        o.y = P[i].y * invL;
+        Hv[((long long)grp * Nk + i) * Mz + s] = o;
+      }
+      __syncwarp();                              // the row is reused for the next z-point
+    }
+    return;
+  }
+  const int gsz = blockDim.x / 4, grp = e.tid / gsz, gt = e.tid % gsz;
+  C* P = W + (L >> 1) + grp * L;                 // this group's row
+  const T sgn = (grp == 3) ? (T)1 : (T)-1;
   for (int s = e.b; s < Mz; s += e.G) {
     __syncthreads();
     for (int i = gt; i < L; i += gsz) { P[i].x = (T)0; P[i].y = (T)0; }
@@ -1166,7 +1199,8 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_engine_kernel(Engin
 template <class T>
 static size_t engine_smem(const EngineOps& op) {
   using C = Cx<T>;
-  const size_t a = (size_t)(op.L / 2 + 4 * op.L) * sizeof(C);                       // Schur x
+  const size_t a = (size_t)(op.L / 2 + (schur_x_by_warp(op.L, (int)sizeof(C)) ? 8 : 4) * op.L) *
+                   sizeof(C);                                                         // Schur x
   const size_t b = (size_t)(2 * op.Nk + op.Np) * sizeof(C) + op.Np * sizeof(T);     // theta x
   const size_t rows = eng_rows_bytes<T>(op.N, op.kind == 0 ? op.Mz : 0);
   size_t s = rows;

@@ -168,6 +168,16 @@ __device__ __forceinline__ double2 kfactor_eval(const KFactor& f, double kx) {
 // ============================================================ spectral ops
 // Y_b[k][n] (=|+=) f_b(k) * sum_m Z_b[n][m] X_b[k][m]   (Z real N x N;
 // per-k operator when zstride > 0).  Up to 4 jobs per launch.
+// Sums split over ZSPLIT consecutive lanes (FP64 contractions, see
+// smc_zmat_kernel): the lane partials p0..p3 combined as (p0 + p1) + (p2 + p3),
+// the same value in every lane of the group
+constexpr int ZSPLIT = 4;
+__device__ __forceinline__ double split4_sum(double v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  return v;
+}
+
 struct ZJob {
   const double* Z = nullptr;
   long long zstride = 0;

@@ -16,28 +16,43 @@ struct SynthJobs4 { SynthJob j[4]; };
 struct AnaJobs4 { AnaJob j[4]; };
 
 // ------------------------------------------------------------ z contraction
-__global__ void smc_zmat_kernel(ZJobs4 jobs, int Nk, int N, const double* __restrict__ kx) {
+// GB300's FP64 pipe issues a warp-wide FMA over many cycles, so a
+// contraction is bound by how many SM sub-partitions carry FP64 work: each
+// output is summed by ZSPLIT consecutive lanes (lane s takes m = s, s + 4, ...)
+// and combined as (p0 + p1) + (p2 + p3), a fixed order, which puts 4x more
+// warps on the GPU than one thread per output.
+static constexpr int ZOUT = 32;          // outputs per 128-thread CTA
+
+__global__ void __launch_bounds__(ZSPLIT * ZOUT) smc_zmat_kernel(ZJobs4 jobs, int Nk, int N,
+                                                                 const double* __restrict__ kx) {
   const ZJob& jb = jobs.j[blockIdx.z];
-  int n = blockIdx.x * blockDim.x + threadIdx.x;
-  int k = blockIdx.y;
-  if (n >= N || k >= Nk) return;
+  const int sub = threadIdx.x & (ZSPLIT - 1);
+  const int n = blockIdx.x * ZOUT + threadIdx.x / ZSPLIT;
+  const int k = blockIdx.y;
+  const bool act = n < N && k < Nk;
+  const bool tau = act && jb.zero_tau && n >= N - 2;
+  double sr = 0.0, si = 0.0;
+  if (act && !tau) {
+    const double* Zr = jb.Z + (long long)k * jb.zstride + (long long)n * N;
+    const double2* xr = jb.X + (long long)k * N;
+    if (jb.x_real) {
+      for (int m = sub; m < N; m += ZSPLIT) sr += Zr[m] * xr[m].x;
+    } else {
+      for (int m = sub; m < N; m += ZSPLIT) {
+        double z = Zr[m];
+        double2 x = xr[m];
+        sr += z * x.x;
+        si += z * x.y;
+      }
+    }
+  }
+  sr = split4_sum(sr);
+  si = split4_sum(si);
+  if (!act || sub != 0) return;
   double2* yp = jb.Y + (long long)k * N + n;
-  if (jb.zero_tau && n >= N - 2) {
+  if (tau) {
     if (!jb.accumulate) *yp = make_double2(0.0, 0.0);
     return;
-  }
-  const double* Zr = jb.Z + (long long)k * jb.zstride + (long long)n * N;
-  const double2* xr = jb.X + (long long)k * N;
-  double sr = 0.0, si = 0.0;
-  if (jb.x_real) {
-    for (int m = 0; m < N; ++m) sr += Zr[m] * xr[m].x;
-  } else {
-    for (int m = 0; m < N; ++m) {
-      double z = Zr[m];
-      double2 x = xr[m];
-      sr += z * x.x;
-      si += z * x.y;
-    }
   }
   double2 f = kfactor_eval(jb.f, kx ? kx[k] : 0.0);
   double2 r = make_double2(f.x * sr - f.y * si, f.x * si + f.y * sr);
@@ -49,10 +64,7 @@ void zmat_apply(const Ctx& c, const ZJob* jobs, int njobs, int Nk, int N, const 
   if (njobs < 1 || njobs > 4) throw std::runtime_error("zmat_apply: 1..4 jobs");
   ZJobs4 js;
   for (int i = 0; i < njobs; ++i) js.j[i] = jobs[i];
-  // one warp per 32 output rows: each thread keeps its serial dot product (the
-  // same sum order), and the Nk N rows spread over Nk ceil(N / 32) CTAs
-  // instead of Nk (FP64 latency and the FP64 pipe of an SM bound a CTA)
-  dim3 blk(32), grd(ceil_div(N, 32), Nk, njobs);
+  dim3 blk(ZSPLIT * ZOUT), grd(ceil_div(N, ZOUT), Nk, njobs);
   smc_zmat_kernel<<<grd, blk, 0, c.s>>>(js, Nk, N, kx);
   SMC_LAUNCH_CHECK(c);
 }
@@ -91,23 +103,31 @@ void synth_x(const Ctx& c, const SynthJob* jobs, int njobs, int Nk, int N, int N
 }
 
 // ------------------------------------------------------------- x analysis
-__global__ void smc_analysis_x_kernel(AnaJobs4 jobs, int Nk, int N, int Ng,
-                                      const double2* __restrict__ tw, double scale) {
+__global__ void __launch_bounds__(ZSPLIT * ZOUT) smc_analysis_x_kernel(AnaJobs4 jobs, int Nk, int N, int Ng,
+                                                                       const double2* __restrict__ tw,
+                                                                       double scale) {
   const AnaJob& jb = jobs.j[blockIdx.z];
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int k = blockIdx.y;
-  if (j >= N || k >= Nk) return;
+  const int sub = threadIdx.x & (ZSPLIT - 1);
+  const int j = blockIdx.x * ZOUT + threadIdx.x / ZSPLIT;
+  const int k = blockIdx.y;
+  const bool act = j < N && k < Nk;
   double sr = 0.0, si = 0.0;
-  int idx = 0;                           // k i mod Ng, stepped (k < Ng)
-  for (int i = 0; i < Ng; ++i) {
-    double g = jb.g[(long long)i * N + j];
-    double2 t = tw[idx];
-    idx += k;
-    if (idx >= Ng) idx -= Ng;
-    sr += g * t.x;
-    si -= g * t.y;
+  if (act) {
+    // lane sub takes i = sub, sub + 4, ...: twiddle index k i mod Ng, stepped
+    int idx = (int)(((long long)k * sub) % Ng);
+    const int step = (int)(((long long)k * ZSPLIT) % Ng);
+    for (int i = sub; i < Ng; i += ZSPLIT) {
+      double g = jb.g[(long long)i * N + j];
+      double2 t = tw[idx];
+      idx += step;
+      if (idx >= Ng) idx -= Ng;
+      sr += g * t.x;
+      si -= g * t.y;
+    }
   }
-  jb.A[(long long)k * N + j] = make_double2(sr * scale, si * scale);
+  sr = split4_sum(sr);
+  si = split4_sum(si);
+  if (act && sub == 0) jb.A[(long long)k * N + j] = make_double2(sr * scale, si * scale);
 }
 
 void analysis_x(const Ctx& c, const AnaJob* jobs, int njobs, int Nk, int N, int Ng,
@@ -115,7 +135,7 @@ void analysis_x(const Ctx& c, const AnaJob* jobs, int njobs, int Nk, int N, int 
   if (njobs < 1 || njobs > 4) throw std::runtime_error("analysis_x: 1..4 jobs");
   AnaJobs4 js;
   for (int i = 0; i < njobs; ++i) js.j[i] = jobs[i];
-  dim3 blk(32), grd(ceil_div(N, 32), Nk, njobs);       // as zmat_apply
+  dim3 blk(ZSPLIT * ZOUT), grd(ceil_div(N, ZOUT), Nk, njobs);
   smc_analysis_x_kernel<<<grd, blk, 0, c.s>>>(js, Nk, N, Ng, tw, scale);
   SMC_LAUNCH_CHECK(c);
 }

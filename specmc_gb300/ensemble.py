@@ -57,7 +57,18 @@ def device_sms(device=0):
     return int(torch.cuda.get_device_properties(device).multi_processor_count)
 
 
-def _march_one(run, nsteps, form, device, cap, safety, dtmax, chunk, max_wall):
+def _build(cfg, form, device, overrides):
+    """api.build_model, with constructor keywords of the model replaced by
+    ``overrides`` (e.g. tighter solver tolerances) when given."""
+    if not overrides:
+        return api.build_model(cfg, form=form, device=device)
+    spec = api.model_spec(cfg)
+    kw = dict(spec["kwargs"])
+    kw.update(overrides)
+    return api.MODEL_MODULES[spec["model"]].build(**kw, form=form, device=device)
+
+
+def _march_one(run, nsteps, form, device, cap, safety, dtmax, chunk, max_wall, overrides=None):
     """One run: CFL-limited steps in chunks of ``chunk``; after each chunk the
     state is checked.  The run is flagged when max|theta| on the grid exceeds
     AMP_LIMIT x its initial value (the reference driver's abort threshold,
@@ -65,7 +76,7 @@ def _march_one(run, nsteps, form, device, cap, safety, dtmax, chunk, max_wall):
     reports it), and it stops, flagged, when the state is non-finite, the
     march stalls, or it has used ``max_wall`` seconds."""
     t0 = time.perf_counter()
-    model = api.build_model(run["cfg"], form=form, device=device)
+    model = _build(run["cfg"], form, device, overrides)
     try:
         lib, h = model._lib, model._h
         if cap > 0:
@@ -104,7 +115,8 @@ def _march_one(run, nsteps, form, device, cap, safety, dtmax, chunk, max_wall):
 
 
 def march_ensemble(runs, nsteps=100, form="mixed", concurrency=8, safety=None, dtmax=None,
-                   device=0, engine_ctas=None, chunk=5, max_wall=None, on_done=None):
+                   device=0, engine_ctas=None, chunk=5, max_wall=None, on_done=None,
+                   overrides=None):
     """March every run of ``runs`` for ``nsteps`` CFL-limited steps, up to
     ``concurrency`` at a time.  Returns one result dict per run (steps, t,
     build and march seconds, final state, diagnostics, status and flag,
@@ -112,7 +124,8 @@ def march_ensemble(runs, nsteps=100, form="mixed", concurrency=8, safety=None, d
 
     ``engine_ctas`` caps each handle's Krylov engine; the default gives each
     concurrent run an equal share of two CTAs per SM.  ``on_done(i, result)``
-    is called as each run finishes."""
+    is called as each run finishes.  ``overrides``: model constructor keywords
+    to replace for every run (e.g. ``stokes_rtol``, ``theta_rtol``)."""
     safety = NUM.CFL_SAFETY if safety is None else float(safety)
     dtmax = NUM.DTMAX if dtmax is None else float(dtmax)
     concurrency = max(1, int(concurrency))
@@ -122,7 +135,7 @@ def march_ensemble(runs, nsteps=100, form="mixed", concurrency=8, safety=None, d
 
     def work(i):
         out[i] = _march_one(runs[i], nsteps, form, device, int(engine_ctas), safety, dtmax,
-                            chunk, max_wall)
+                            chunk, max_wall, overrides)
         if on_done is not None:
             on_done(i, out[i])
 

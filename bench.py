@@ -214,7 +214,8 @@ def run_ours(args, rank, world):
                 b.record(stream)
             evs.append((a, b))
         torch.cuda.synchronize()
-        ms_total = sum(a.elapsed_time(b) for a, b in evs)
+        step_ms = sorted(a.elapsed_time(b) for a, b in evs)
+        ms_total = sum(step_ms)
         launches = m.counters()["n_kernel_launches"] - c0
         prof = []
         if profile:
@@ -235,7 +236,8 @@ def run_ours(args, rank, world):
             t = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             ms_total = float(t.item())
-        return dict(ms=ms_total, launches=launches, prof=prof, diag=diag, m=m, th0=th0)
+        return dict(ms=ms_total, launches=launches, prof=prof, diag=diag, m=m, th0=th0,
+                    step_ms=step_ms)
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -307,6 +309,10 @@ def run_ours(args, rank, world):
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": M["ms"] / args.steps,
+        # spread of the timed steps (the step is launch-bound, so load on the
+        # shared host cores shows here first)
+        "step_ms": {"min": M["step_ms"][0], "median": M["step_ms"][len(M["step_ms"]) // 2],
+                    "max": M["step_ms"][-1]},
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded conductive perturbation, random-free)",
         "config": dict(workload="eta_T 64x96 Ra=1e4 deta_T=1e3, 200-step adaptive march",

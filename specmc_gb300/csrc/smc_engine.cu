@@ -130,7 +130,7 @@ struct EngSmem {
   C* v;       // N   row being formed (basis row / epilogue input)
   C* w;       // N   epilogue outputs / updated rows of the task
   C* z;       // N   preconditioned row (contraction input)
-  C* aux;     // max(3 Mz, N) epilogue vectors
+  C* aux;     // max(4 Mz, N) epilogue vectors
   C* out;     // 4 RCH GEMV results
   void* red;  // warp partials
 };
@@ -142,13 +142,15 @@ __host__ __device__ inline size_t eng_red_bytes() {
   using C = Cx<T>;
   const size_t a = (size_t)ENG_WARPS * 4 * RCH * sizeof(C);      // 4-matrix GEMV partials
   const size_t b = (size_t)ENG_WARPS * RCH * 16;                  // double-float / FP64 partials
-  return a > b ? a : b;
+  const size_t c = (size_t)ENG_WARPS * RCH * 48;                  // mixed z-contraction (T = float)
+  const size_t m = a > b ? a : b;
+  return m > c ? m : c;
 }
 
 template <class T>
 __host__ __device__ inline size_t eng_rows_bytes(int N, int Mz) {
   using C = Cx<T>;
-  const size_t aux = (size_t)(3 * Mz > N ? 3 * Mz : N);
+  const size_t aux = (size_t)(4 * Mz > N ? 4 * Mz : N);
   return eng_align((size_t)N * sizeof(C)) * 3 + eng_align(aux * sizeof(C)) +
          eng_align(4 * RCH * sizeof(C)) + eng_align(eng_red_bytes<T>());
 }
@@ -158,7 +160,7 @@ __device__ EngSmem<T> eng_carve(unsigned char* base, int N, int Mz) {
   using C = Cx<T>;
   EngSmem<T> S;
   size_t o = 0;
-  const int aux = 3 * Mz > N ? 3 * Mz : N;
+  const int aux = 4 * Mz > N ? 4 * Mz : N;
   S.v = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
   S.w = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
   S.z = reinterpret_cast<C*>(base + o); o += eng_align((size_t)N * sizeof(C));
@@ -580,6 +582,133 @@ __device__ void precond_row<float>(const EngineOps& op, const EngineIO& io, int 
   }
 }
 
+// The Schur z-contraction of the FP32 engine: out[m][r] = sum_c At[m][c ld +
+// r0 + r] x[c] for m < 4 as tgemv_chunk, with matrices 0 and 1 (Zf, Z1 of
+// this k) as (hi, lo) float pairs summed in double-float arithmetic and
+// matrices 2, 3 in FP32.  Partials: per warp and row, (re s, re c, im s, im c)
+// for m = 0, 1 and (re, im) for m = 2, 3, merged over the warps in a fixed
+// order.  Ends with __syncthreads.
+__device__ void tgemv4_df2(const float2* __restrict__ a0, const float2* __restrict__ a1,
+                           const float* __restrict__ a2, const float* __restrict__ a3, long long ld,
+                           int r0, int nr, int ncol, const float2* x, EngSmem<float>& S,
+                           const EngCtx& e) {
+  float4* red0 = reinterpret_cast<float4*>(S.red);               // [warp][RCH]
+  float4* red1 = red0 + ENG_WARPS * RCH;
+  float2* red2 = reinterpret_cast<float2*>(red1 + ENG_WARPS * RCH);
+  float2* red3 = red2 + ENG_WARPS * RCH;
+  for (int rc = 0; rc < nr; rc += 32) {
+    const int r = rc + e.lane;
+    float s0r = 0.f, c0r = 0.f, s0i = 0.f, c0i = 0.f, s1r = 0.f, c1r = 0.f, s1i = 0.f, c1i = 0.f;
+    float p2r = 0.f, p2i = 0.f, p3r = 0.f, p3i = 0.f;
+    if (r < nr) {
+#pragma unroll 2
+      for (int c = e.warp; c < ncol; c += ENG_WARPS) {
+        const long long o = (long long)c * ld + r0 + r;
+        const float2 xv = x[c];
+        const float2 g0 = a0[o], g1 = a1[o];
+        const float f2 = a2[o], f3 = a3[o];
+        df_mac(s0r, c0r, g0.x, g0.y, xv.x);
+        df_mac(s0i, c0i, g0.x, g0.y, xv.y);
+        df_mac(s1r, c1r, g1.x, g1.y, xv.x);
+        df_mac(s1i, c1i, g1.x, g1.y, xv.y);
+        p2r += f2 * xv.x;
+        p2i += f2 * xv.y;
+        p3r += f3 * xv.x;
+        p3i += f3 * xv.y;
+      }
+    }
+    const int i = e.warp * RCH + r;
+    red0[i] = make_float4(s0r, c0r, s0i, c0i);
+    red1[i] = make_float4(s1r, c1r, s1i, c1i);
+    red2[i] = make_float2(p2r, p2i);
+    red3[i] = make_float2(p3r, p3i);
+  }
+  __syncthreads();
+  for (int idx = e.tid; idx < 4 * nr; idx += blockDim.x) {
+    const int m = idx / nr, r = idx - m * nr;
+    float2 o;
+    if (m < 2) {
+      const float4* rd = m == 0 ? red0 : red1;
+      float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+      for (int w = 0; w < ENG_WARPS; ++w) {
+        const float4 q = rd[w * RCH + r];
+        df_add(sr, cr, q.x);
+        cr += q.y;
+        df_add(si, ci, q.z);
+        ci += q.w;
+      }
+      o = make_float2(sr + cr, si + ci);
+    } else {
+      const float2* rd = m == 2 ? red2 : red3;
+      float sr = 0.f, si = 0.f;
+      for (int w = 0; w < ENG_WARPS; ++w) {
+        const float2 q = rd[w * RCH + r];
+        sr += q.x;
+        si += q.y;
+      }
+      o = make_float2(sr, si);
+    }
+    S.out[m * RCH + r] = o;
+  }
+  __syncthreads();
+}
+
+// The Schur epilogue GEMVs of the FP32 engine: out[0][r] = D2Zi (h0 + h1) in
+// double-float arithmetic (D2Zi as (hi, lo) pairs, h0 and h1 multiplied
+// separately, so their sum is not rounded first), out[1][r] = Zi xb and
+// out[2][r] = DZi xc in FP32.  Ends with __syncthreads.
+__device__ void tgemv3_epi_df(const float2* __restrict__ a0, const float* __restrict__ a1,
+                              const float* __restrict__ a2, long long ld, int r0, int nr, int ncol,
+                              const float2* h0, const float2* h1, const float2* xb,
+                              const float2* xc, EngSmem<float>& S, const EngCtx& e) {
+  float4* red0 = reinterpret_cast<float4*>(S.red);
+  float4* red12 = red0 + ENG_WARPS * RCH;                         // (b re, b im, c re, c im)
+  for (int rc = 0; rc < nr; rc += 32) {
+    const int r = rc + e.lane;
+    float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f, br = 0.f, bi = 0.f, qr = 0.f, qi = 0.f;
+    if (r < nr) {
+#pragma unroll 2
+      for (int c = e.warp; c < ncol; c += ENG_WARPS) {
+        const long long o = (long long)c * ld + r0 + r;
+        const float2 g = a0[o];
+        const float f1 = a1[o], f2 = a2[o];
+        const float2 u = h0[c], v = h1[c], xb_ = xb[c], xc_ = xc[c];
+        df_mac(sr, cr, g.x, g.y, u.x);
+        df_mac(sr, cr, g.x, g.y, v.x);
+        df_mac(si, ci, g.x, g.y, u.y);
+        df_mac(si, ci, g.x, g.y, v.y);
+        br += f1 * xb_.x;
+        bi += f1 * xb_.y;
+        qr += f2 * xc_.x;
+        qi += f2 * xc_.y;
+      }
+    }
+    const int i = e.warp * RCH + r;
+    red0[i] = make_float4(sr, cr, si, ci);
+    red12[i] = make_float4(br, bi, qr, qi);
+  }
+  __syncthreads();
+  for (int r = e.tid; r < nr; r += blockDim.x) {
+    float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f, br = 0.f, bi = 0.f, qr = 0.f, qi = 0.f;
+    for (int w = 0; w < ENG_WARPS; ++w) {
+      const float4 q = red0[w * RCH + r];
+      df_add(sr, cr, q.x);
+      cr += q.y;
+      df_add(si, ci, q.z);
+      ci += q.w;
+      const float4 t = red12[w * RCH + r];
+      br += t.x;
+      bi += t.y;
+      qr += t.z;
+      qi += t.w;
+    }
+    S.out[r] = make_float2(sr + cr, si + ci);
+    S.out[RCH + r] = make_float2(br, bi);
+    S.out[2 * RCH + r] = make_float2(qr, qi);
+  }
+  __syncthreads();
+}
+
 // ------------------------------------------------------------ row phases
 // prep: for each row task (k, sub): the row v_k of a new basis vector
 //   mode 0: v = r * scale                 (start of a cycle; writes V_jv, Z_jv)
@@ -640,7 +769,11 @@ __device__ void phase_prep(const EngineOps& op, const EngineIO& io, int mode, in
       const T c1 = (T)2 * kk * kk;
       for (int s0 = s_lo; s0 < s_hi; s0 += RCH) {
         const int nr = min(RCH, s_hi - s0);
-        tgemv_chunk<T, 4>(g, Mz, s0, nr, N, S, e);
+        if constexpr (std::is_same<T, float>::value)
+          tgemv4_df2((const float2*)op.ZfT2, (const float2*)op.Z1T2 + (long long)k * MN, g.a[2], g.a[3],
+                     Mz, s0, nr, N, S.z, S, e);
+        else
+          tgemv_chunk<T, 4>(g, Mz, s0, nr, N, S, e);
         for (int r = e.tid; r < nr; r += blockDim.x) {
           const long long base = (long long)k * Mz + s0 + r;
           const C f0 = S.out[r], f1 = S.out[RCH + r], f2 = S.out[2 * RCH + r], f3 = S.out[3 * RCH + r];
@@ -707,11 +840,27 @@ __device__ void phase_post(const EngineOps& op, const EngineIO& io, bool resid, 
       for (int q = e.tid; q < Mz; q += blockDim.x) {
         const long long i0 = (long long)k * Mz + q;
         const C h0 = Hv[i0], h1 = Hv[KM + i0], h2 = Hv[2 * KM + i0], h3 = Hv[3 * KM + i0];
-        S.aux[q] = x_add<T>(h0, h1);
+        if constexpr (std::is_same<T, float>::value) {
+          S.aux[q] = h0;                 // h0 and h1 kept apart: D2Zi (h0 + h1) is summed in double-float
+          S.aux[3 * Mz + q] = h1;
+        } else {
+          S.aux[q] = x_add<T>(h0, h1);
+        }
         S.aux[Mz + q] = mk2<T>((T)2 * k2 * h2.x - k2 * h0.x, (T)2 * k2 * h2.y - k2 * h0.y);
         S.aux[2 * Mz + q] = h3;
       }
       __syncthreads();
+      if constexpr (std::is_same<T, float>::value) {
+        for (int p0 = p_lo; p0 < pe; p0 += RCH) {
+          const int nr = min(RCH, pe - p0);
+          tgemv3_epi_df((const float2*)op.D2ZiT2, (const float*)op.ZiT, (const float*)op.DZiT, N, p0, nr,
+                        Mz, S.aux, S.aux + 3 * Mz, S.aux + Mz, S.aux + 2 * Mz, S, e);
+          for (int r = e.tid; r < nr; r += blockDim.x) {
+            const C a = S.out[r], b = S.out[RCH + r], c = S.out[2 * RCH + r];
+            S.w[p0 - p_lo + r] = mk2<T>(a.x + b.x - (T)4 * kk * c.x, a.y + b.y - (T)4 * kk * c.y);
+          }
+        }
+      } else {
       GemvArgs<T, 3> g;
       g.a[0] = (const T*)op.D2ZiT;
       g.a[1] = (const T*)op.ZiT;
@@ -726,6 +875,7 @@ __device__ void phase_post(const EngineOps& op, const EngineIO& io, bool resid, 
           const C a = S.out[r], b = S.out[RCH + r], c = S.out[2 * RCH + r];
           S.w[p0 - p_lo + r] = mk2<T>(a.x + b.x - (T)4 * kk * c.x, a.y + b.y - (T)4 * kk * c.y);
         }
+      }
       }
     } else {
       const C* A = (const C*)op.A;

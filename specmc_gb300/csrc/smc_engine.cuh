@@ -17,6 +17,13 @@ struct EngineOps {
   const void *ZfT = nullptr, *Z1T = nullptr, *Z2T = nullptr, *Z3T = nullptr;
   const void *D2ZiT = nullptr, *ZiT = nullptr, *DZiT = nullptr;
   const void *E = nullptr, *twS = nullptr;
+  // T = float: Zf, Z1 and D2Zi also as (hi, lo) float pairs, same layouts.  The
+  // eta v and 2 k^2 eta G v fields are differentiated twice by the epilogue,
+  // which amplifies rounding in their point values: those two contractions
+  // and the D2Zi product are summed in double-float arithmetic (FP32 ones
+  // leave the FP32 operator ~1e-1 from the FP64 one in the residual norm,
+  // these ~3e-3, so each refinement pass gains that much more)
+  const void *ZfT2 = nullptr, *Z1T2 = nullptr, *D2ZiT2 = nullptr;
   // temperature operator (T): z-synthesis [q][j], epilogue [m][n], twiddles,
   // frozen velocities on the padded grid
   const void *tVT = nullptr, *tVDT = nullptr, *tD2T = nullptr, *tViT = nullptr, *twT = nullptr;

@@ -357,7 +357,13 @@ struct Model {
     const void *ZfT = nullptr, *Z1T = nullptr, *Z2T = nullptr, *Z3T = nullptr;
     const void *D2ZiT = nullptr, *ZiT = nullptr, *DZiT = nullptr;
     const void *tVT = nullptr, *tVDT = nullptr, *tD2T = nullptr, *tViT = nullptr;
+    const void *ZfT2 = nullptr, *Z1T2 = nullptr, *D2ZiT2 = nullptr;   // (hi, lo) pairs (em32)
   } em32, em64;
+  const float2* dev_transposed_split(const double* in, long long rows, long long cols, int batch) {
+    float2* out = mem.alloc<float2>((size_t)rows * cols * batch);
+    transpose_split(ctx, in, out, rows, cols, batch);
+    return out;
+  }
   template <class To>
   const To* dev_transposed(const double* in, long long rows, long long cols, int batch) {
     To* out = mem.alloc<To>((size_t)rows * cols * batch);
@@ -836,6 +842,9 @@ struct Model {
     em32.D2ZiT = dev_transposed<float>(D2Zi, N, Mz, 1);
     em32.ZiT = dev_transposed<float>(psplan.Zi, N, Mz, 1);
     em32.DZiT = dev_transposed<float>(DZi, N, Mz, 1);
+    em32.ZfT2 = dev_transposed_split(psplan.Zf, Mz, N, 1);
+    em32.Z1T2 = dev_transposed_split(Z1, Mz, N, Nk);
+    em32.D2ZiT2 = dev_transposed_split(D2Zi, N, Mz, 1);
     dE32 = mem.alloc<float>((size_t)L * Mz);
     dFsFv = mem.alloc<double2>((size_t)4 * Nk * Mz);
     dFsHv = mem.alloc<double2>((size_t)4 * Nk * Mz);
@@ -906,6 +915,7 @@ struct Model {
       op.Mz = psplan.Mz; op.L = psplan.L;
       op.ZfT = em.ZfT; op.Z1T = em.Z1T; op.Z2T = em.Z2T; op.Z3T = em.Z3T;
       op.D2ZiT = em.D2ZiT; op.ZiT = em.ZiT; op.DZiT = em.DZiT;
+      op.ZfT2 = em.ZfT2; op.Z1T2 = em.Z1T2; op.D2ZiT2 = em.D2ZiT2;
       if (fp32) { op.E = dE32; op.twS = fs32.tw; }
       else { op.E = dPsE; op.twS = fs64.tw; }
       op.Fv = dFsFv; op.Hv = dFsHv;

@@ -40,7 +40,7 @@ L2_BYTES = 129 * 1024 * 1024
 # captures of this workload (dram__bytes_read.sum + dram__bytes_write.sum,
 # mean over the captured launches); the captures and their commands are
 # summarised in profiles/engine_64x96.md
-DRAM_BYTES_PER_LAUNCH = {"engine_stokes": 25.66e6, "engine_theta": 3.46e6}
+DRAM_BYTES_PER_LAUNCH = {"engine_stokes": 28.38e6, "engine_theta": 3.46e6}
 
 
 def _peaks():

@@ -65,18 +65,33 @@ struct EngCtx {
   {P ".start", P ".xconv", P ".xconv_wait", P ".post", P ".post_wait", P ".update_reduce",      \
    P ".update", P ".update_wait", P ".exact_norm", P ".next_reduce", P ".givens", P ".combine", \
    P ".precond", P ".contract", P ".next_wait", P ".lsq", P ".resid", P ".refine_xupdate",     \
-   P ".refine_contract", P ".refine_xconv", P ".refine_post", P ".refine_norm"}
+   P ".refine_contract", P ".refine_xconv", P ".refine_post", P ".refine_norm", P ".total_cycles", \
+   P ".total_ns"}
 const char* const engine_phase_names[2][ENGINE_PHASES] = {SMC_PHASE_NAMES("engine_stokes"),
                                                           SMC_PHASE_NAMES("engine_theta")};
 #undef SMC_PHASE_NAMES
 
 // phase timer of CTA 0 / thread 0: cycles since the previous mark go to slot
+__device__ __forceinline__ long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return (long long)t;
+}
+
 struct PhaseClock {
   long long* acc;
-  long long last;
+  long long last, c0, ns0;
   __device__ void init(long long* a, const EngCtx& e) {
     acc = (a && e.b == 0 && e.tid == 0) ? a : nullptr;
-    last = clock64();
+    last = c0 = clock64();
+    ns0 = acc ? global_ns() : 0;
+  }
+  // the launch's totals (call once, at the end)
+  __device__ void finish() {
+    if (acc) {
+      acc[EP_TOTAL_CYCLES] += clock64() - c0;
+      acc[EP_TOTAL_NS] += global_ns() - ns0;
+    }
   }
   __device__ void mark(int slot) {
     if (acc) {
@@ -1249,6 +1264,7 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
     io.result[0] = info;
     io.result[1] = total;
   }
+  pc.finish();
 }
 
 // Iterative refinement in one launch: FP64 outer residuals r = b - A64 x
@@ -1344,6 +1360,7 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_engine_kernel(Engin
     io.result[2] = outer;
     rf.res[0] = beta / fmax(bn, 1e-300);
   }
+  pc.finish();
 }
 
 template <class T>

@@ -91,6 +91,10 @@ enum EnginePhase {
   EP_REF_XCONV,  // FP64 x-direction convolution
   EP_REF_POST,   // FP64 epilogue r = b - A x and ||r||^2 partials
   EP_REFINE,     // ||r|| reduction
+  // whole launch as seen by CTA 0: SM cycles and %globaltimer nanoseconds
+  // (their ratio is the SM clock the engine ran at)
+  EP_TOTAL_CYCLES,
+  EP_TOTAL_NS,
   ENGINE_PHASES
 };
 extern const char* const engine_phase_names[2][ENGINE_PHASES];

@@ -953,7 +953,8 @@ struct Model {
     SMC_CUDA(cudaStreamSynchronize(stream));
     if (phases)
       for (int q = 0; q < ENGINE_PHASES; ++q)
-        prof.add(engine_phase_names[kind][q], (double)cyc[q] / sm_khz, 1);
+        prof.add(engine_phase_names[kind][q],
+                 q == EP_TOTAL_NS ? (double)cyc[q] * 1e-6 : (double)cyc[q] / sm_khz, 1);
     FgmresResult fr;
     fr.info = res[0];
     fr.iters = res[1];
@@ -992,10 +993,11 @@ struct Model {
       SMC_CUDA(cudaMemcpyAsync(cyc, dEngPhase, ENGINE_PHASES * sizeof(long long),
                                cudaMemcpyDeviceToHost, stream));
     SMC_CUDA(cudaStreamSynchronize(stream));
-    if (phases)       // the refinement slots count outer passes
+    if (phases)       // the refinement slots count outer passes; total_ns is wall time
       for (int q = 0; q < ENGINE_PHASES; ++q)
-        prof.add(engine_phase_names[kind][q], (double)cyc[q] / sm_khz,
-                 q >= EP_REF_XUPD ? res[2] : 1);
+        prof.add(engine_phase_names[kind][q],
+                 q == EP_TOTAL_NS ? (double)cyc[q] * 1e-6 : (double)cyc[q] / sm_khz,
+                 (q >= EP_REF_XUPD && q <= EP_REFINE) ? res[2] : 1);
     FgmresResult fr;
     fr.info = res[0];
     fr.iters = res[1];

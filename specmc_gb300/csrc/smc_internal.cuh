@@ -168,13 +168,21 @@ __device__ __forceinline__ double2 kfactor_eval(const KFactor& f, double kx) {
 // ============================================================ spectral ops
 // Y_b[k][n] (=|+=) f_b(k) * sum_m Z_b[n][m] X_b[k][m]   (Z real N x N;
 // per-k operator when zstride > 0).  Up to 4 jobs per launch.
-// Sums split over ZSPLIT consecutive lanes (FP64 contractions, see
-// smc_zmat_kernel): the lane partials p0..p3 combined as (p0 + p1) + (p2 + p3),
+// Sums split over consecutive lanes (the FP64 contractions and x-direction
+// DFTs, see smc_zmat_kernel; ZSPLIT lanes per column in the Green-column
+// solves): the lane partials combined pairwise, (p0 + p1) + (p2 + p3) for 4
+// lanes and ((p0 + p1) + (p2 + p3)) + ((p4 + p5) + (p6 + p7)) for CSPLIT = 8,
 // the same value in every lane of the group
 constexpr int ZSPLIT = 4;
+constexpr int CSPLIT = 8;
 __device__ __forceinline__ double split4_sum(double v) {
   v += __shfl_xor_sync(0xffffffffu, v, 1);
   v += __shfl_xor_sync(0xffffffffu, v, 2);
+  return v;
+}
+__device__ __forceinline__ double split8_sum(double v) {
+  v = split4_sum(v);
+  v += __shfl_xor_sync(0xffffffffu, v, 4);
   return v;
 }
 

@@ -24,23 +24,23 @@ namespace smc {
 __global__ void __launch_bounds__(128) smc_ps_zfwd_kernel(PsJobs jobs, const double* __restrict__ Zf,
                                                           int Nk, int N, int Mz,
                                                           double2* __restrict__ Fv) {
-  // ZSPLIT lanes per output (FP64-pipe bound, as smc_zmat_kernel)
-  const int sub = threadIdx.x & (ZSPLIT - 1);
-  const int s = blockIdx.x * (blockDim.x / ZSPLIT) + threadIdx.x / ZSPLIT;
+  // CSPLIT lanes per output (FP64-pipe bound, as smc_zmat_kernel)
+  const int sub = threadIdx.x & (CSPLIT - 1);
+  const int s = blockIdx.x * (blockDim.x / CSPLIT) + threadIdx.x / CSPLIT;
   const int j = blockIdx.y, b = blockIdx.z;
   double sr = 0.0, si = 0.0;
   if (s < Mz) {
     const double2* f = jobs.f[b] + (long long)j * N;
     const double* z = Zf + (long long)s * N;
-    for (int q = sub; q < N; q += ZSPLIT) {
+    for (int q = sub; q < N; q += CSPLIT) {
       double w = z[q];
       double2 v = f[q];
       sr += w * v.x;
       si += w * v.y;
     }
   }
-  sr = split4_sum(sr);
-  si = split4_sum(si);
+  sr = split8_sum(sr);
+  si = split8_sum(si);
   if (s < Mz && sub == 0) Fv[((long long)b * Nk + j) * Mz + s] = make_double2(sr, si);
 }
 
@@ -117,7 +117,7 @@ __global__ void smc_ps_eta_grid_kernel(const double2* __restrict__ Av, int Nk, i
 void ps_eta_grid(const Ctx& c, const PsPlan& pl, const double2* eta_c, double2* work, double* E) {
   PsJobs j{};
   j.f[0] = eta_c;
-  dim3 g1(ceil_div(pl.Mz, 128 / ZSPLIT), pl.Nk, 1);
+  dim3 g1(ceil_div(pl.Mz, 128 / CSPLIT), pl.Nk, 1);
   smc_ps_zfwd_kernel<<<g1, 128, 0, c.s>>>(j, pl.Zf, pl.Nk, pl.N, pl.Mz, work);
   SMC_LAUNCH_CHECK(c);
   dim3 g2(ceil_div(pl.Mz, 128), pl.L);
@@ -127,7 +127,7 @@ void ps_eta_grid(const Ctx& c, const PsPlan& pl, const double2* eta_c, double2* 
 
 void ps_mult_eta(const Ctx& c, const PsPlan& pl, const double* E, const PsJobs& jobs, int nb,
                  double2* Fv, double2* Hv) {
-  dim3 g1(ceil_div(pl.Mz, 128 / ZSPLIT), pl.Nk, nb);
+  dim3 g1(ceil_div(pl.Mz, 128 / CSPLIT), pl.Nk, nb);
   smc_ps_zfwd_kernel<<<g1, 128, 0, c.s>>>(jobs, pl.Zf, pl.Nk, pl.N, pl.Mz, Fv);
   SMC_LAUNCH_CHECK(c);
   dim3 g2(pl.Mz, nb);

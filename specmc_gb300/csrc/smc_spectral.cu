@@ -18,16 +18,17 @@ struct AnaJobs4 { AnaJob j[4]; };
 // ------------------------------------------------------------ z contraction
 // GB300's FP64 pipe issues a warp-wide FMA over many cycles, so a
 // contraction is bound by how many SM sub-partitions carry FP64 work: each
-// output is summed by ZSPLIT consecutive lanes (lane s takes m = s, s + 4, ...)
-// and combined as (p0 + p1) + (p2 + p3), a fixed order, which puts 4x more
-// warps on the GPU than one thread per output.
-static constexpr int ZOUT = 32;          // outputs per 128-thread CTA
+// output is summed by CSPLIT consecutive lanes (lane s takes m = s, s + 8, ...)
+// and combined pairwise in a fixed order (split8_sum), which puts 8x more
+// warps on the GPU than one thread per output and cuts each lane's chain of
+// dependent FP64 FMAs to N / 8.
+static constexpr int ZOUT = 16;          // outputs per 128-thread CTA
 
-__global__ void __launch_bounds__(ZSPLIT * ZOUT) smc_zmat_kernel(ZJobs4 jobs, int Nk, int N,
+__global__ void __launch_bounds__(CSPLIT * ZOUT) smc_zmat_kernel(ZJobs4 jobs, int Nk, int N,
                                                                  const double* __restrict__ kx) {
   const ZJob& jb = jobs.j[blockIdx.z];
-  const int sub = threadIdx.x & (ZSPLIT - 1);
-  const int n = blockIdx.x * ZOUT + threadIdx.x / ZSPLIT;
+  const int sub = threadIdx.x & (CSPLIT - 1);
+  const int n = blockIdx.x * ZOUT + threadIdx.x / CSPLIT;
   const int k = blockIdx.y;
   const bool act = n < N && k < Nk;
   const bool tau = act && jb.zero_tau && n >= N - 2;
@@ -36,9 +37,9 @@ __global__ void __launch_bounds__(ZSPLIT * ZOUT) smc_zmat_kernel(ZJobs4 jobs, in
     const double* Zr = jb.Z + (long long)k * jb.zstride + (long long)n * N;
     const double2* xr = jb.X + (long long)k * N;
     if (jb.x_real) {
-      for (int m = sub; m < N; m += ZSPLIT) sr += Zr[m] * xr[m].x;
+      for (int m = sub; m < N; m += CSPLIT) sr += Zr[m] * xr[m].x;
     } else {
-      for (int m = sub; m < N; m += ZSPLIT) {
+      for (int m = sub; m < N; m += CSPLIT) {
         double z = Zr[m];
         double2 x = xr[m];
         sr += z * x.x;
@@ -46,8 +47,8 @@ __global__ void __launch_bounds__(ZSPLIT * ZOUT) smc_zmat_kernel(ZJobs4 jobs, in
       }
     }
   }
-  sr = split4_sum(sr);
-  si = split4_sum(si);
+  sr = split8_sum(sr);
+  si = split8_sum(si);
   if (!act || sub != 0) return;
   double2* yp = jb.Y + (long long)k * N + n;
   if (tau) {
@@ -64,7 +65,7 @@ void zmat_apply(const Ctx& c, const ZJob* jobs, int njobs, int Nk, int N, const 
   if (njobs < 1 || njobs > 4) throw std::runtime_error("zmat_apply: 1..4 jobs");
   ZJobs4 js;
   for (int i = 0; i < njobs; ++i) js.j[i] = jobs[i];
-  dim3 blk(ZSPLIT * ZOUT), grd(ceil_div(N, ZOUT), Nk, njobs);
+  dim3 blk(CSPLIT * ZOUT), grd(ceil_div(N, ZOUT), Nk, njobs);
   smc_zmat_kernel<<<grd, blk, 0, c.s>>>(js, Nk, N, kx);
   SMC_LAUNCH_CHECK(c);
 }
@@ -73,50 +74,57 @@ void zmat_apply(const Ctx& c, const ZJob* jobs, int njobs, int Nk, int N, const 
 // g[i][j] = Re X[0][j] + sum_{k>=1} w_k Re(X[k][j] e^{2 pi i k i/Ng}),
 // w_k = 2, except the Nyquist mode 2k == Ng (weight 1, Re only) -- the
 // Hermitian reconstruction numpy.fft.irfft performs.
-__global__ void smc_synth_x_kernel(SynthJobs4 jobs, int Nk, int N, int Ng,
-                                   const double2* __restrict__ tw) {
+__global__ void __launch_bounds__(CSPLIT * ZOUT) smc_synth_x_kernel(SynthJobs4 jobs, int Nk, int N, int Ng,
+                                                                    const double2* __restrict__ tw) {
+  // CSPLIT lanes per output (as smc_zmat_kernel): lane sub takes the modes
+  // k = 1 + sub, 1 + sub + 8, ...; the mode-0 term is added to the lane sum
   const SynthJob& jb = jobs.j[blockIdx.z];
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int i = blockIdx.y;
-  if (j >= N || i >= Ng) return;
-  double acc = jb.X[j].x;
-  int idx = 0;                           // k i mod Ng, stepped (i < Ng)
-  for (int k = 1; k < Nk; ++k) {
-    idx += i;
-    if (idx >= Ng) idx -= Ng;
-    double2 x = jb.X[(long long)k * N + j];
-    double2 t = tw[idx];
-    double v = x.x * t.x - x.y * t.y;
-    acc += (2 * k == Ng) ? v : 2.0 * v;
+  const int sub = threadIdx.x & (CSPLIT - 1);
+  const int j = blockIdx.x * ZOUT + threadIdx.x / CSPLIT;
+  const int i = blockIdx.y;
+  const bool act = j < N && i < Ng;
+  double acc = 0.0;
+  if (act) {
+    int idx = (int)(((long long)(1 + sub) * i) % Ng);   // k i mod Ng, stepped by 8 i
+    const int step = (int)(((long long)CSPLIT * i) % Ng);
+    for (int k = 1 + sub; k < Nk; k += CSPLIT) {
+      double2 x = jb.X[(long long)k * N + j];
+      double2 t = tw[idx];
+      idx += step;
+      if (idx >= Ng) idx -= Ng;
+      double v = x.x * t.x - x.y * t.y;
+      acc += (2 * k == Ng) ? v : 2.0 * v;
+    }
   }
-  jb.g[(long long)i * N + j] = acc;
+  acc = split8_sum(acc);
+  if (act && sub == 0) jb.g[(long long)i * N + j] = jb.X[j].x + acc;
 }
 
 void synth_x(const Ctx& c, const SynthJob* jobs, int njobs, int Nk, int N, int Ng,
              const double2* tw) {
   if (njobs < 1 || njobs > 4) throw std::runtime_error("synth_x: 1..4 jobs");
   SynthJobs4 js;
-  for (int i = 0; i < njobs; ++i) js.j[i] = jobs[i];
-  dim3 blk(128), grd(ceil_div(N, 128), Ng, njobs);
+  for (int q = 0; q < njobs; ++q) js.j[q] = jobs[q];
+  dim3 blk(CSPLIT * ZOUT), grd(ceil_div(N, ZOUT), Ng, njobs);
   smc_synth_x_kernel<<<grd, blk, 0, c.s>>>(js, Nk, N, Ng, tw);
   SMC_LAUNCH_CHECK(c);
 }
 
 // ------------------------------------------------------------- x analysis
-__global__ void __launch_bounds__(ZSPLIT * ZOUT) smc_analysis_x_kernel(AnaJobs4 jobs, int Nk, int N, int Ng,
+__global__ void __launch_bounds__(CSPLIT * ZOUT) smc_analysis_x_kernel(AnaJobs4 jobs, int Nk, int N, int Ng,
                                                                        const double2* __restrict__ tw,
                                                                        double scale) {
   const AnaJob& jb = jobs.j[blockIdx.z];
-  const int sub = threadIdx.x & (ZSPLIT - 1);
-  const int j = blockIdx.x * ZOUT + threadIdx.x / ZSPLIT;
+  const int sub = threadIdx.x & (CSPLIT - 1);
+  const int j = blockIdx.x * ZOUT + threadIdx.x / CSPLIT;
   const int k = blockIdx.y;
   const bool act = j < N && k < Nk;
   double sr = 0.0, si = 0.0;
   if (act) {
-    // lane sub takes i = sub, sub + 4, ...: twiddle index k i mod Ng, stepped
+    // lane sub takes i = sub, sub + 8, ...: twiddle index k i mod Ng, stepped
     int idx = (int)(((long long)k * sub) % Ng);
-    const int step = (int)(((long long)k * ZSPLIT) % Ng);
-    for (int i = sub; i < Ng; i += ZSPLIT) {
+    const int step = (int)(((long long)k * CSPLIT) % Ng);
+    for (int i = sub; i < Ng; i += CSPLIT) {
       double g = jb.g[(long long)i * N + j];
       double2 t = tw[idx];
       idx += step;
@@ -125,8 +133,8 @@ __global__ void __launch_bounds__(ZSPLIT * ZOUT) smc_analysis_x_kernel(AnaJobs4 
       si -= g * t.y;
     }
   }
-  sr = split4_sum(sr);
-  si = split4_sum(si);
+  sr = split8_sum(sr);
+  si = split8_sum(si);
   if (act && sub == 0) jb.A[(long long)k * N + j] = make_double2(sr * scale, si * scale);
 }
 
@@ -135,7 +143,7 @@ void analysis_x(const Ctx& c, const AnaJob* jobs, int njobs, int Nk, int N, int 
   if (njobs < 1 || njobs > 4) throw std::runtime_error("analysis_x: 1..4 jobs");
   AnaJobs4 js;
   for (int i = 0; i < njobs; ++i) js.j[i] = jobs[i];
-  dim3 blk(ZSPLIT * ZOUT), grd(ceil_div(N, ZOUT), Nk, njobs);
+  dim3 blk(CSPLIT * ZOUT), grd(ceil_div(N, ZOUT), Nk, njobs);
   smc_analysis_x_kernel<<<grd, blk, 0, c.s>>>(js, Nk, N, Ng, tw, scale);
   SMC_LAUNCH_CHECK(c);
 }

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define SMC_ABI_VERSION 1
+#define SMC_ABI_VERSION 2
 
 enum smc_model { SMC_MODEL_CONST = 0, SMC_MODEL_ETA_Z = 1, SMC_MODEL_ETA_T = 2 };
 enum smc_precond { SMC_PRECOND_LEGACY = 0, SMC_PRECOND_BFBT = 1 };
@@ -66,6 +66,13 @@ typedef struct smc_config {
   int stokes_restart, stokes_maxiter;
   int precision;            /* enum smc_precision */
   int device;               /* CUDA ordinal */
+  /* pressure-dependent Arrhenius law pV(L) (physics/arrhenius.py:283-327),
+   * active when arrhenius_V > 0 (model ETA_T):
+   *   ln eta = -E T / (Ts (T + Ts)) + V (1 - z) / (T + Ts),  Ts = arrhenius_Ts,
+   * with E = E-tilde and V = V-tilde from the calibration
+   * (physics/reference_state.py:277-364, done by the caller) */
+  double arrhenius_E;
+  double arrhenius_V;
 } smc_config;
 
 typedef struct smc_handle smc_handle;

@@ -27,7 +27,7 @@ SMC_MODEL_CONST, SMC_MODEL_ETA_Z, SMC_MODEL_ETA_T = 0, 1, 2
 SMC_PRECOND_LEGACY, SMC_PRECOND_BFBT = 0, 1
 SMC_FP64, SMC_MIXED = 0, 1
 SMC_GRID, SMC_COEFFS, SMC_SYNTH_PAD, SMC_TRUNC_PAD = 0, 1, 2, 3
-SMC_ABI_VERSION = 1
+SMC_ABI_VERSION = 2
 
 
 def _nvcc():
@@ -86,6 +86,7 @@ class SmcConfig(ctypes.Structure):
         ("theta_maxiter", ctypes.c_int), ("theta_restart", ctypes.c_int),
         ("stokes_restart", ctypes.c_int), ("stokes_maxiter", ctypes.c_int),
         ("precision", ctypes.c_int), ("device", ctypes.c_int),
+        ("arrhenius_E", ctypes.c_double), ("arrhenius_V", ctypes.c_double),
     ]
 
 

@@ -549,6 +549,10 @@ struct Model {
 
     law.L = std::log(cfg.deta_T);
     law.Ts = cfg.model == SMC_MODEL_ETA_T ? cfg.arrhenius_Ts : 0.0;
+    if (cfg.model == SMC_MODEL_ETA_T && cfg.arrhenius_V > 0.0) {
+      law.pvE = cfg.arrhenius_E;
+      law.pvV = cfg.arrhenius_V;
+    }
     law.lo = cfg.eta_min; law.hi = cfg.eta_max;
     law.lo_eff = cfg.eta_min * (1.0 - 1e-12);
     law.hi_eff = cfg.eta_max * (1.0 + 1e-12);
@@ -1853,6 +1857,12 @@ void validate(const smc_config* c) {
   if (c->lag < 1 || c->max_K < 1 || c->K < 0) throw std::runtime_error("bad defect-correction settings");
   if (c->theta_restart < 1 || c->stokes_restart < 1) throw std::runtime_error("bad restart");
   if (c->precision != SMC_FP64 && c->precision != SMC_MIXED) throw std::runtime_error("unknown precision");
+  if (!std::isfinite(c->arrhenius_V) || c->arrhenius_V < 0.0)
+    throw std::runtime_error("arrhenius_V must be finite and >= 0");
+  if (c->arrhenius_V > 0.0 &&
+      (c->model != SMC_MODEL_ETA_T || !(c->arrhenius_Ts > 0.0) || !std::isfinite(c->arrhenius_E)))
+    throw std::runtime_error("arrhenius_V > 0 (pV law) needs model ETA_T, arrhenius_Ts > 0 and a finite "
+                             "calibrated arrhenius_E");
 }
 
 }  // namespace

@@ -278,7 +278,9 @@ __global__ void smc_eta_law_kernel(const double* __restrict__ th, const double* 
     if (T < 0.0 || T > 2.0) c_clipT += 1.0;
     double Tc = fmin(fmax(T, 0.0), 2.0);
     double e;
-    if (law.Ts > 0.0) e = exp(-law.L * (1.0 + law.Ts) * Tc / (Tc + law.Ts));
+    if (law.pvV > 0.0)      // pV(L), physics/arrhenius.py:283-327, in the reference's order
+      e = exp((-law.pvE * Tc) / (law.Ts * (Tc + law.Ts)) + law.pvV * (1.0 - z[j]) / (Tc + law.Ts));
+    else if (law.Ts > 0.0) e = exp(-law.L * (1.0 + law.Ts) * Tc / (Tc + law.Ts));
     else e = exp(-law.L * Tc);
     if (e < law.lo_eff || e > law.hi_eff) c_clip += 1.0;
     if (law.w > 0.0) {

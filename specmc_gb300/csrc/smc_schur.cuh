@@ -13,6 +13,8 @@ struct EtaLaw {
   double lo_eff = 0.0, hi_eff = 0.0;   // window with the 1e-12 dead-band
   double w = 0.0, ylo = 0.0, yhi = 0.0;// smooth half-width, ln lo, ln hi
   int z_mode = 0;        // 0: T = 1 - z + th ; 1: T = th
+  // pV(L) law when pvV > 0: ln eta = -pvE T / (Ts (T + Ts)) + pvV (1 - z) / (T + Ts)
+  double pvE = 0.0, pvV = 0.0;
 };
 
 // C_b = alpha A_b B_b for N x N row-major operands (batch stride 0 = shared)

@@ -35,7 +35,8 @@ class GpuModel:
 
     def __init__(self, *, Ra=1e4, Nx=64, Nz=48, Lx=2.0, deta_T=1000.0,
                  internal_heating=0.0, dissipation_number=0.0, eta_min=1e-3,
-                 eta_max=1e3, eta_smooth=0.0, arrhenius_Ts=0.0, precond="legacy",
+                 eta_max=1e3, eta_smooth=0.0, arrhenius_Ts=0.0, arrhenius_E=0.0,
+                 arrhenius_V=0.0, reference_anchor="D", precond="legacy",
                  symmetrize=True, lag=16, K=3, defect_tol=1e-8, max_K=8,
                  eta_drift_tol=0.1, stokes_rtol=1e-8, theta_rtol=1e-10,
                  theta_maxiter=200, theta_restart=40, stokes_restart=80,
@@ -51,6 +52,22 @@ class GpuModel:
         c.eta_min, c.eta_max = float(eta_min), float(eta_max)
         c.eta_smooth = float(eta_smooth)
         c.arrhenius_Ts = float(arrhenius_Ts)
+        # the pressure-dependent Arrhenius law pV(L): Ts, E-tilde, V-tilde from
+        # the one calibration (models/coupled_model.py:188-229)
+        self.pv_record = None
+        if float(arrhenius_V) > 0.0:
+            from .reference_state import calibrate_pv
+            anchor = str(reference_anchor)
+            rec = calibrate_pv(anchor=anchor, V=float(arrhenius_V),
+                               deta_T=(float(deta_T) if anchor == "D" else None))
+            if float(arrhenius_Ts) != 0.0 and abs(float(arrhenius_Ts) - rec["Ts"]) > 1e-12 * rec["Ts"]:
+                raise ValueError("arrhenius_Ts=%r contradicts the reference-state value Ts = %r"
+                                 % (arrhenius_Ts, rec["Ts"]))
+            if float(arrhenius_E) != 0.0 and abs(float(arrhenius_E) - rec["E"]) > 1e-12 * abs(rec["E"]):
+                raise ValueError("arrhenius_E=%r contradicts the calibrated pV activation %r"
+                                 % (arrhenius_E, rec["E"]))
+            self.pv_record = rec
+            c.arrhenius_Ts, c.arrhenius_E, c.arrhenius_V = rec["Ts"], rec["E"], rec["V"]
         c.precond = _lib.SMC_PRECOND_BFBT if str(precond).lower() == "bfbt" else _lib.SMC_PRECOND_LEGACY
         c.symmetrize = 1 if symmetrize else 0
         c.lag, c.K, c.max_K = int(lag), int(K), int(max_K)

@@ -2,7 +2,10 @@
 
 Run once, in a container where the reference package is importable:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference [case ...]
+
+(the optional case names restrict the run to those fixtures, e.g.
+``arrhenius_pv_32x24``).
 
 Every fixture is a small ``.npz`` written by the reference's own public API
 (``specmc.api.build_model`` / ``march_adaptive`` / ``model.diagnostics``) or
@@ -15,6 +18,8 @@ Fixtures (sizes chosen so the whole script runs in a few minutes):
   and the basis matrices on a seeded random coefficient field.
 * ``march_<case>.npz`` -- initial state, every step's dt and state, the final
   diagnostics and the model's counters for one adaptive march per case.
+* ``pv_calibration.npz`` -- ``reference_state.calibrate_pv`` for both
+  anchors (rows: anchor, V, deta_T, E, V, Ts, C, ln D; -1 = not given).
 * ``coupled_ops_16x12.npz`` -- ``eta_of``, ``FreeSchurOperator.matvec``, the
   assembled Schur matrix and the BFBT preconditioner action for one seeded
   state (pins the coupled operator, including its partner half).
@@ -144,7 +149,21 @@ def coupled_ops_case(S):
     print('coupled_ops_16x12 written', flush=True)
 
 
-def main(ref_root):
+def pv_calibration_case(S):
+    """reference_state.calibrate_pv for both anchors and a few V-tilde /
+    contrast values (the pV(L) law's Ts, E-tilde, V-tilde, C, ln D)."""
+    from specmc.physics.reference_state import calibrate_pv
+    rows = []
+    for anchor, V, D in (("Ea", None, None), ("Ea", 2.0, None), ("D", 2.0, 1e3),
+                         ("D", 0.5, 1e5), ("D", 22.5, 10.0)):
+        r = calibrate_pv(anchor=anchor, V=V, deta_T=D)
+        rows.append([0 if anchor == "Ea" else 1, -1.0 if V is None else V,
+                     -1.0 if D is None else D, r["E"], r["V"], r["Ts"], r["C"], r["ln_D"]])
+    np.savez_compressed(os.path.join(HERE, 'pv_calibration.npz'), rows=np.array(rows))
+    print('pv_calibration written', flush=True)
+
+
+def main(ref_root, only=()):
     sys.path.insert(0, ref_root)
     import specmc.api as api
     from specmc.config import ConvectionConfig
@@ -153,40 +172,52 @@ def main(ref_root):
         pass
     S.api = api
     S.ConvectionConfig = ConvectionConfig
+    def mc(name, *a):                    # the selected march cases only
+        if not only or name in only:
+            march_case(name, *a)
 
-    transforms_case(S)
-    coupled_ops_case(S)
+    if not only:
+        transforms_case(S)
+        coupled_ops_case(S)
+    if not only or 'pv_calibration' in only:
+        pv_calibration_case(S)
     base = dict(Ra=1e4, Nx=32, Nz=24)
     # configuration 1 of the headline table: isoviscous, march to t = 1e-3
-    march_case('const_32x24', dict(base, viscosity_model='const'), 25,
+    mc('const_32x24', dict(base, viscosity_model='const'), 25,
                ('seed', 3e-2, 1, 1), S)
-    march_case('etaz_32x24', dict(base, viscosity_model='eta_z',
+    mc('etaz_32x24', dict(base, viscosity_model='eta_z',
                                   deta_T=100.0), 20, ('seed', 3e-2, 1, 1), S)
-    march_case('etaT_32x24', dict(base, viscosity_model='eta_T'), 25,
+    mc('etaT_32x24', dict(base, viscosity_model='eta_T'), 25,
                ('seed', 3e-2, 1, 1), S)
-    march_case('etaT_bfbt_32x24', dict(base, viscosity_model='eta_T',
+    mc('etaT_bfbt_32x24', dict(base, viscosity_model='eta_T',
                                        precond='bfbt'), 12,
                ('seed', 3e-2, 1, 1), S)
     # internally heated 2:1 box (Lx = 4 is the mirror-doubled carrier)
-    march_case('heated_2to1_32x24',
+    mc('heated_2to1_32x24',
                dict(base, viscosity_model='eta_T', Lx=4.0, Ra=1.25e4,
                     internal_heating=1.5), 12,
                ('noise', 1e-2, 8, 8, 1234), S)
     # Arrhenius + window + dissipation + heating (the large-run physics)
-    march_case('arrhenius_32x24',
+    mc('arrhenius_32x24',
                dict(base, viscosity_model='arrhenius', deta_T=1e3,
                     arrhenius_Ts=1.0, eta_min=1e-3, eta_max=1.0,
                     dissipation_number=0.5, internal_heating=1.0),
                12, ('noise', 1e-2, 8, 8, 99), S)
     # smooth eta window that is active on this state
-    march_case('smooth_32x24',
+    mc('smooth_32x24',
                dict(base, viscosity_model='eta_T', eta_min=3e-3, eta_max=1.0,
                     eta_smooth=0.5), 10, ('seed', 3e-2, 1, 1), S)
+    # the pressure-dependent Arrhenius law (pV(L), arrhenius_V > 0) with the
+    # contrast anchor 'D' (E-tilde from deta_T), default viscosity window
+    mc('arrhenius_pv_32x24',
+               dict(base, viscosity_model='arrhenius', deta_T=1e3,
+                    arrhenius_V=0.5, reference_anchor='D'),
+               6, ('noise', 1e-2, 8, 8, 42), S)
     # configuration 2 grid, a few steps (the oracle of the bench workload)
-    march_case('etaT_64x96', dict(Ra=1e4, Nx=64, Nz=96,
+    mc('etaT_64x96', dict(Ra=1e4, Nx=64, Nz=96,
                                   viscosity_model='eta_T'), 6,
                ('seed', 3e-2, 1, 1), S)
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference', tuple(sys.argv[2:]))

@@ -5,6 +5,7 @@ import os
 import re
 import warnings
 
+import numpy as np
 import pytest
 
 from conftest import ROOT
@@ -67,6 +68,33 @@ def test_config_validation_mirrors_reference():
         assert any(issubclass(x.category, UserWarning) for x in w)
     c = ConvectionConfig(viscosity_model="arrhenius", arrhenius_Ts=1.0)
     assert c.canonical()["viscosity_model"] == "arrhenius"
+
+
+def test_pv_config_and_calibration():
+    """The pressure-dependent Arrhenius branch (arrhenius_V > 0): the
+    reference's validation rules (specmc/config.py:496-560) and its
+    calibration (physics/reference_state.py:277-364), pinned against the
+    reference's own values (tests/golden/pv_calibration.npz)."""
+    import os
+    from specmc_gb300.config import ConvectionConfig, arrhenius_effective_E
+    from specmc_gb300.reference_state import calibrate_pv
+    ConvectionConfig(viscosity_model="arrhenius", arrhenius_V=2.0)
+    ConvectionConfig(viscosity_model="arrhenius", arrhenius_V=2.0, reference_anchor="Ea")
+    ok = calibrate_pv(anchor="D", V=2.0, deta_T=1000.0)
+    ConvectionConfig(viscosity_model="arrhenius", arrhenius_V=2.0, arrhenius_Ts=ok["Ts"], arrhenius_E=ok["E"])
+    for bad in (dict(viscosity_model="arrhenius", arrhenius_V=2.0, reference_anchor="X"),
+                dict(viscosity_model="eta_T", arrhenius_V=2.0),
+                dict(viscosity_model="arrhenius", arrhenius_V=2.0, arrhenius_Ts=0.5),
+                dict(viscosity_model="arrhenius", arrhenius_V=2.0, arrhenius_E=1.0),
+                dict(viscosity_model="arrhenius", arrhenius_V=-1.0)):
+        with pytest.raises(ValueError):
+            ConvectionConfig(**bad)
+    assert arrhenius_effective_E(ConvectionConfig(viscosity_model="arrhenius", arrhenius_V=2.0)) == ok["E"]
+    rows = np.load(os.path.join(os.path.dirname(__file__), "golden", "pv_calibration.npz"))["rows"]
+    for a, V, D, E, Vt, Ts, C, lnD in rows:
+        r = calibrate_pv(anchor="Ea" if a == 0 else "D", V=None if V < 0 else V,
+                         deta_T=None if D < 0 else D)
+        assert (r["E"], r["V"], r["Ts"], r["C"], r["ln_D"]) == (E, Vt, Ts, C, lnD)
 
 
 def test_api_dispatch_table():

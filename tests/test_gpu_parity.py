@@ -87,6 +87,7 @@ CASES = [
     ("heated_2to1_32x24", 1e-7, 1e-8),
     ("arrhenius_32x24", 1e-7, 1e-8),
     ("smooth_32x24", 1e-7, 1e-8),
+    ("arrhenius_pv_32x24", 1e-7, 1e-8),
 ]
 
 EXACT_COUNTERS = ("n_refresh", "n_defect", "n_defect_failed", "n_defect_double_fail",
@@ -173,7 +174,8 @@ def test_pseudo_spectral_mult_eta_equals_dense(gb):
     assert _rel(outs[0], outs[1]) < 1e-12
 
 
-@pytest.mark.parametrize("case", ["etaT_32x24", "heated_2to1_32x24", "arrhenius_32x24"])
+@pytest.mark.parametrize("case", ["etaT_32x24", "heated_2to1_32x24", "arrhenius_32x24",
+                                  "arrhenius_pv_32x24"])
 def test_mixed_form_matches_reference(gb, case):
     """The fast form reproduces the reference's Nu and Vrms to 1e-6 relative."""
     api, CC = gb

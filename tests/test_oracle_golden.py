@@ -65,7 +65,8 @@ def test_coupled_operator():
 
 
 CASES = ["const_32x24", "etaz_32x24", "etaT_32x24", "etaT_bfbt_32x24",
-         "heated_2to1_32x24", "arrhenius_32x24", "smooth_32x24"]
+         "heated_2to1_32x24", "arrhenius_32x24", "smooth_32x24", "arrhenius_pv_32x24"]
+DIAG_TOL = {}
 
 
 def _cfg_from(g):
@@ -90,4 +91,4 @@ def test_march_matches_reference(case):
     assert worst < 1e-7, worst
     for key in ("Nu_top", "urms", "Nu_energy"):
         ref = g["diag_" + key].item()
-        assert abs(d[key] - ref) <= 1e-9 * abs(ref), (key, d[key], ref)
+        assert abs(d[key] - ref) <= DIAG_TOL.get(case, 1e-9) * abs(ref), (key, d[key], ref)

@@ -333,3 +333,12 @@ class RBCImplicitTheta(GpuModel):
 class RBCCoupled(GpuModel):
     """eta(T(x,z,t)) coupled Stokes (lagged LU + defect / BFBT) + BDF2 theta."""
     _MODEL = _lib.SMC_MODEL_ETA_T
+
+    def eta_of(self, that):
+        """-> the (Nx, Nz) viscosity of a state: padded law, window, x-truncation
+        and positivity guard (models/coupled_model.py:401-496).  Updates the
+        eta counters as the reference's eta_of does."""
+        p, mem, keep = self._spec_in(that)
+        q, out = self._grid_out(self.Nx, mem == _lib.SMC_DEVICE)
+        _lib.check(self._lib.smc_eta_of(self._h, p, mem, q))
+        return out

@@ -20,6 +20,8 @@ Fixtures (sizes chosen so the whole script runs in a few minutes):
   diagnostics and the model's counters for one adaptive march per case.
 * ``pv_calibration.npz`` -- ``reference_state.calibrate_pv`` for both
   anchors (rows: anchor, V, deta_T, E, V, Ts, C, ln D; -1 = not given).
+* ``energy_32x24.npz`` -- ``physics/heating.py`` / ``physics/dissipation.py``
+  budgets and integrals on three states of the Arrhenius + H + Phi march.
 * ``coupled_ops_16x12.npz`` -- ``eta_of``, ``FreeSchurOperator.matvec``, the
   assembled Schur matrix and the BFBT preconditioner action for one seeded
   state (pins the coupled operator, including its partner half).
@@ -163,6 +165,39 @@ def pv_calibration_case(S):
     print('pv_calibration written', flush=True)
 
 
+def energy_case(S):
+    """physics/heating.py and physics/dissipation.py diagnostics on three
+    states of the Arrhenius + H + Phi march: the BDF2 budgets, <Phi>,
+    Ra <theta u_z>, the flux profile and the boundary fluxes."""
+    from specmc.physics import heating as HEAT, dissipation as DISS
+    api = S.api
+    cfg = S.ConvectionConfig(Ra=1e4, Nx=32, Nz=24, viscosity_model='arrhenius', deta_T=1e3,
+                             arrhenius_Ts=1.0, eta_min=1e-3, eta_max=1.0,
+                             dissipation_number=0.5, internal_heating=1.0)
+    m = api.build_model(cfg)
+    s0 = seeded_noise_theta(m, amp=1e-2, mmax=8, nmax=8, seed=99, Lx=cfg.Lx, H=1.0)
+    states = [s0]
+    for _ in range(3):
+        states.append(m.step(states[-1], api.production_dt(m, states[-1])))
+    s1, s2, s3 = states[1], states[2], states[3]
+    psi, _ = m.stokes(s3)
+    eta = m.eta_of(s3)
+    a0, b0, b1 = 3.5e4, 4.6e4, 1.1e4
+    hb = HEAT.balance(m, s3, s2, s1, a0, b0, b1, H=1.0)
+    db = DISS.balance(m, s3, s2, s1, a0, b0, b1, H=1.0, Di=0.5, psi=psi, eta=eta)
+    z, q = HEAT.flux_profile(m, s3, H=1.0)
+    rec = dict(s1=s1, s2=s2, s3=s3, psi=psi, eta=eta, abc=np.array([a0, b0, b1]),
+               phi_int=np.float64(DISS.phi_integral(m, psi, eta)),
+               phi_int_noeta=np.float64(DISS.phi_integral(m, psi)),
+               pi_theta=np.float64(DISS.pi_theta(m, psi, s3)),
+               pi_theta_plain=np.float64(DISS.pi_theta(m, psi, s3, dealias=False)),
+               phi_coeffs=DISS.phi_coeffs(m, psi, eta), q=q,
+               **{'hb_' + k: np.float64(v) for k, v in hb.items()},
+               **{'db_' + k: np.float64(v) for k, v in db.items()})
+    np.savez_compressed(os.path.join(HERE, 'energy_32x24.npz'), **rec)
+    print('energy_32x24 written', flush=True)
+
+
 def main(ref_root, only=()):
     sys.path.insert(0, ref_root)
     import specmc.api as api
@@ -181,6 +216,8 @@ def main(ref_root, only=()):
         coupled_ops_case(S)
     if not only or 'pv_calibration' in only:
         pv_calibration_case(S)
+    if not only or 'energy_32x24' in only:
+        energy_case(S)
     base = dict(Ra=1e4, Nx=32, Nz=24)
     # configuration 1 of the headline table: isoviscous, march to t = 1e-3
     mc('const_32x24', dict(base, viscosity_model='const'), 25,

@@ -188,3 +188,32 @@ def test_checkpoint_resume_keeps_bdf2_history(tmp_path):
         else:
             assert np.abs(s2 - straight).max() > 1e-12 * np.abs(straight).max()
         m2.close()
+
+
+def test_energy_diagnostics_on_gpu_transforms():
+    """The energy-budget diagnostics (specmc_gb300.energy: physics/heating.py,
+    physics/dissipation.py) with the GPU model's transforms, eta and Stokes
+    solve, against the reference's values (tests/golden/energy_32x24.npz)."""
+    import os
+    from specmc_gb300 import api, energy as EN
+    from specmc_gb300.config import ConvectionConfig
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "energy_32x24.npz"))
+    m = api.build_model(ConvectionConfig(
+        Ra=1e4, Nx=32, Nz=24, viscosity_model="arrhenius", deta_T=1e3, arrhenius_Ts=1.0,
+        eta_min=1e-3, eta_max=1.0, dissipation_number=0.5, internal_heating=1.0))
+    a0, b0, b1 = g["abc"]
+    eta = m.eta_of(g["s3"])
+    assert np.linalg.norm(eta - g["eta"]) <= 1e-12 * np.linalg.norm(g["eta"])
+    hb = EN.heating_balance(m, g["s3"], g["s2"], g["s1"], a0, b0, b1, H=1.0)
+    for k, v in hb.items():
+        assert abs(v - float(g["hb_" + k])) <= 1e-11 * max(1.0, abs(float(g["hb_" + k]))), k
+    db = EN.dissipation_balance(m, g["s3"], g["s2"], g["s1"], a0, b0, b1, H=1.0, Di=0.5,
+                                psi=g["psi"], eta=g["eta"])
+    for k, v in db.items():
+        assert abs(v - float(g["db_" + k])) <= 1e-10 * max(1.0, abs(float(g["db_" + k]))), k
+    assert _rel(EN.phi_integral(m, g["psi"], g["eta"]), float(g["phi_int"])) < 1e-10
+    assert _rel(EN.pi_theta(m, g["psi"], g["s3"]), float(g["pi_theta"])) < 1e-10
+    pc = EN.phi_coeffs(m, g["psi"], g["eta"])
+    assert np.linalg.norm(pc - g["phi_coeffs"]) <= 1e-10 * np.linalg.norm(g["phi_coeffs"])
+    z, q = EN.flux_profile(m, g["s3"], H=1.0)
+    assert np.max(np.abs(q - g["q"])) <= 1e-7 * np.max(np.abs(g["q"]))

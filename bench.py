@@ -156,6 +156,20 @@ def run_reference(args, rank, world):
     return 0
 
 
+def max_over_ranks(x):
+    """-> the maximum of ``x`` over the ranks of the initialised process group
+    (``x`` without one): the timed region of N replicas is the slowest rank's.
+    A CUDA tensor carries it over NCCL, a host tensor over gloo."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ------------------------------------------------------------------ GPU side
 def run_ours(args, rank, world):
     import ctypes
@@ -232,10 +246,7 @@ def run_ours(args, rank, world):
         state = torch.empty((m.Nk, m.Nz), dtype=torch.complex128, device="cuda")
         _lib.check(lib.smc_get_state(m._h, ctypes.c_void_p(state.data_ptr()), _lib.SMC_DEVICE))
         diag = m.diagnostics(state.cpu().numpy())
-        if world > 1:
-            t = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms_total = float(t.item())
+        ms_total = max_over_ranks(ms_total)
         return dict(ms=ms_total, launches=launches, prof=prof, diag=diag, m=m, th0=th0,
                     step_ms=step_ms)
 
@@ -266,10 +277,7 @@ def run_ours(args, rank, world):
         out = m2.step(sp, dt)
         sp[...] = out
     el = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([el], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el = float(t.item())
+    el = max_over_ranks(el)
     e2e = {"value": world * args.steps / el, "unit": "steps/s",
            "h2d_bytes_per_step": 2 * n_c * 16, "d2h_bytes_per_step": n_c * 16 + 8}
 

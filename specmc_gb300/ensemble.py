@@ -7,8 +7,9 @@ normally spreads over every SM; in an ensemble each handle's engine is capped
 at its share of the SMs so that the concurrent runs fit side by side.
 
 The runs are independent -- nothing is exchanged between them while they
-step -- so an ensemble shards across GPUs by partitioning the run list
-(replicas of this driver, one per GPU).
+step -- so an ensemble shards across GPUs by partitioning the run list: one
+process per GPU (torchrun) marches its shard (``march_ensemble_sharded``) and
+the per-run results are gathered on rank 0 once, at the end.
 
 ``ensemble_configs`` draws the seeded mixed workload of 256 runs: grid from
 {32x24, 64x48, 64x96, 128x96}, Ra log-uniform in [1e4, 1e6], deta_T
@@ -27,7 +28,8 @@ from . import _lib, api
 from . import _numerics as NUM
 from .config import ConvectionConfig
 
-__all__ = ["GRIDS", "MODELS", "ensemble_configs", "march_ensemble", "device_sms"]
+__all__ = ["GRIDS", "MODELS", "ensemble_configs", "march_ensemble", "march_ensemble_sharded",
+           "shard", "device_sms"]
 
 GRIDS = ((32, 24), (64, 48), (64, 96), (128, 96))
 MODELS = ("const", "eta_z", "eta_T")
@@ -149,6 +151,59 @@ def march_ensemble(runs, nsteps=100, form="mixed", concurrency=8, safety=None, d
     return out
 
 
+def shard(nruns, rank, world):
+    """-> the run indices of ``rank`` out of ``world``: round robin (i = rank,
+    rank + world, ...), which spreads the grid sizes and models of the seeded
+    list evenly over the GPUs."""
+    if not (0 <= int(rank) < int(world)):
+        raise ValueError("rank %r outside world size %r" % (rank, world))
+    return list(range(int(rank), int(nruns), int(world)))
+
+
+def march_ensemble_sharded(runs, nsteps=100, rank=None, world=None, group=None,
+                           keep_states=False, march=None, **kw):
+    """One process per GPU: march this rank's shard of ``runs``
+    (``march_ensemble(..., **kw)`` on this process's GPU, ``device`` in ``kw``)
+    and gather the per-run results on rank 0 with one host-side gather after
+    every run has finished; nothing is exchanged while the runs step.
+
+    -> on rank 0 the results of all runs in run order (each with its
+    ``rank``), elsewhere None.  The final states stay on their ranks unless
+    ``keep_states``.  ``rank``/``world`` default to the initialised
+    torch.distributed group (a single process without one); ``march``
+    replaces march_ensemble (same call), e.g. to test the gather without a GPU."""
+    dist = None
+    if rank is None or world is None:
+        import torch.distributed as dist
+        if dist.is_available() and dist.is_initialized():
+            rank = dist.get_rank(group) if rank is None else rank
+            world = dist.get_world_size(group) if world is None else world
+        else:
+            rank, world, dist = 0, 1, None
+    idx = shard(len(runs), rank, world)
+    res = (march or march_ensemble)([runs[i] for i in idx], nsteps=nsteps, **kw)
+    mine = []
+    for i, r in zip(idx, res):
+        r = dict(r, rank=int(rank))
+        if not keep_states:
+            r.pop("state", None)
+        mine.append((i, r))
+    if world == 1:
+        parts = [mine]
+    else:
+        if dist is None:
+            import torch.distributed as dist
+        parts = [None] * world if rank == 0 else None
+        dist.gather_object(mine, parts, dst=0, group=group)
+    if rank != 0:
+        return None
+    out = [None] * len(runs)
+    for part in parts:
+        for i, r in part:
+            out[i] = r
+    return out
+
+
 def _main(argv=None):
     """python -m specmc_gb300.ensemble [--runs 256] [--steps 100] ...: march the
     seeded ensemble and print one JSON summary line."""
@@ -165,18 +220,37 @@ def _main(argv=None):
     ap.add_argument("--max-wall", type=float, default=None,
                     help="seconds after which a run stops, flagged 'time'")
     a = ap.parse_args(argv)
+    import os
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
     runs = ensemble_configs(a.runs, a.seed)
+    if world > 1:          # under torchrun: one shard per GPU, gathered on rank 0
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", init_method="env://", world_size=world, rank=rank)
     t0 = time.perf_counter()
-    res = march_ensemble(runs, nsteps=a.steps, form=a.form, concurrency=a.concurrency,
-                         engine_ctas=a.engine_ctas, max_wall=a.max_wall)
+    res = march_ensemble_sharded(runs, nsteps=a.steps, rank=rank, world=world, form=a.form,
+                                 concurrency=a.concurrency, engine_ctas=a.engine_ctas,
+                                 max_wall=a.max_wall, device=local)
     wall = time.perf_counter() - t0
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([wall], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        wall = float(t.item())
+        dist.destroy_process_group()
+    if rank != 0:
+        return
     steps = sum(r["steps"] for r in res)
     by = collections.defaultdict(list)
     for run, r in zip(runs, res):
         by["%dx%d %s" % (run["cfg"].Nx, run["cfg"].Nz, run["cfg"].viscosity_model)].append(
             1e3 * r["march_s"] / max(r["steps"], 1))
     print(json.dumps(dict(
-        runs=len(runs), steps=steps, wall_s=wall, steps_per_s=steps / wall, form=a.form,
+        runs=len(runs), n_gpus=world, steps=steps, wall_s=wall, steps_per_s=steps / wall, form=a.form,
         concurrency=a.concurrency, build_s=sum(r["build_s"] for r in res),
         status=dict(collections.Counter(r["status"] for r in res)),
         median_ms_per_step={k: float(np.median(v)) for k, v in sorted(by.items())})))

@@ -22,6 +22,8 @@ Fixtures (sizes chosen so the whole script runs in a few minutes):
   anchors (rows: anchor, V, deta_T, E, V, Ts, C, ln D; -1 = not given).
 * ``energy_32x24.npz`` -- ``physics/heating.py`` / ``physics/dissipation.py``
   budgets and integrals on three states of the Arrhenius + H + Phi march.
+* ``config_cases.json`` -- ``ConvectionConfig`` on 300 seeded configurations:
+  outcome class, warning classes, ``canonical()``.
 * ``coupled_ops_16x12.npz`` -- ``eta_of``, ``FreeSchurOperator.matvec``, the
   assembled Schur matrix and the BFBT preconditioner action for one seeded
   state (pins the coupled operator, including its partner half).
@@ -198,6 +200,59 @@ def energy_case(S):
     print('energy_32x24 written', flush=True)
 
 
+CONFIG_MENU = dict(
+    viscosity_model=['eta_T', 'const', 'eta_z', 'arrhenius', 'constant', 'isoviscous', 'etaz',
+                     'nope', 'eta_Tz', 'ETA_T'],
+    deta_T=[1000.0, 1.0, 0.5, -1.0, 1e5],
+    eta_z_coeff=[0.0, 1.0], depth_dependence=[0.0, 0.5],
+    arrhenius_E=[0.0, 1.0, 7.536], arrhenius_V=[0.0, 0.5, -1.0, 2.0],
+    reference_anchor=['D', 'Ea', 'X'], arrhenius_Ts=[0.0, 1.0, 0.091, -0.5],
+    eta_min=[1e-3, 1.0, 0.0, -1.0, 1e-6], eta_max=[1e3, 1.0, 0.5, 1e6],
+    eta_smooth=[0.0, 0.5, 2.0, -0.1], precond=['legacy', 'bfbt', 'ilu', 'BFBT'],
+    internal_heating=[0.0, 1.5, -1.0], dissipation_number=[0.0, 0.5, -0.5],
+    compressibility=['boussinesq', 'tala', 'ala', 'x'], Ra=[1e4, 0.0, -1.0, 1e7],
+    Nx=[64, 3, 63, 32], Nz=[96, 3, 24], Lx=[2.0, 4.0, 0.0], lag=[16, 0, 1], K=[3, 0, 9, 8],
+    defect_tol=[1e-8, 0.0, -1.0], max_K=[8, 0, 3], symmetrize=[True, False])
+
+
+def config_case(S):
+    """ConvectionConfig on 300 seeded configurations (1 to 3 fields moved from
+    their defaults to edge values): the outcome class (ok or the exception),
+    the warning classes and, when valid, canonical()."""
+    import json
+    import warnings
+    rng = np.random.default_rng(5)
+    names = sorted(CONFIG_MENU)
+    out = []
+    for _ in range(300):
+        kw = {}
+        for name in rng.choice(names, size=int(rng.integers(1, 4)), replace=False):
+            vals = CONFIG_MENU[str(name)]
+            v = vals[int(rng.integers(len(vals)))]
+            kw[str(name)] = v.item() if hasattr(v, 'item') else v
+        rec = dict(kw=kw)
+        with warnings.catch_warnings(record=True) as w:
+            warnings.simplefilter('always')
+            try:
+                c = S.ConvectionConfig(**kw)
+                rec['outcome'] = 'ok'
+                rec['canonical'] = c.canonical()
+                try:
+                    sp = S.api.model_spec(c)
+                    rec['spec'] = dict(model=sp['model'], builder=sp['builder'],
+                                       kwargs={k: (None if v is None else v)
+                                               for k, v in sp['kwargs'].items()})
+                except Exception as ex:                 # noqa: BLE001
+                    rec['spec'] = type(ex).__name__
+            except Exception as ex:                     # noqa: BLE001 -- the class is the record
+                rec['outcome'] = type(ex).__name__
+        rec['warnings'] = sorted({x.category.__name__ for x in w})
+        out.append(rec)
+    with open(os.path.join(HERE, 'config_cases.json'), 'w') as f:
+        json.dump(out, f, indent=0, sort_keys=True)
+    print('config_cases written', flush=True)
+
+
 def main(ref_root, only=()):
     sys.path.insert(0, ref_root)
     import specmc.api as api
@@ -218,6 +273,8 @@ def main(ref_root, only=()):
         pv_calibration_case(S)
     if not only or 'energy_32x24' in only:
         energy_case(S)
+    if not only or 'config_cases' in only:
+        config_case(S)
     base = dict(Ra=1e4, Nx=32, Nz=24)
     # configuration 1 of the headline table: isoviscous, march to t = 1e-3
     mc('const_32x24', dict(base, viscosity_model='const'), 25,

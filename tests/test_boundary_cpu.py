@@ -137,12 +137,12 @@ def test_config_and_model_spec_match_reference_on_seeded_cases():
         if cfg is None:
             continue
         assert cfg.canonical() == c["canonical"], c["kw"]
-        if str(cfg.compressibility).lower() == "tala":
-            with pytest.raises(NotImplementedError):
-                api.model_spec(cfg)
-            continue
         with warnings.catch_warnings():
-            warnings.simplefilter("ignore")
+            warnings.simplefilter("ignore")            # validate() repeats the warnings above
+            if str(cfg.compressibility).lower() == "tala":
+                with pytest.raises(NotImplementedError):
+                    api.model_spec(cfg)
+                continue
             sp = api.model_spec(cfg)
         assert (sp["model"], sp["builder"], sp["kwargs"]) == (
             c["spec"]["model"], c["spec"]["builder"], c["spec"]["kwargs"]), c["kw"]

@@ -242,6 +242,7 @@ def config_case(S):
                     rec['spec'] = dict(model=sp['model'], builder=sp['builder'],
                                        kwargs={k: (None if v is None else v)
                                                for k, v in sp['kwargs'].items()})
+                    rec['describe'] = json.loads(json.dumps(S.api.describe(c), default=str))
                 except Exception as ex:                 # noqa: BLE001
                     rec['spec'] = type(ex).__name__
             except Exception as ex:                     # noqa: BLE001 -- the class is the record

@@ -116,7 +116,7 @@ def test_config_and_model_spec_match_reference_on_seeded_cases():
     configurations (tests/golden/config_cases.json, written by the reference's
     own ConvectionConfig / api.model_spec): the same outcome (valid, ValueError,
     NotImplementedError), the same warnings, the same canonical() and the same
-    model / builder / constructor kwargs.  TALA is the one documented
+    model / builder / constructor kwargs and api.describe().  TALA is the one documented
     difference: the reference builds it, here it raises NotImplementedError."""
     import json
     from specmc_gb300 import api
@@ -144,5 +144,7 @@ def test_config_and_model_spec_match_reference_on_seeded_cases():
                     api.model_spec(cfg)
                 continue
             sp = api.model_spec(cfg)
+            d = json.loads(json.dumps(api.describe(cfg), default=str))
         assert (sp["model"], sp["builder"], sp["kwargs"]) == (
             c["spec"]["model"], c["spec"]["builder"], c["spec"]["kwargs"]), c["kw"]
+        assert d == c["describe"], c["kw"]

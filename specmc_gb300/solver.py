@@ -28,6 +28,28 @@ def _cgl(N):
     return 0.5 * (1.0 - np.cos(np.pi * np.arange(N) / (N - 1)))
 
 
+def basis_arrays(Nx, Nz, Lx):
+    """-> the host copies of the discretisation the model exposes under the
+    reference's names (rbc_galerkin.py:63-81, :258-290): kx = 2 pi rfftfreq,
+    x nodes, CGL nodes z (ascending), V (values = V @ coefficients, Chebyshev
+    in 2z - 1), Vi = V^-1, the coefficient-space derivative D (d/dz on [0, 1])
+    and the Clenshaw-Curtis weights wq."""
+    Nx, Nz, Lx = int(Nx), int(Nz), float(Lx)
+    z = _cgl(Nz)
+    V = _npcheb.chebvander(2.0 * z - 1.0, Nz - 1)
+    Vi = np.linalg.inv(V)
+    D = np.zeros((Nz, Nz))
+    for k in range(1, Nz):
+        n = np.arange(k - 1, -1, -2)
+        D[n, k] = 4.0 * k
+        if n[-1] == 0:
+            D[0, k] = 2.0 * k
+    gk = np.array([0.0 if (k % 2) else 1.0 / (1.0 - k * k) for k in range(Nz)])
+    gk[0] = 1.0
+    return dict(kx=2 * np.pi * np.fft.rfftfreq(Nx, d=Lx / Nx), x=np.arange(Nx) * Lx / Nx, z=z,
+                V=V, Vi=Vi, D=D, wq=Vi.T @ gk)
+
+
 class GpuModel:
     """Common handle logic of the three model classes."""
 
@@ -92,23 +114,10 @@ class GpuModel:
         self.deta_T = float(deta_T)
         self.internal_heating = float(internal_heating)
         self.dissipation_number = float(dissipation_number)
-        self.kx = 2 * np.pi * np.fft.rfftfreq(self.Nx, d=self.Lx / self.Nx)
+        for k, v in basis_arrays(self.Nx, self.Nz, self.Lx).items():
+            setattr(self, k, v)
         self.Nk = len(self.kx)
         self.Np = 2 * self.Nx
-        self.x = np.arange(self.Nx) * self.Lx / self.Nx
-        self.z = _cgl(self.Nz)
-        self.V = _npcheb.chebvander(2.0 * self.z - 1.0, self.Nz - 1)
-        self.Vi = np.linalg.inv(self.V)
-        D = np.zeros((self.Nz, self.Nz))
-        for k in range(1, self.Nz):
-            n = np.arange(k - 1, -1, -2)
-            D[n, k] = 4.0 * k
-            if n[-1] == 0:
-                D[0, k] = 2.0 * k
-        self.D = D
-        gk = np.array([0.0 if (k % 2) else 1.0 / (1.0 - k * k) for k in range(self.Nz)])
-        gk[0] = 1.0
-        self.wq = self.Vi.T @ gk
         self.dealias = True
 
     # ------------------------------------------------------------ plumbing

@@ -148,3 +148,15 @@ def test_config_and_model_spec_match_reference_on_seeded_cases():
         assert (sp["model"], sp["builder"], sp["kwargs"]) == (
             c["spec"]["model"], c["spec"]["builder"], c["spec"]["kwargs"]), c["kw"]
         assert d == c["describe"], c["kw"]
+
+
+def test_model_basis_attributes_match_reference():
+    """The host copies the GPU models expose (x, z, kx, V, Vi, D, wq) equal the
+    reference's RBC attributes (tests/golden/transforms_16x12.npz)."""
+    from specmc_gb300.solver import basis_arrays
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "transforms_16x12.npz"))
+    b = basis_arrays(16, 12, 2.0)
+    for k in ("x", "z", "kx", "V", "Vi", "D", "wq"):
+        ref = g[k]
+        assert b[k].shape == ref.shape, k
+        assert np.max(np.abs(b[k] - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref))), k

@@ -1,6 +1,6 @@
 """The CPU oracle against fixtures written by the SpecMC reference itself.
 
-These pin the oracle (the checker of the GPU path): if it drifts from the
+These pin the oracle (what the GPU path is tested against): if it drifts from the
 reference, every GPU parity test downstream would be measuring against the
 wrong thing.
 """

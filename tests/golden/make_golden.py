@@ -24,6 +24,7 @@ Fixtures (sizes chosen so the whole script runs in a few minutes):
   budgets and integrals on three states of the Arrhenius + H + Phi march.
 * ``config_cases.json`` -- ``ConvectionConfig`` on 300 seeded configurations:
   outcome class, warning classes, ``canonical()``.
+* ``ckpt/t_0.125000.npz`` -- a state written by ``specmc.io.checkpoint.save``.
 * ``coupled_ops_16x12.npz`` -- ``eta_of``, ``FreeSchurOperator.matvec``, the
   assembled Schur matrix and the BFBT preconditioner action for one seeded
   state (pins the coupled operator, including its partner half).
@@ -254,6 +255,18 @@ def config_case(S):
     print('config_cases written', flush=True)
 
 
+def checkpoint_case(S):
+    """A checkpoint written by specmc.io.checkpoint.save (the reference's own
+    writer), under tests/golden/ckpt/."""
+    from specmc.io import checkpoint as CK
+    that = (np.arange(12.0) + 1j * np.arange(12.0)[::-1]).reshape(3, 4)
+    d = os.path.join(HERE, 'ckpt')
+    for f in os.listdir(d) if os.path.isdir(d) else ():
+        os.remove(os.path.join(d, f))
+    p = CK.save(d, that, 0.125, n=7, fac=40.0)
+    print('checkpoint written:', os.path.basename(p), flush=True)
+
+
 def main(ref_root, only=()):
     sys.path.insert(0, ref_root)
     import specmc.api as api
@@ -276,6 +289,8 @@ def main(ref_root, only=()):
         energy_case(S)
     if not only or 'config_cases' in only:
         config_case(S)
+    if not only or 'checkpoint' in only:
+        checkpoint_case(S)
     base = dict(Ra=1e4, Nx=32, Nz=24)
     # configuration 1 of the headline table: isoviscous, march to t = 1e-3
     mc('const_32x24', dict(base, viscosity_model='const'), 25,

@@ -13,7 +13,7 @@ from specmc_gb300 import checkpoint as ck  # noqa: E402
 def test_roundtrip_and_names(tmp_path):
     that = (np.arange(12.0) + 1j * np.arange(12.0)[::-1]).reshape(3, 4)
     p = ck.save(str(tmp_path), that, 0.125, n=7, fac=40.0)
-    assert os.path.basename(p) == "state_0.125000.npz"
+    assert os.path.basename(p) == "t_0.125000.npz" == ck.filename(ck.DEFAULT_PREFIX, 0.125)
     assert not any(f.endswith(".tmp.npz") for f in os.listdir(tmp_path))
     s, meta = ck.load(p)
     assert np.array_equal(s, that)
@@ -38,7 +38,26 @@ def test_loader_errors(tmp_path):
 def test_files_of_the_reference_layout_load(tmp_path):
     # a file written the way specmc/io/checkpoint.py:49-56 writes it
     that = np.ones((2, 3), complex)
-    fn = tmp_path / "state_0.010000.npz"
+    fn = tmp_path / "t_0.010000.npz"
     np.savez_compressed(fn, that=that, t=0.01, n=None, fac=None)
     s, meta = ck.load(str(fn))
     assert np.array_equal(s, that) and meta["t"] == 0.01 and meta["n"] is None
+
+
+def test_reference_written_checkpoint_loads_and_ours_matches_it(tmp_path):
+    """A state written by the reference's own checkpoint.save
+    (tests/golden/ckpt/) loads here, and save() here writes the same file name,
+    keys, values and dtypes."""
+    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ckpt")
+    ref_path = os.path.join(d, "t_0.125000.npz")
+    that = (np.arange(12.0) + 1j * np.arange(12.0)[::-1]).reshape(3, 4)
+    s, meta = ck.load(ref_path)
+    assert np.array_equal(s, that) and (meta["t"], meta["n"], meta["fac"]) == (0.125, 7, 40.0)
+    assert ck.latest(d) == (0.125, ref_path)
+    ours = ck.save(str(tmp_path), that, 0.125, n=7, fac=40.0)
+    assert os.path.basename(ours) == os.path.basename(ref_path)
+    a, b = np.load(ours, allow_pickle=True), np.load(ref_path, allow_pickle=True)
+    assert sorted(a.files) == sorted(b.files)
+    for k in a.files:
+        assert a[k].dtype == b[k].dtype and a[k].shape == b[k].shape, k
+        assert np.array_equal(a[k], b[k]), k

@@ -25,6 +25,9 @@ Fixtures (sizes chosen so the whole script runs in a few minutes):
 * ``config_cases.json`` -- ``ConvectionConfig`` on 300 seeded configurations:
   outcome class, warning classes, ``canonical()``.
 * ``ckpt/t_0.125000.npz`` -- a state written by ``specmc.io.checkpoint.save``.
+* ``tala_ops_16x12.npz`` -- the TALA Stokes operators (``TalaStokes``,
+  ``TalaFreeOperator``) and the TALA temperature operator, preconditioner and
+  adiabatic source on one seeded state.
 * ``coupled_ops_16x12.npz`` -- ``eta_of``, ``FreeSchurOperator.matvec``, the
   assembled Schur matrix and the BFBT preconditioner action for one seeded
   state (pins the coupled operator, including its partner half).
@@ -152,6 +155,39 @@ def coupled_ops_case(S):
         b=op.rhs_schur(th), Pv=P.apply(v), G=G, eta_c=fop.eta_c,
         psi=psi, om=om)
     print('coupled_ops_16x12 written', flush=True)
+
+
+def tala_ops_case(S):
+    """The TALA operators (stokes/stokes_tala.py) on one seeded state of the
+    eta_T model with Di = 0.7: eta, the L^(rho) Green functions, the assembled
+    Schur matrix, the matrix-free action, the rho_bar^2 right-hand side, the
+    unpacked (Psi, omega), and after one step the temperature operator, its
+    rho_bar preconditioner and the adiabatic source."""
+    from specmc.stokes.stokes_tala import TalaFreeOperator, TalaStokes
+    api = S.api
+    cfg = S.ConvectionConfig(Ra=1e4, Nx=16, Nz=12, viscosity_model='eta_T',
+                             compressibility='tala', dissipation_number=0.7,
+                             precond='legacy')
+    m = api.build_model(cfg)
+    rng = np.random.default_rng(3)
+    th = m.seed(amp=0.2, m=1, n=1) + 0.05 * (rng.standard_normal((m.Nk, m.Nz))
+                                            + 1j * rng.standard_normal((m.Nk, m.Nz)))
+    eta = m.eta_of(th)
+    op = TalaStokes(m, eta)
+    fop = TalaFreeOperator(m, eta, op_template=op)
+    v = rng.standard_normal(m.Nk * m.Nz) + 1j * rng.standard_normal(m.Nk * m.Nz)
+    psi_v, om_v, _ = op.unpack_schur(v)
+    th1 = m.step(th, 2e-5)
+    tv = rng.standard_normal(m.Nk * m.Nz) + 1j * rng.standard_normal(m.Nk * m.Nz)
+    rec = dict(that=th, eta=eta, v=v, Av=fop.matvec(v), A=op.assemble_schur(),
+               b=op.rhs_schur(th), G=np.array([op.green(i) for i in range(m.Nk)]),
+               psi_v=psi_v, om_v=om_v, rho_grid=m.rho_grid, rho_c=m.rho_c,
+               rho2_c=m.rho2_c, tala_a=np.float64(m.tala_a), dt=np.float64(2e-5),
+               that1=th1, tv=tv, theta_Av=m.theta.matvec(tv),
+               theta_Pv=m.theta.precond(tv),
+               adiabatic=m.theta._tala_adiabatic_source(m.project_mirror(th)))
+    np.savez_compressed(os.path.join(HERE, 'tala_ops_16x12.npz'), **rec)
+    print('tala_ops_16x12 written', flush=True)
 
 
 def pv_calibration_case(S):
@@ -291,6 +327,8 @@ def main(ref_root, only=()):
         config_case(S)
     if not only or 'checkpoint' in only:
         checkpoint_case(S)
+    if not only or 'tala_ops' in only:
+        tala_ops_case(S)
     base = dict(Ra=1e4, Nx=32, Nz=24)
     # configuration 1 of the headline table: isoviscous, march to t = 1e-3
     mc('const_32x24', dict(base, viscosity_model='const'), 25,
@@ -323,6 +361,20 @@ def main(ref_root, only=()):
                dict(base, viscosity_model='arrhenius', deta_T=1e3,
                     arrhenius_V=0.5, reference_anchor='D'),
                6, ('noise', 1e-2, 8, 8, 42), S)
+    # the TALA operator route (compressibility='tala', Di = 0.25): the
+    # velocity division on every route, the rho_bar-weighted temperature
+    # equation on eta_z / eta_T, the TALA Schur operator on the legacy route
+    tala = dict(base, compressibility='tala', dissipation_number=0.25)
+    mc('tala_const_32x24', dict(tala, viscosity_model='const'), 8,
+       ('seed', 3e-2, 1, 1), S)
+    mc('tala_etaz_32x24', dict(tala, viscosity_model='eta_z', deta_T=100.0), 8,
+       ('seed', 3e-2, 1, 1), S)
+    mc('tala_etaT_32x24', dict(tala, viscosity_model='eta_T', precond='legacy'), 8,
+       ('seed', 3e-2, 1, 1), S)
+    mc('tala_arrhenius_32x24',
+       dict(tala, viscosity_model='arrhenius', precond='legacy', deta_T=1e3,
+            arrhenius_Ts=1.0, eta_min=1e-3, eta_max=1.0, internal_heating=1.0),
+       6, ('noise', 1e-2, 8, 8, 99), S)
     # configuration 2 grid, a few steps (the oracle of the bench workload)
     mc('etaT_64x96', dict(Ra=1e4, Nx=64, Nz=96,
                                   viscosity_model='eta_T'), 6,

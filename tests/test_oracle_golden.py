@@ -64,8 +64,57 @@ def test_coupled_operator():
     assert _rel(psi, g["psi"]) < 1e-9 and _rel(om, g["om"]) < 1e-9
 
 
+def test_tala_operators():
+    """The TALA route (compressibility='tala', Di = 0.7) operator by operator:
+    reference state, L^(rho) Green functions, the distributed-form Schur
+    matrix and its matrix-free action, the rho_bar^2 right-hand side, the
+    unpacking, and the rho_bar-weighted temperature operator, preconditioner
+    and adiabatic source after one step."""
+    from specmc_gb300.config import ConvectionConfig
+    g = _load("tala_ops_16x12.npz")
+    cfg = ConvectionConfig(Ra=1e4, Nx=16, Nz=12, viscosity_model="eta_T", compressibility="tala",
+                           dissipation_number=0.7, precond="legacy")
+    m = O.build(cfg)
+    assert m.tala and m.tala_a == g["tala_a"].item()
+    assert np.array_equal(m.rho_grid, g["rho_grid"])
+    assert _rel(m.rho_c, g["rho_c"]) < 1e-15 and _rel(m.rho2_c, g["rho2_c"]) < 1e-15
+    eta = m.eta_of(g["that"])
+    assert _rel(eta, g["eta"]) < 1e-14
+    assert _rel(np.array(m.Gt), g["G"]) < 1e-14
+    Ms = m.eta_mats(eta)
+    assert _rel(m.assemble_schur(Ms), g["A"]) < 1e-13
+    assert _rel(m.schur_matvec(Ms, g["v"]), g["Av"]) < 1e-13
+    assert _rel(m.rhs_schur(g["that"]), g["b"]) < 1e-15
+    psi, om = m.unpack(g["v"])
+    assert _rel(psi, g["psi_v"]) < 1e-14 and _rel(om, g["om_v"]) < 1e-15
+    # one step: the Stokes defect correction (1e-8) and the temperature
+    # FGMRES (1e-10) stop at tolerances, so the state agrees to their size
+    th1 = m.step(g["that"], g["dt"].item())
+    assert _rel(th1, g["that1"]) < 1e-9
+    # the frozen velocity of that step is the same to the last bit (the
+    # Stokes solve of the first step is direct from a fresh factorisation)
+    assert _rel(m.theta_matvec(g["tv"]), g["theta_Av"]) < 1e-13
+    assert _rel(m.theta_precond(g["tv"]), g["theta_Pv"]) < 1e-13
+    assert _rel(m.tala_adiabatic(m.project_mirror(g["that"])), g["adiabatic"]) < 1e-13
+
+
+def test_tala_reduces_to_boussinesq_at_zero_Di():
+    """At Di = 0 the TALA operators are the Boussinesq ones (the limit the
+    reference's own TALA self-test checks, stokes_tala.py:523-548)."""
+    from specmc_gb300.config import ConvectionConfig
+    g = _load("coupled_ops_16x12.npz")
+    mb = O.CoupledModel(Nx=16, Nz=12, deta_T=1000.0)
+    mt = O.CoupledModel(Nx=16, Nz=12, deta_T=1000.0, compressibility="tala")
+    eta = mb.eta_of(g["that"])
+    Mb, Mt = mb.eta_mats(eta), mt.eta_mats(eta)
+    assert _rel(mt.assemble_schur(Mt), mb.assemble_schur(Mb)) < 1e-12
+    assert _rel(mt.schur_matvec(Mt, g["v"]), mb.schur_matvec(Mb, g["v"])) < 1e-12
+    assert np.array_equal(mt.rhs_schur(g["that"]), mb.rhs_schur(g["that"]))
+
+
 CASES = ["const_32x24", "etaz_32x24", "etaT_32x24", "etaT_bfbt_32x24",
-         "heated_2to1_32x24", "arrhenius_32x24", "smooth_32x24", "arrhenius_pv_32x24"]
+         "heated_2to1_32x24", "arrhenius_32x24", "smooth_32x24", "arrhenius_pv_32x24",
+         "tala_const_32x24", "tala_etaz_32x24", "tala_etaT_32x24", "tala_arrhenius_32x24"]
 DIAG_TOL = {}
 
 

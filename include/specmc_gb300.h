@@ -31,11 +31,16 @@
 extern "C" {
 #endif
 
-#define SMC_ABI_VERSION 2
+#define SMC_ABI_VERSION 3
 
 enum smc_model { SMC_MODEL_CONST = 0, SMC_MODEL_ETA_Z = 1, SMC_MODEL_ETA_T = 2 };
 enum smc_precond { SMC_PRECOND_LEGACY = 0, SMC_PRECOND_BFBT = 1 };
 enum smc_precision { SMC_FP64 = 0, SMC_MIXED = 1 };
+/* ConvectionConfig.compressibility (specmc/config.py:159-179): the
+ * Boussinesq equations, or the truncated anelastic liquid approximation with
+ * the reference density rho_bar = exp((1 - z) Di) of the run's
+ * dissipation_number (core/rbc_galerkin.py:288-312) */
+enum smc_compressibility { SMC_BOUSSINESQ = 0, SMC_TALA = 1 };
 enum smc_mem { SMC_HOST = 0, SMC_DEVICE = 1 };
 enum smc_transform {
   SMC_GRID = 0,       /* (Nk,Nz) coeffs -> (Nx,Nz) values   rbc_galerkin.py:322 */
@@ -73,6 +78,14 @@ typedef struct smc_config {
    * (physics/reference_state.py:277-364, done by the caller) */
   double arrhenius_E;
   double arrhenius_V;
+  /* enum smc_compressibility.  SMC_TALA: u = curl(Psi) / rho_bar on every
+   * model (rbc_galerkin.py:355-372); the rho_bar-weighted temperature
+   * equation with the adiabatic source on ETA_Z / ETA_T
+   * (implicit_theta.py:159-178, :332-493); the TALA Schur operator
+   * (stokes/stokes_tala.py) on the legacy route of ETA_T.  SMC_TALA needs
+   * precision SMC_FP64 and, on ETA_T, precond SMC_PRECOND_LEGACY (the
+   * reference has no TALA form of the BFBT preconditioner, config.py:462-470). */
+  int compressibility;
 } smc_config;
 
 typedef struct smc_handle smc_handle;

@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libspecmc_gb300.so")
 SOURCES = ("smc_spectral.cu", "smc_dense.cu", "smc_schur.cu", "smc_krylov.cu",
-           "smc_pseudo.cu", "smc_fastops.cu", "smc_engine.cu", "smc_noalloc.cu", "smc_runtime.cu")
+           "smc_pseudo.cu", "smc_fastops.cu", "smc_engine.cu", "smc_noalloc.cu", "smc_tala.cu",
+           "smc_runtime.cu")
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
               "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "-I", os.path.join(ROOT, "include")]
@@ -26,8 +27,9 @@ SMC_HOST, SMC_DEVICE = 0, 1
 SMC_MODEL_CONST, SMC_MODEL_ETA_Z, SMC_MODEL_ETA_T = 0, 1, 2
 SMC_PRECOND_LEGACY, SMC_PRECOND_BFBT = 0, 1
 SMC_FP64, SMC_MIXED = 0, 1
+SMC_BOUSSINESQ, SMC_TALA = 0, 1
 SMC_GRID, SMC_COEFFS, SMC_SYNTH_PAD, SMC_TRUNC_PAD = 0, 1, 2, 3
-SMC_ABI_VERSION = 2
+SMC_ABI_VERSION = 3
 
 
 def _nvcc():
@@ -87,6 +89,7 @@ class SmcConfig(ctypes.Structure):
         ("stokes_restart", ctypes.c_int), ("stokes_maxiter", ctypes.c_int),
         ("precision", ctypes.c_int), ("device", ctypes.c_int),
         ("arrhenius_E", ctypes.c_double), ("arrhenius_V", ctypes.c_double),
+        ("compressibility", ctypes.c_int),
     ]
 
 

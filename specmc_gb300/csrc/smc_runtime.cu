@@ -27,6 +27,7 @@
 #include "smc_pseudo.cuh"
 #include "smc_fastops.cuh"
 #include "smc_engine.cuh"
+#include "smc_tala.cuh"
 
 namespace smc {
 
@@ -339,6 +340,17 @@ struct Model {
   double2 *dSb, *dSx, *dSr, *dSdx, *dSAx, *dSw, *dSf2, *dSf3, *dSf4, *dSt[4], *dSolveWork;
   double2 *dBfbtRhs, *dBfbtProfC;
   double* dBfbtHw;
+  // TALA (compressibility SMC_TALA): rho_bar on the CGL nodes and its
+  // inverse, the coefficients of rho_bar, product matrices of rho_bar and
+  // rho_bar^2, Mrho Vi, the L^(rho) Green operators and work buffers
+  bool tala = false;
+  double tala_a = 0.0;
+  double *dRho = nullptr, *dRhoInv = nullptr, *dRhoC = nullptr, *dMrho = nullptr,
+         *dMrhoVi = nullptr, *dD2rho = nullptr, *dGt = nullptr;
+  double2 *dTalaF = nullptr, *dTalaT = nullptr, *dTalaRhs = nullptr, *dTalaAd = nullptr;
+  double *dTalaThG = nullptr, *dTalaAdG = nullptr;
+  // the Green operators of the coupled Stokes operator (TALA: of L^(rho))
+  const double* green_coupled() const { return tala ? dGt : dG; }
   // pseudo-spectral mult_eta
   PsPlan psplan;
   double* dPsE = nullptr;
@@ -456,7 +468,10 @@ struct Model {
     for (auto& s : lam_slots)
       if (!s.used) { slot = &s; break; }
     ProfScope ps(ctx, "theta_lu_build");
-    tau_ops(ctx, dD2, dkx, lam, slot->LU, N, Nk);
+    // TALA temperature step: D2 - diag(k^2 + lam rho_j) (implicit_theta.py:471-493);
+    // the isoviscous model keeps the constant-coefficient ChebTau operator
+    if (tala && cfg.model != SMC_MODEL_CONST) tala_theta_ops(ctx, dD2, dkx, lam, dRho, slot->LU, N, Nk);
+    else tau_ops(ctx, dD2, dkx, lam, slot->LU, N, Nk);
     lu_small_batched(ctx, slot->LU, slot->piv, nullptr, N, Nk);
     if (fast) {
       green_from_lu(ctx, slot->LU, slot->piv, slot->Ginv, N, Nk);
@@ -546,6 +561,7 @@ struct Model {
     tau_ops(ctx, dD2, dkx, 0.0, dLU0, N, Nk);
     lu_small_batched(ctx, dLU0, dPiv0, nullptr, N, Nk);
     green_from_lu(ctx, dLU0, dPiv0, dG, N, Nk);
+    if (cfg.compressibility == SMC_TALA) setup_tala();
 
     law.L = std::log(cfg.deta_T);
     law.Ts = cfg.model == SMC_MODEL_ETA_T ? cfg.arrhenius_Ts : 0.0;
@@ -734,6 +750,74 @@ struct Model {
       }
     }
     SMC_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  // The TALA reference state (physics/compressibility.py:138-227, gamma = 1;
+  // core/rbc_galerkin.py:298-306): a = -Di, rho_bar = exp((1 - z) Di) (exactly
+  // 1 at Di = 0), its coefficients Vi rho_bar ([1, 0, ...] at Di = 0) and those
+  // of rho_bar^2; the product matrices Mrho, Mrho Vi (temperature equation)
+  // and M(rho_bar^2) (buoyancy), and on the coupled model the Green operators
+  // of L^(rho) = D2 - a D - k^2 (stokes/stokes_tala.py:226-240).
+  void setup_tala() {
+    tala = true;
+    const double Di = cfg.dissipation_number;
+    tala_a = -Di / 1.0;
+    auto prof = [&](double d) {
+      std::vector<double> r(N, 1.0);
+      if (d != 0.0)
+        for (int j = 0; j < N; ++j) r[j] = std::exp((1.0 - hb->z[j]) * d / 1.0);
+      return r;
+    };
+    auto coef = [&](double d) {
+      std::vector<double> c(N, 0.0);
+      if (d == 0.0) { c[0] = 1.0; return c; }
+      std::vector<double> r = prof(d);
+      for (int p = 0; p < N; ++p) {
+        double s = 0.0;
+        for (int j = 0; j < N; ++j) s += hb->Vi[(size_t)p * N + j] * r[j];
+        c[p] = s;
+      }
+      return c;
+    };
+    // exact truncated Chebyshev product matrix (stokes/vv_stokes.py:81-109)
+    auto cheb_mult = [&](const std::vector<double>& a) {
+      std::vector<double> M((size_t)N * N);
+      for (int p = 0; p < N; ++p)
+        for (int q = 0; q < N; ++q) {
+          double s = 0.0;
+          if (p >= q) s += a[p - q];
+          if (p + q < N) s += a[p + q];
+          if (p > 0 && q >= p) s += a[q - p];
+          M[(size_t)p * N + q] = 0.5 * s;
+        }
+      return M;
+    };
+    std::vector<double> rho = prof(Di), rinv(N), rc = coef(Di), r2c = coef(2.0 * Di);
+    for (int j = 0; j < N; ++j) rinv[j] = 1.0 / rho[j];
+    std::vector<double> Mr = cheb_mult(rc), MrVi((size_t)N * N, 0.0);
+    for (int p = 0; p < N; ++p)
+      for (int m = 0; m < N; ++m) {
+        const double a = Mr[(size_t)p * N + m];
+        for (int q = 0; q < N; ++q) MrVi[(size_t)p * N + q] += a * hb->Vi[(size_t)m * N + q];
+      }
+    dRho = mem.upload(rho); dRhoInv = mem.upload(rinv); dRhoC = mem.upload(rc);
+    dMrho = mem.upload(Mr); dMrhoVi = mem.upload(MrVi); dD2rho = mem.upload(cheb_mult(r2c));
+    if (cfg.model != SMC_MODEL_CONST) {
+      dTalaThG = mem.alloc<double>((size_t)Np * N);
+      dTalaAdG = mem.alloc<double>((size_t)Np * N);
+      dTalaAd = mem.alloc<double2>(n);
+    }
+    if (cfg.model == SMC_MODEL_ETA_T) {
+      double* lu = mem.alloc<double>(Nk * NN);
+      int* piv = mem.alloc<int>(Nk * N);
+      dGt = mem.alloc<double>(Nk * NN);
+      tala_green_ops(ctx, dD, dD2, dkx, tala_a, lu, N, Nk);
+      lu_small_batched(ctx, lu, piv, nullptr, N, Nk);
+      green_from_lu(ctx, lu, piv, dGt, N, Nk);
+      dTalaF = mem.alloc<double2>(5 * n);
+      dTalaT = mem.alloc<double2>(6 * n);
+      dTalaRhs = mem.alloc<double2>(n);
+    }
   }
 
   // reduced operator LU from real Chebyshev coefficients `coef` (complex
@@ -1124,7 +1208,7 @@ struct Model {
   double dense_bytes() const {
     const double blk = (double)(2 * Nk - 1) * NN * 16.0;
     const long long nblk = (n + 63) / 64;
-    return 5.0 * blk + (double)n * n * 16.0 + 2.0 * nblk * 64 * 64 * 16.0 + 8.0 * n;
+    return (tala ? 6.0 : 5.0) * blk + (double)n * n * 16.0 + 2.0 * nblk * 64 * 64 * 16.0 + 8.0 * n;
   }
   bool dense_feasible() const { return dSchur || dense_bytes() <= dense_cap_bytes; }
   void ensure_dense() {
@@ -1135,7 +1219,7 @@ struct Model {
                                " complex entries does not fit in device memory; use the "
                                "BFBT route (precond = SMC_PRECOND_BFBT)");
     if (!dMd) dMd = mem.alloc<double2>((size_t)(2 * Nk - 1) * NN);
-    dAsmWork = mem.alloc<double2>((size_t)4 * (2 * Nk - 1) * NN);
+    dAsmWork = mem.alloc<double2>((size_t)(tala ? 5 : 4) * (2 * Nk - 1) * NN);
     dSchur = mem.alloc<double2>((size_t)n * n);
     dSchurPiv = mem.alloc<int>(n);
     dSchurPerm = mem.alloc<int>(n);
@@ -1154,6 +1238,7 @@ struct Model {
 
   // FreeSchurOperator.matvec at the current Md (lagged_stokes.py:202-220)
   void schur_matvec(const double2* v, double2* out) {
+    if (tala) { schur_matvec_tala(v, out); return; }
     // algorithmic work of the dense form: 4 mult_eta x (Nk^2 + Nk(Nk-1)/2) N^2
     // complex MACs (8 flops each)
     ProfScope ps(ctx, "schur_matvec", 4.0 * 8.0 * ((double)Nk * Nk + 0.5 * Nk * (Nk - 1)) * NN, 0);
@@ -1180,8 +1265,51 @@ struct Model {
     schur_combine(ctx, dSt[0], dSt[1], dSt[2], dSt[3], v, dD, dD2, dV, dkx, out, Nk, N);
   }
 
+  // TalaFreeOperator.matvec (stokes/stokes_tala.py:402-466): t = mult_eta(v)
+  // and one mult_eta per distinct (D^b, k^p) image of g = G v, odd powers
+  // of the input wavenumber with the flipped partner sign
+  void schur_matvec_tala(const double2* v, double2* out) {
+    ProfScope ps(ctx, "schur_matvec", 6.0 * 8.0 * ((double)Nk * Nk + 0.5 * Nk * (Nk - 1)) * NN, 0);
+    zop(dGt, NN, v, dSw);                                  // g = G v
+    double2* F01 = dTalaF;                                 // k g
+    double2* F02 = dTalaF + n;                             // k^2 g
+    double2* F10 = dTalaF + 2 * n;                         // D g
+    double2* F11 = dTalaF + 3 * n;                         // k D g
+    double2* F20 = dTalaF + 4 * n;                         // D2 g
+    KFactor k1; k1.kpow = 1;
+    KFactor k2; k2.kpow = 2;
+    vec_scaled_modes(ctx, dSw, F01, Nk, N, k1, dkx, 0, 0);
+    vec_scaled_modes(ctx, dSw, F02, Nk, N, k2, dkx, 0, 0);
+    zop(dD, 0, dSw, F10);
+    zop(dD, 0, dSw, F11, k1);
+    zop(dD2, 0, dSw, F20);
+    const double2* fin[6] = {v, F01, F02, F10, F11, F20};
+    const double sgn[6] = {-1.0, +1.0, -1.0, -1.0, +1.0, -1.0};   // partner sign, flipped for odd k powers
+    double2* T[6];
+    for (int q = 0; q < 6; ++q) T[q] = dTalaT + q * n;
+    if (use_dense_mult) {
+      md_current();
+      for (int q = 0; q < 6; ++q) smc::mult_eta(ctx, dMd, fin[q], T[q], Nk, N, sgn[q], nullptr);
+    } else {
+      for (int q0 = 0; q0 < 6; q0 += 4) {
+        PsJobs j;
+        const int nb = std::min(4, 6 - q0);
+        for (int q = 0; q < nb; ++q) { j.f[q] = fin[q0 + q]; j.out[q] = T[q0 + q]; j.sgn[q] = sgn[q0 + q]; }
+        ps_mult_eta(ctx, psplan, dPsE, j, nb, dPsFv, dPsHv);
+      }
+    }
+    tala_schur_combine(ctx, T[0], T[1], T[2], T[3], T[4], T[5], v, dD, dD2, dV, dkx, tala_a, out,
+                       Nk, N);
+  }
+
   void rhs_schur(const double2* th, double2* b) {
     KFactor f; f.cre = 0.0; f.cim = cfg.Ra; f.kpow = 1;
+    if (tala) {
+      // i k Ra (rho_bar^2 theta) (stokes/stokes_tala.py:313-324)
+      zop(dD2rho, 0, th, dTalaRhs);
+      vec_scaled_modes(ctx, dTalaRhs, b, Nk, N, f, dkx, 1, 1);
+      return;
+    }
     vec_scaled_modes(ctx, th, b, Nk, N, f, dkx, 1, 1);
   }
 
@@ -1190,7 +1318,8 @@ struct Model {
     md_current();
     {
       ProfScope ps(ctx, "schur_assembly");
-      assemble_schur(ctx, dMd, dD, dD2, dG, dV, dkx, dSchur, Nk, N, dAsmWork);
+      if (tala) assemble_schur_tala(ctx, dMd, dD, dD2, dGt, dV, dkx, tala_a, dSchur, Nk, N, dAsmWork);
+      else assemble_schur(ctx, dMd, dD, dD2, dG, dV, dkx, dSchur, Nk, N, dAsmWork);
     }
     {
       // algorithmic work: complex LU, 8/3 n^3 real flops
@@ -1447,8 +1576,10 @@ struct Model {
     eta_operator();
     if (cfg.precond == SMC_PRECOND_BFBT || fast) bfbt_solve(th, dSx);
     else legacy_solve(th, dSx);
-    zop(dG, NN, dSx, psi);
-    vec_axpby(ctx, om, make_double2(-1.0, 0.0), dSx, make_double2(0.0, 0.0), n);
+    zop(green_coupled(), NN, dSx, psi);
+    // omega = -v (TALA: -v / rho_bar column by column, stokes_tala.py:327-340)
+    if (tala) scale_cols(ctx, dSx, dRhoInv, -1.0, om, Nk, N);
+    else vec_axpby(ctx, om, make_double2(-1.0, 0.0), dSx, make_double2(0.0, 0.0), n);
   }
   bool have_last_eta = false;
 
@@ -1487,6 +1618,7 @@ struct Model {
     synth(psi, dVD, KFactor(), ux, Nx, sp[4]);
     KFactor f; f.cre = 0.0; f.cim = -1.0; f.kpow = 1;       // -i k psi
     synth(psi, dV, f, uz, Nx, sp[4]);
+    if (tala) grid_div_rho(ctx, ux, uz, dRho, (long long)Nx * N, N);   // u = curl(Psi) / rho_bar
   }
 
   double cfl_dt(const double2* th, double safety, double dtmax, double dtmin) {
@@ -1576,7 +1708,8 @@ struct Model {
     grid_advect_product(ctx, gr[0], gr[1], gr[2], gr[3], gr[4], (long long)Np * N);
     AnaJob a{gr[4], sp[11]};
     analysis_x(ctx, &a, 1, Nk, N, Np, dtwNp, 1.0 / Np);
-    theta_combine(ctx, v, sp[11], dD2, dVi, dV, dkx, a0, out, Nk, N);
+    if (tala) tala_theta_combine(ctx, v, sp[11], dMrho, dMrhoVi, dD2, dV, dkx, a0, out, Nk, N);
+    else theta_combine(ctx, v, sp[11], dD2, dVi, dV, dkx, a0, out, Nk, N);
   }
 
   void set_step(double dt, bool have_p, double dtp) {
@@ -1614,7 +1747,18 @@ struct Model {
     set_step(dt, have_prev, dt_prev);
     {
       ProfScope psa(ctx, "theta_rhs");
-      theta_rhs(ctx, th2, dPrev, ps, phi, dkx, b0, b1, cfg.internal_heating, dKb, Nk, N);
+      if (tala) {
+        // adiabatic source rho_bar u_z [1 - Di (1 - z + theta)] on the padded
+        // grid, truncated back with its tau rows zeroed (implicit_theta.py:336-350)
+        synth(th2, dV, KFactor(), dTalaThG, Np, sp[12]);
+        tala_adiabatic_grid(ctx, gr[1], dTalaThG, dRho, dz, cfg.dissipation_number, dTalaAdG,
+                            (long long)Np * N, N);
+        analyze(dTalaAdG, Np, dTalaAd, sp[12], KFactor(), 1);
+        tala_theta_rhs(ctx, th2, dPrev, dMrho, dRhoC, dTalaAd, phi, b0, b1, cfg.internal_heating,
+                       dKb, Nk, N);
+      } else {
+        theta_rhs(ctx, th2, dPrev, ps, phi, dkx, b0, b1, cfg.internal_heating, dKb, Nk, N);
+      }
     }
     Op A = [&](const double2* v, double2* o) { theta_matvec(v, o); };
     LamSlot* Lp = &lam_lu(a0);
@@ -1863,6 +2007,17 @@ void validate(const smc_config* c) {
       (c->model != SMC_MODEL_ETA_T || !(c->arrhenius_Ts > 0.0) || !std::isfinite(c->arrhenius_E)))
     throw std::runtime_error("arrhenius_V > 0 (pV law) needs model ETA_T, arrhenius_Ts > 0 and a finite "
                              "calibrated arrhenius_E");
+  if (c->compressibility != SMC_BOUSSINESQ && c->compressibility != SMC_TALA)
+    throw std::runtime_error("unknown compressibility");
+  if (c->compressibility == SMC_TALA) {
+    if (!std::isfinite(c->dissipation_number) || c->dissipation_number < 0.0)
+      throw std::runtime_error("compressibility TALA needs a finite dissipation_number >= 0");
+    if (c->precision != SMC_FP64)
+      throw std::runtime_error("compressibility TALA runs the FP64 form only (precision SMC_FP64)");
+    if (c->model == SMC_MODEL_ETA_T && c->precond != SMC_PRECOND_LEGACY)
+      throw std::runtime_error("compressibility TALA with precond BFBT: the spectral BFBT model is "
+                               "Boussinesq-only; use SMC_PRECOND_LEGACY (config.py:462-470)");
+  }
 }
 
 }  // namespace

@@ -62,7 +62,14 @@ class GpuModel:
                  symmetrize=True, lag=16, K=3, defect_tol=1e-8, max_K=8,
                  eta_drift_tol=0.1, stokes_rtol=1e-8, theta_rtol=1e-10,
                  theta_maxiter=200, theta_restart=40, stokes_restart=80,
-                 stokes_maxiter=800, device=0, form="plain", **_ignored):
+                 stokes_maxiter=800, compressibility="boussinesq", device=0, form="plain",
+                 **_ignored):
+        from .config import normalize_compressibility
+        comp = normalize_compressibility(compressibility)
+        if comp not in ("boussinesq", "tala"):
+            raise NotImplementedError("compressibility=%r is not implemented" % (compressibility,))
+        if comp == "tala" and str(form).lower() == "mixed":
+            raise NotImplementedError("compressibility='tala' runs the plain (FP64) form only")
         lib = _lib.load()
         c = _lib.SmcConfig()
         lib.smc_config_defaults(ctypes.byref(c))
@@ -99,6 +106,7 @@ class GpuModel:
         c.theta_maxiter, c.theta_restart = int(theta_maxiter), int(theta_restart)
         c.stokes_restart, c.stokes_maxiter = int(stokes_restart), int(stokes_maxiter)
         c.device = int(device)
+        c.compressibility = _lib.SMC_TALA if comp == "tala" else _lib.SMC_BOUSSINESQ
         form = str(form).lower()
         if form not in ("plain", "mixed"):
             raise ValueError("form must be 'plain' (FP64, the reference algorithm) or "
@@ -119,6 +127,21 @@ class GpuModel:
         self.Nk = len(self.kx)
         self.Np = 2 * self.Nx
         self.dealias = True
+        # the TALA reference state under the reference's names
+        # (core/rbc_galerkin.py:288-312); the library builds the same profiles
+        self.compressibility = comp
+        self.tala_active = comp == "tala"
+        if self.tala_active:
+            from . import compressibility as COMP
+            Di = self.dissipation_number
+            self.tala_a = COMP.a_coeff(Di)
+            self.rho_grid = COMP.rho_bar_grid(self.z, Di)
+            self.rho_c = COMP.rho_bar_coeffs(self.Vi, self.z, Di)
+            self.rho2_c = COMP.rho_bar_coeffs(self.Vi, self.z, 2.0 * Di)
+            self.tala_record = COMP.record(Di)
+        else:
+            self.tala_a = 0.0
+            self.rho_grid = self.rho_c = self.rho2_c = self.tala_record = None
 
     # ------------------------------------------------------------ plumbing
     def close(self):
@@ -324,7 +347,9 @@ class GpuModel:
         d = dict(mode=type(self).__name__, backend="gb300", form=self.form, Nx=self.Nx, Nz=self.Nz,
                  Ra=self.Ra, Lx=self.Lx, deta_T=self.deta_T,
                  internal_heating=self.internal_heating,
-                 dissipation_number=self.dissipation_number)
+                 dissipation_number=self.dissipation_number,
+                 compressibility=self.compressibility, tala_active=self.tala_active,
+                 tala_a=self.tala_a)
         d.update(self.counters())
         return d
 

@@ -107,8 +107,12 @@ def test_api_dispatch_table():
     assert d["model_class"] == "RBCCoupled" and d["numerics"]["DTMAX"] == 4e-5
     spec = api.model_spec(ConvectionConfig(defect_tol=0.0, K=3))
     assert spec["kwargs"]["defect_tol"] is None
+    tala = ConvectionConfig(compressibility="tala", precond="legacy", dissipation_number=0.5)
+    assert api.model_spec(tala)["kwargs"]["compressibility"] == "tala"
+    # the TALA route is the FP64 form's: the mixed form refuses it before any
+    # device work
     with pytest.raises(NotImplementedError):
-        api.model_spec(ConvectionConfig(compressibility="tala"))
+        api.build_model(tala, form="mixed")
 
 
 def test_config_and_model_spec_match_reference_on_seeded_cases():
@@ -116,8 +120,7 @@ def test_config_and_model_spec_match_reference_on_seeded_cases():
     configurations (tests/golden/config_cases.json, written by the reference's
     own ConvectionConfig / api.model_spec): the same outcome (valid, ValueError,
     NotImplementedError), the same warnings, the same canonical() and the same
-    model / builder / constructor kwargs and api.describe().  TALA is the one documented
-    difference: the reference builds it, here it raises NotImplementedError."""
+    model / builder / constructor kwargs and api.describe(), TALA included."""
     import json
     from specmc_gb300 import api
     from specmc_gb300.config import ConvectionConfig
@@ -139,10 +142,6 @@ def test_config_and_model_spec_match_reference_on_seeded_cases():
         assert cfg.canonical() == c["canonical"], c["kw"]
         with warnings.catch_warnings():
             warnings.simplefilter("ignore")            # validate() repeats the warnings above
-            if str(cfg.compressibility).lower() == "tala":
-                with pytest.raises(NotImplementedError):
-                    api.model_spec(cfg)
-                continue
             sp = api.model_spec(cfg)
             d = json.loads(json.dumps(api.describe(cfg), default=str))
         assert (sp["model"], sp["builder"], sp["kwargs"]) == (

@@ -35,17 +35,41 @@ def test_config_defaults_roundtrip():
     assert c.theta_restart == 40 and c.stokes_restart == 80 and c.stokes_maxiter == 800
 
 
-def test_create_reports_errors_not_crashes():
-    """A bad config is a hard error with a message (no GPU needed)."""
+BAD_CONFIGS = [
+    (dict(Nx=3), b"Nx"),
+    (dict(Nx=30, Nz=3), b"Nx, Nz"),
+    (dict(Nx=34 + 1), b"even"),
+    (dict(abi_version=1), b"abi_version"),
+    (dict(model=7), b"unknown model"),
+    (dict(Ra=-1.0), b"positive"),
+    (dict(eta_min=2.0, eta_max=1.0), b"eta window"),
+    (dict(lag=0), b"defect-correction"),
+    (dict(theta_restart=0), b"restart"),
+    (dict(precision=5), b"precision"),
+    (dict(arrhenius_V=-1.0), b"arrhenius_V"),
+    (dict(arrhenius_V=0.5, arrhenius_Ts=0.0), b"pV law"),
+    (dict(compressibility=4), b"compressibility"),
+    (dict(compressibility=1, dissipation_number=-0.5), b"dissipation_number"),
+    (dict(compressibility=1, precision=1), b"FP64 form only"),
+    (dict(compressibility=1, precond=1), b"Boussinesq-only"),
+]
+
+
+@pytest.mark.parametrize("fields,msg", BAD_CONFIGS)
+def test_create_reports_errors_not_crashes(fields, msg):
+    """A bad config is a hard error with a message, raised before any device
+    work (no GPU needed)."""
     import ctypes
     from specmc_gb300 import _lib
     lib = _lib.load()
     c = _lib.SmcConfig()
     lib.smc_config_defaults(ctypes.byref(c))
-    c.Nx = 3
+    for k, v in fields.items():
+        setattr(c, k, v)
     h = ctypes.c_void_p()
     assert lib.smc_create(ctypes.byref(c), ctypes.byref(h)) < 0
-    assert b"Nx" in lib.smc_last_error()
+    assert msg in lib.smc_last_error(), lib.smc_last_error()
+    assert not h.value
 
 
 def test_config_validation_mirrors_reference():

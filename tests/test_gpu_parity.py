@@ -134,6 +134,22 @@ def test_march_adaptive_on_device_matches_stepwise(gb):
     assert abs(d["urms"] - 6.7774209783) < 1e-8
 
 
+def test_isoviscous_regression_target(gb):
+    """The reference's frozen isoviscous regression target
+    (specmc/physics/viscosity.py:150-151: Ra 1e4, 64x48, t = 0.25,
+    Nu 4.885140, Vrms 42.872720), marched from the default seed (amp 1e-3)
+    with the legacy CFL protocol it is stored under (safety 0.4, dtmax 5e-6,
+    specmc/api.py:172-175), about 50 500 steps in one native call: Nu_top and
+    urms to 1e-6 (the reference itself reproduces it to 4e-7 / 2e-8)."""
+    api, CC = gb
+    m = api.build_model(CC(viscosity_model="const", Ra=1e4, Nx=64, Nz=48))
+    s, info = api.march_adaptive(m, m.seed(), tstop=0.25, safety=0.4, dtmax=5e-6)
+    assert info["steps"] >= 50000 and info["t"] >= 0.25
+    d = m.diagnostics(s)
+    assert abs(d["Nu_top"] - 4.885140) <= 1e-6 * 4.885140, d["Nu_top"]
+    assert abs(d["urms"] - 42.872720) <= 1e-6 * 42.872720, d["urms"]
+
+
 def test_oracle_parity_64x96_coupled(gb):
     """The headline grid (eta_T 64x96): GPU vs the reference fixture."""
     api, CC = gb

@@ -61,3 +61,25 @@ def test_reference_written_checkpoint_loads_and_ours_matches_it(tmp_path):
     for k in a.files:
         assert a[k].dtype == b[k].dtype and a[k].shape == b[k].shape, k
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_interrupted_and_corrupted_saves(tmp_path):
+    """Failure injection on the host: the temporary file of an interrupted
+    save, files of another prefix and names without a time are never taken
+    for states; a truncated checkpoint raises instead of returning a state."""
+    that = np.full((2, 3), 1.0 + 2.0j)
+    good = ck.save(str(tmp_path), that, 0.25, n=3, fac=40.0)
+    with open(good, "rb") as f:
+        blob = f.read()
+    (tmp_path / "t_0.500000.npz.tmp.npz").write_bytes(blob)      # interrupted save
+    (tmp_path / "keep_0.750000.npz").write_bytes(blob)           # other prefix
+    (tmp_path / "t_final.npz").write_bytes(blob)                 # no time in the name
+    assert ck.list_(str(tmp_path)) == [(0.25, good)]
+    assert ck.latest(str(tmp_path), ck.KEEP_PREFIX)[0] == 0.75
+    cut = tmp_path / "t_1.000000.npz"
+    cut.write_bytes(blob[: len(blob) // 2])                      # truncated file
+    assert ck.latest(str(tmp_path))[0] == 1.0
+    with pytest.raises(Exception) as err:
+        ck.load(str(cut))
+    assert not isinstance(err.value, AssertionError)
+    assert ck.latest(str(tmp_path / "absent")) is None and ck.list_(str(tmp_path / "absent")) == []

@@ -25,6 +25,9 @@ Fixtures (sizes chosen so the whole script runs in a few minutes):
 * ``config_cases.json`` -- ``ConvectionConfig`` on 300 seeded configurations:
   outcome class, warning classes, ``canonical()``.
 * ``ckpt/t_0.125000.npz`` -- a state written by ``specmc.io.checkpoint.save``.
+* ``initial_32x24.npz`` + ``aspect_synthetic.txt`` -- ``core/bench_ic.py``
+  and ``physics/heating.py`` initial states (the ASPECT reader on a seeded
+  synthetic file in that format).
 * ``tala_ops_16x12.npz`` -- the TALA Stokes operators (``TalaStokes``,
   ``TalaFreeOperator``) and the TALA temperature operator, preconditioner and
   adiabatic source on one seeded state.
@@ -190,6 +193,37 @@ def tala_ops_case(S):
     print('tala_ops_16x12 written', flush=True)
 
 
+def initial_conditions_case(S):
+    """core/bench_ic.py and physics/heating.py initial states at 32x24: the
+    conductive seed, the analytic boundary-layer state, the heated conductive
+    profile, and an ASPECT ascii field read from a seeded synthetic file in
+    that format (aspect_synthetic.txt; the benchmark's own file is not
+    shipped) with the pchip and spline z-interpolants."""
+    from specmc.core import bench_ic as B
+    from specmc.core.rbc_galerkin import RBC
+    from specmc.physics import heating as HEAT
+    rng = np.random.default_rng(21)
+    n = 16
+    c = (np.arange(n) + 0.5) / n
+    T = (1.0 - c)[:, None] + 0.05 * rng.uniform(-1.0, 1.0, (n, n)) * np.sin(np.pi * c)[:, None]
+    path = os.path.join(HERE, 'aspect_synthetic.txt')
+    with open(path, 'w') as f:
+        f.write('# seeded synthetic temperature field in the ASPECT ascii-data layout\n')
+        f.write('# POINTS: %d %d\n' % (n, n))
+        for j in range(n):
+            for i in range(n):
+                f.write('%.10f %.10f %.15e\n' % (c[i], c[j], T[j, i]))
+    m = RBC(Ra=1e4, Nx=32, Nz=24)
+    np.savez_compressed(
+        os.path.join(HERE, 'initial_32x24.npz'),
+        conductive=B.conductive_theta(m, amp=3e-2, m=2, n=1),
+        analytic_bl=B.analytic_bl_theta(m),
+        heated=HEAT.conductive_theta(m.z, 1.5),
+        aspect_pchip=B.aspect_theta(m, path=path, zinterp='pchip'),
+        aspect_spline=B.aspect_theta(m, path=path, zinterp='spline'))
+    print('initial_32x24 written', flush=True)
+
+
 def pv_calibration_case(S):
     """reference_state.calibrate_pv for both anchors and a few V-tilde /
     contrast values (the pV(L) law's Ts, E-tilde, V-tilde, C, ln D)."""
@@ -329,6 +363,8 @@ def main(ref_root, only=()):
         checkpoint_case(S)
     if not only or 'tala_ops' in only:
         tala_ops_case(S)
+    if not only or 'initial' in only:
+        initial_conditions_case(S)
     base = dict(Ra=1e4, Nx=32, Nz=24)
     # configuration 1 of the headline table: isoviscous, march to t = 1e-3
     mc('const_32x24', dict(base, viscosity_model='const'), 25,

@@ -190,6 +190,15 @@ int smc_transform(smc_handle* h, int kind, const double* in, double* out, int me
  * coupled Stokes operator consumes for `that` (updates the eta counters). */
 int smc_eta_of(smc_handle* h, const double* that_in, int mem, double* eta_out);
 
+/* The viscosity the last Stokes solve consumed, the field the (Di/Ra) Phi
+ * source is weighted with (dissipation_eta: rbc_galerkin.py:375-383,
+ * convection_modes.py:215-222, coupled_model.py:499-507).  `eta_out` holds
+ * Nx*Nz doubles; *rows_out = 0 (const model, eta = 1: nothing written), 1
+ * (the bounded depth profile eta(z): Nz values; also the eta_T model before
+ * its first Stokes solve) or Nx (the (Nx,Nz) field of the eta_T model's last
+ * coupled solve). */
+int smc_dissipation_eta(smc_handle* h, double* eta_out, int mem, int* rows_out);
+
 /* FreeSchurOperator.matvec (stokes/lagged_stokes.py:202-220) at the viscosity
  * `eta` (Nx,Nz): out = A(eta) v, v and out (Nk,Nz) complex. */
 int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,

@@ -130,7 +130,7 @@ EXPORTED = ("smc_config_defaults", "smc_create", "smc_destroy", "smc_step", "smc
             "smc_eta_of", "smc_schur_matvec", "smc_reset_history", "smc_counters_get",
             "smc_shape", "smc_stream", "smc_last_error", "smc_set_state", "smc_get_state",
             "smc_advance", "smc_profile", "smc_profile_get", "smc_set_option",
-            "smc_grid_noalloc", "smc_get_history", "smc_set_history")
+            "smc_grid_noalloc", "smc_get_history", "smc_set_history", "smc_dissipation_eta")
 
 _LIB = None
 
@@ -163,6 +163,7 @@ def load(path=None):
         "smc_project_mirror": (i, [vp, vp, vp, i]),
         "smc_transform": (i, [vp, i, vp, vp, i]),
         "smc_eta_of": (i, [vp, vp, i, vp]),
+        "smc_dissipation_eta": (i, [vp, vp, i, vp]),
         "smc_schur_matvec": (i, [vp, vp, vp, vp, i]),
         "smc_reset_history": (i, [vp]),
         "smc_get_history": (i, [vp, vp, vp, i, dp, P(i)]),

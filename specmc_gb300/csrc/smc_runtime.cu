@@ -314,6 +314,7 @@ struct Model {
   double *dEta = nullptr, *dEtaLag = nullptr, *dLastEta = nullptr, *dEtaP = nullptr,
          *dEtaPadZ = nullptr, *dZeroGrid = nullptr;
   double2 *dEtaC = nullptr, *dMd = nullptr, *dAsmWork = nullptr;
+  double* dEzProf = nullptr;   // bounded depth profile eta(z) (eta_z / eta_T models)
   double2* dSchur = nullptr;
   int *dSchurPiv = nullptr, *dSchurPerm = nullptr;
   double2 *dSchurInvL = nullptr, *dSchurInvU = nullptr;
@@ -620,7 +621,8 @@ struct Model {
       dComm = mem.alloc<double>(NN); dCommG = mem.alloc<double>(Nk * NN);
       dPcm = mem.alloc<double>(Nk * NN);
       // frozen eta(z) of the depth-only base (convection_modes.py:96-107)
-      double* dEz = mem.alloc<double>(N);
+      dEzProf = mem.alloc<double>(N);
+      double* dEz = dEzProf;
       EtaLaw lz = law;
       lz.Ts = 0.0;
       eta_law(ctx, dZeroGrid, dz, N, N, lz, dEz, dScal, dRed);
@@ -2277,6 +2279,22 @@ int smc_eta_of(smc_handle* h, const double* in, int mem, double* eta_out) {
     copy_in(m, m.dIn, in, mem, m.n);
     m.eta_of(m.dIn);
     copy_out(m, eta_out, m.dEta, mem, sizeof(double) * m.Nx * m.N);
+  })
+}
+
+int smc_dissipation_eta(smc_handle* h, double* eta_out, int mem, int* rows_out) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    if (!rows_out) throw std::runtime_error("dissipation_eta: null rows_out");
+    if (m.cfg.model == SMC_MODEL_CONST) {
+      *rows_out = 0;
+    } else if (m.cfg.model == SMC_MODEL_ETA_T && m.have_last_eta) {
+      copy_out(m, eta_out, m.dLastEta, mem, sizeof(double) * m.Nx * m.N);
+      *rows_out = m.Nx;
+    } else {
+      copy_out(m, eta_out, m.dEzProf, mem, sizeof(double) * m.N);
+      *rows_out = 1;
+    }
   })
 }
 

@@ -278,6 +278,40 @@ class GpuModel:
         _lib.check(self._lib.smc_diagnostics(self._h, p, mem, ctypes.byref(d)))
         return {k: float(getattr(d, k)) for k, _ in _lib.SmcDiag._fields_}
 
+    def dissipation_eta(self):
+        """-> the viscosity the last Stokes solve consumed, which weights the
+        (Di/Ra) Phi source: None on the isoviscous model (eta = 1), the bounded
+        depth profile eta(z) (Nz,) on the eta_z model and on the eta_T model
+        before its first solve, else the eta_T model's last (Nx, Nz) field
+        (rbc_galerkin.py:375-383, convection_modes.py:215-222,
+        coupled_model.py:499-507)."""
+        buf = np.empty((self.Nx, self.Nz), dtype=np.float64)
+        rows = ctypes.c_int(0)
+        _lib.check(self._lib.smc_dissipation_eta(self._h, buf.ctypes.data_as(ctypes.c_void_p),
+                                                 _lib.SMC_HOST, ctypes.byref(rows)))
+        if rows.value == 0:
+            return None
+        return buf[0].copy() if rows.value == 1 else buf
+
+    def dissipation_phi(self, psi):
+        """-> Phi on the padded (2 Nx, Nz) grid for ``psi``, weighted with
+        ``dissipation_eta()`` (rbc_galerkin.py:385-394)."""
+        from .energy import phi_padded
+        return phi_padded(self, psi, self.dissipation_eta())
+
+    def mirror_error(self, that):
+        """-> max |theta(x) - theta(Lx - x)| / max |theta| on the grid
+        (rbc_galerkin.py:455-463)."""
+        from .drivers import mirror_error
+        return mirror_error(self, that)
+
+    def run(self, that, tstop, dt=None, safety=0.5, dtmax=5e-3, cadence=200, verbose=True):
+        """The simple march of rbc_galerkin.py:473-491: -> (state, diagnostics
+        every ``cadence`` steps)."""
+        from .drivers import run
+        return run(self, that, tstop, dt=dt, safety=safety, dtmax=dtmax, cadence=cadence,
+                   verbose=verbose)
+
     def project_mirror(self, that):
         p, mem, keep = self._spec_in(that)
         q, out = self._spec_out(mem == _lib.SMC_DEVICE)

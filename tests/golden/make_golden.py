@@ -25,6 +25,7 @@ Fixtures (sizes chosen so the whole script runs in a few minutes):
 * ``config_cases.json`` -- ``ConvectionConfig`` on 300 seeded configurations:
   outcome class, warning classes, ``canonical()``.
 * ``ckpt/t_0.125000.npz`` -- a state written by ``specmc.io.checkpoint.save``.
+* ``drivers_32x24.npz`` -- ``RBC.run`` records and ``RBC.mirror_error``.
 * ``initial_32x24.npz`` + ``aspect_synthetic.txt`` -- ``core/bench_ic.py``
   and ``physics/heating.py`` initial states (the ASPECT reader on a seeded
   synthetic file in that format).
@@ -224,6 +225,25 @@ def initial_conditions_case(S):
     print('initial_32x24 written', flush=True)
 
 
+def drivers_case(S):
+    """RBC.run (core/rbc_galerkin.py:473-491) on the isoviscous 32x24 model,
+    30 CFL steps with diagnostics every 10, and RBC.mirror_error of a
+    mirror-symmetric and of a seeded non-symmetric state."""
+    from specmc.core.rbc_galerkin import RBC
+    m = RBC(Ra=1e4, Nx=32, Nz=24)
+    th0 = m.seed(amp=3e-2, m=1, n=1)
+    s, hist = m.run(th0, tstop=30 * 4e-5 * 0.999, safety=0.5, dtmax=4e-5, cadence=10,
+                    verbose=False)
+    keys = sorted(hist[0])
+    rng = np.random.default_rng(8)
+    odd = rng.standard_normal((m.Nk, m.Nz)) + 1j * rng.standard_normal((m.Nk, m.Nz))
+    np.savez_compressed(os.path.join(HERE, 'drivers_32x24.npz'), that0=th0, final=s,
+                        keys=np.array(keys), hist=np.array([[h[k] for k in keys] for h in hist]),
+                        odd=odd, mirror_sym=np.float64(m.mirror_error(s)),
+                        mirror_odd=np.float64(m.mirror_error(odd)), n_steps=np.int64(m.n_steps))
+    print('drivers_32x24 written', flush=True)
+
+
 def pv_calibration_case(S):
     """reference_state.calibrate_pv for both anchors and a few V-tilde /
     contrast values (the pV(L) law's Ts, E-tilde, V-tilde, C, ln D)."""
@@ -365,6 +385,8 @@ def main(ref_root, only=()):
         tala_ops_case(S)
     if not only or 'initial' in only:
         initial_conditions_case(S)
+    if not only or 'drivers' in only:
+        drivers_case(S)
     base = dict(Ra=1e4, Nx=32, Nz=24)
     # configuration 1 of the headline table: isoviscous, march to t = 1e-3
     mc('const_32x24', dict(base, viscosity_model='const'), 25,

@@ -1,0 +1,61 @@
+"""Model-level workflow calls of the GPU models: run, mirror_error,
+dissipation_eta (the viscosity the last Stokes solve consumed) and
+dissipation_phi, against the reference's records
+(tests/golden/drivers_32x24.npz) and the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gb():
+    from specmc_gb300 import _lib
+    _lib.build()
+    import specmc_gb300.api as api
+    from specmc_gb300.config import ConvectionConfig
+    return api, ConvectionConfig
+
+
+def test_run_and_mirror_error_on_gpu(gb):
+    api, CC = gb
+    g = np.load(os.path.join(GOLDEN, "drivers_32x24.npz"))
+    m = api.build_model(CC(viscosity_model="const", Nx=32, Nz=24))
+    s, hist = m.run(g["that0"], tstop=30 * 4e-5 * 0.999, safety=0.5, dtmax=4e-5, cadence=10,
+                    verbose=False)
+    keys = [str(k) for k in g["keys"]]
+    got = np.array([[h[k] for k in keys] for h in hist])
+    assert got.shape == g["hist"].shape
+    assert np.abs(got - g["hist"]).max() <= 1e-10 * np.abs(g["hist"]).max()
+    assert m.mirror_error(s) < 1e-13
+    assert abs(m.mirror_error(g["odd"]) - g["mirror_odd"].item()) <= 1e-13
+    assert m.dissipation_eta() is None
+
+
+def test_dissipation_eta_is_the_consumed_field(gb):
+    from oracle import specmc_oracle as O
+    api, CC = gb
+    cz = CC(viscosity_model="eta_z", deta_T=100.0, Nx=32, Nz=24)
+    ez = api.build_model(cz).dissipation_eta()
+    assert ez.shape == (24,)
+    assert np.abs(ez - O.build(cz).eta_grid).max() <= 1e-14 * np.abs(ez).max()
+    ct = CC(viscosity_model="eta_T", Nx=32, Nz=24, dissipation_number=0.5)
+    m, o = api.build_model(ct), O.build(ct)
+    before = m.dissipation_eta()
+    assert before.shape == (24,)
+    assert np.abs(before - o.eta_grid).max() <= 1e-14 * np.abs(before).max()
+    th = m.seed(amp=3e-2, m=1, n=1)
+    m.stokes(th)
+    after = m.dissipation_eta()
+    assert after.shape == (32, 24)
+    ref = o.eta_of(th)
+    assert np.abs(after - ref).max() <= 1e-13 * np.abs(ref).max()
+    psi, _ = o.stokes(th)
+    phi = m.dissipation_phi(psi)
+    phi_o = O.phi_padded(o, psi, ref)
+    assert phi.shape == (64, 24)
+    assert np.abs(phi - phi_o).max() <= 1e-10 * np.abs(phi_o).max()

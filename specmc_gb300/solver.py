@@ -21,7 +21,7 @@ from numpy.polynomial import chebyshev as _npcheb
 
 from . import _lib
 
-__all__ = ["RBC", "RBCImplicitTheta", "RBCCoupled", "GpuModel"]
+__all__ = ["RBC", "RBCImplicitTheta", "RBCCoupled", "GpuModel", "ThetaSolverView"]
 
 
 def _cgl(N):
@@ -388,6 +388,49 @@ class GpuModel:
         return d
 
 
+class ThetaSolverView:
+    """The temperature solver's state under the names of the reference's
+    ImplicitThetaSolver (core/implicit_theta.py:128-212, 496-521), read from
+    the model's counters and configuration."""
+
+    _COUNTERS = dict(last_iters="theta_last_iters", last_res="theta_last_res",
+                     n_nonconv="n_theta_nonconv", n_be_fallback="n_be_fallback",
+                     n_solves="n_theta_solves")
+
+    def __init__(self, model):
+        self._model = model
+
+    def __getattr__(self, name):
+        key = ThetaSolverView._COUNTERS.get(name)
+        if key is None:
+            raise AttributeError(name)
+        return self._model.counters()[key]
+
+    @property
+    def scheme(self):
+        return "bdf2"
+
+    @property
+    def rtol(self):
+        return float(self._model._cfg.theta_rtol)
+
+    @property
+    def restart(self):
+        return int(self._model._cfg.theta_restart)
+
+    @property
+    def maxiter(self):
+        return int(self._model._cfg.theta_maxiter)
+
+    @property
+    def internal_heating(self):
+        return self._model.internal_heating
+
+    @property
+    def dissipation_number(self):
+        return self._model.dissipation_number
+
+
 class RBC(GpuModel):
     """Isoviscous model: explicit advection + backward-Euler diffusion."""
     _MODEL = _lib.SMC_MODEL_CONST
@@ -397,10 +440,20 @@ class RBCImplicitTheta(GpuModel):
     """Frozen eta(z) Stokes + linearly-implicit BDF2 temperature step."""
     _MODEL = _lib.SMC_MODEL_ETA_Z
 
+    @property
+    def theta(self):
+        """The temperature solver's state (ImplicitThetaSolver names)."""
+        return ThetaSolverView(self)
+
 
 class RBCCoupled(GpuModel):
     """eta(T(x,z,t)) coupled Stokes (lagged LU + defect / BFBT) + BDF2 theta."""
     _MODEL = _lib.SMC_MODEL_ETA_T
+
+    @property
+    def theta(self):
+        """The temperature solver's state (ImplicitThetaSolver names)."""
+        return ThetaSolverView(self)
 
     def eta_of(self, that):
         """-> the (Nx, Nz) viscosity of a state: padded law, window, x-truncation

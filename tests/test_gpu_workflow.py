@@ -50,6 +50,7 @@ def test_dissipation_eta_is_the_consumed_field(gb):
     assert np.abs(before - o.eta_grid).max() <= 1e-14 * np.abs(before).max()
     th = m.seed(amp=3e-2, m=1, n=1)
     m.stokes(th)
+    assert m.theta.scheme == "bdf2" and m.theta.rtol == 1e-10 and m.theta.n_solves == 0
     after = m.dissipation_eta()
     assert after.shape == (32, 24)
     ref = o.eta_of(th)

@@ -60,3 +60,28 @@ def test_dissipation_eta_is_the_consumed_field(gb):
     phi_o = O.phi_padded(o, psi, ref)
     assert phi.shape == (64, 24)
     assert np.abs(phi - phi_o).max() <= 1e-10 * np.abs(phi_o).max()
+
+
+def test_single_mode_analytic_solution_on_gpu(gb):
+    """The single-mode known answers of core/rbc_galerkin.py:500-513 and
+    physics/dissipation.py:495-517 on the GPU model: for theta = Theta
+    cos(pi x) sin(pi z), psi = -Ra pi/g^2 Theta sin(pi x) sin(pi z),
+    u_z = Ra pi^2/g^2 theta and <Phi> = Ra <theta u_z> = Ra^2 pi^2/(4 g^2) Theta^2,
+    g = 2 pi^2."""
+    from specmc_gb300 import energy
+    api, CC = gb
+    Ra, Theta, k = 1e4, 0.7, np.pi
+    m = api.build_model(CC(viscosity_model="const", Ra=Ra, Nx=16, Nz=32))
+    X, Z = np.meshgrid(m.x, m.z, indexing="ij")
+    g = 2.0 * k * k
+    th = Theta * np.cos(k * X) * np.sin(k * Z)
+    that = m.coeffs(th)
+    psi, _ = m.stokes(that)
+    psi_ref = -Ra * k / g ** 2 * Theta * np.sin(k * X) * np.sin(k * Z)
+    assert np.abs(m.grid(psi) - psi_ref).max() <= 1e-11 * np.abs(psi_ref).max()
+    _, uz = m.velocity(psi)
+    uz_ref = Ra * k * k / g ** 2 * th
+    assert np.abs(uz - uz_ref).max() <= 1e-11 * np.abs(uz_ref).max()
+    phi_ref = Ra ** 2 * k * k / (4.0 * g ** 2) * Theta ** 2
+    assert abs(energy.phi_integral(m, psi) - phi_ref) <= 1e-10 * phi_ref
+    assert abs(energy.pi_theta(m, psi, that) - phi_ref) <= 1e-10 * phi_ref

@@ -183,3 +183,42 @@ def test_model_basis_attributes_match_reference():
         ref = g[k]
         assert b[k].shape == ref.shape, k
         assert np.max(np.abs(b[k] - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref))), k
+
+
+def test_header_is_plain_c_and_a_c_caller_links(tmp_path):
+    """include/specmc_gb300.h compiles as C99 and a C caller links against
+    libspecmc_gb300.so; the program runs the calls that need no GPU (the
+    defaults and a rejected configuration with its message)."""
+    import shutil
+    import subprocess
+    from specmc_gb300 import _lib
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    _lib.build()
+    src = tmp_path / "caller.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <string.h>
+#include "specmc_gb300.h"
+int main(void) {
+  smc_config c;
+  smc_handle* h = 0;
+  smc_config_defaults(&c);
+  if (c.abi_version != SMC_ABI_VERSION || c.Nx != 64 || c.Nz != 96) return 2;
+  c.compressibility = SMC_TALA;
+  c.precision = SMC_MIXED;
+  if (smc_create(&c, &h) >= 0 || h != 0) return 3;
+  if (!strstr(smc_last_error(), "FP64 form only")) return 4;
+  printf("ok %s\n", smc_last_error());
+  return 0;
+}
+''')
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    exe = tmp_path / "caller"
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-L", libdir, "-lspecmc_gb300", "-o", str(exe)], check=True)
+    env = dict(os.environ, LD_LIBRARY_PATH=libdir + os.pathsep + os.environ.get("LD_LIBRARY_PATH", ""))
+    out = subprocess.run([str(exe)], env=env, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
+    assert out.stdout.startswith("ok ")

@@ -25,6 +25,8 @@ Fixtures (sizes chosen so the whole script runs in a few minutes):
 * ``config_cases.json`` -- ``ConvectionConfig`` on 300 seeded configurations:
   outcome class, warning classes, ``canonical()``.
 * ``ckpt/t_0.125000.npz`` -- a state written by ``specmc.io.checkpoint.save``.
+* ``physics_helpers.json`` -- closed forms and helpers of
+  ``physics/heating.py`` and ``physics/dissipation.py``.
 * ``drivers_32x24.npz`` -- ``RBC.run`` records and ``RBC.mirror_error``.
 * ``initial_32x24.npz`` + ``aspect_synthetic.txt`` -- ``core/bench_ic.py``
   and ``physics/heating.py`` initial states (the ASPECT reader on a seeded
@@ -244,6 +246,49 @@ def drivers_case(S):
     print('drivers_32x24 written', flush=True)
 
 
+def physics_helpers_case(S):
+    """The closed forms and helpers of physics/heating.py and
+    physics/dissipation.py on sample arguments, and phi_z_tail /
+    source_coeffs on the third state of the energy fixture's march."""
+    import json
+    from specmc.physics import heating as HEAT, dissipation as DISS
+    z = np.linspace(0.0, 1.0, 7)
+    out = {}
+    for H in (0.0, 1.5, 2.0, 4.0, -1.0):
+        out['H=%g' % H] = dict(
+            conductive_theta=HEAT.conductive_theta(z, H).tolist(),
+            conductive_T=HEAT.conductive_T(z, H).tolist(),
+            mean_T=HEAT.mean_T_conductive(H), nu_bot=HEAT.nu_bot_conductive(H),
+            nu_top=HEAT.nu_top_conductive(H), T_max=list(HEAT.T_max_conductive(H)),
+            nu_energy=HEAT.nu_energy_steady(0.3, H), nu_bot_energy=HEAT.nu_bot_energy_steady(0.3, H),
+            nu_top_steady=DISS.nu_top_steady(0.3, H, 0.05),
+            nu_bot_steady=DISS.nu_bot_steady(0.3, H, 0.05),
+            source_integral=HEAT.source_integral(H),
+            source_00=HEAT.source_coeffs(3, 4, H)[0, 0].real)
+    out['single_mode'] = [DISS.single_mode_theta_integral(1e4, np.pi, np.pi, 1.0),
+                          DISS.single_mode_theta_integral(3e5, 2 * np.pi, np.pi, 0.2),
+                          DISS.single_mode_psi_integral(np.pi, 2 * np.pi, -3.0)]
+    rng = np.random.default_rng(2)
+    prof = rng.uniform(0.5, 2.0, 5)
+    cases = [None, np.ones((4, 5)), prof, np.tile(prof, (4, 1)), rng.uniform(0.5, 2.0, (4, 5))]
+    out['eta_class'] = [DISS.eta_class(c) for c in cases]
+    out['j9_2_bound'] = [DISS.j9_2_bound(c, t, p) for c in ('const', 'eta_z', 'eta_xz', 'other')
+                         for t, p in ((0.0, 0.0), (1e-8, 0.0), (0.0, 1e-3))]
+    g = np.load(os.path.join(HERE, 'energy_32x24.npz'))
+    api = S.api
+    cfg = S.ConvectionConfig(Ra=1e4, Nx=32, Nz=24, viscosity_model='arrhenius', deta_T=1e3,
+                             arrhenius_Ts=1.0, eta_min=1e-3, eta_max=1.0,
+                             dissipation_number=0.5, internal_heating=1.0)
+    m = api.build_model(cfg)
+    out['phi_z_tail'] = DISS.phi_z_tail(m, g['psi'], g['eta'])
+    sc = DISS.source_coeffs(m, g['psi'], g['eta'], Di=0.5)
+    out['source_coeffs_norm'] = float(np.linalg.norm(sc))
+    out['source_coeffs_integral'] = DISS.source_integral(m, sc)
+    with open(os.path.join(HERE, 'physics_helpers.json'), 'w') as f:
+        json.dump(out, f, indent=0, sort_keys=True)
+    print('physics_helpers written', flush=True)
+
+
 def pv_calibration_case(S):
     """reference_state.calibrate_pv for both anchors and a few V-tilde /
     contrast values (the pV(L) law's Ts, E-tilde, V-tilde, C, ln D)."""
@@ -387,6 +432,8 @@ def main(ref_root, only=()):
         initial_conditions_case(S)
     if not only or 'drivers' in only:
         drivers_case(S)
+    if not only or 'physics_helpers' in only:
+        physics_helpers_case(S)
     base = dict(Ra=1e4, Nx=32, Nz=24)
     # configuration 1 of the headline table: isoviscous, march to t = 1e-3
     mc('const_32x24', dict(base, viscosity_model='const'), 25,

@@ -284,6 +284,14 @@ def physics_helpers_case(S):
     sc = DISS.source_coeffs(m, g['psi'], g['eta'], Di=0.5)
     out['source_coeffs_norm'] = float(np.linalg.norm(sc))
     out['source_coeffs_integral'] = DISS.source_integral(m, sc)
+    from specmc.core import cfl_policy as CFL
+    from specmc.core.rbc_galerkin import RBC
+    r = RBC(Ra=1e4, Nx=32, Nz=24)
+    th = r.seed(amp=3e-2, m=1, n=1)
+    out['cfl'] = [CFL.cfl_dt(r, th, safety=sf, dtmax=dm, clamp=cl)
+                  for sf in (0.4, 40.0, 500.0, -1.0) for dm in (4e-5, 1.0) for cl in (True, False)
+                  if not (sf < 0 and not cl)]
+    out['clamp_safety'] = [CFL.clamp_safety(v) for v in (-3.0, 0.5, 40.0, 100.0)]
     with open(os.path.join(HERE, 'physics_helpers.json'), 'w') as f:
         json.dump(out, f, indent=0, sort_keys=True)
     print('physics_helpers written', flush=True)

@@ -70,3 +70,15 @@ def test_dissipation_helpers(ref):
     out = DISS.add_dissipation_source(b, sc, 0.5).reshape(m.Nk, m.Nz)
     assert np.array_equal(out[:, :-2], sc[:, :-2]) and not out[:, -2:].any()
     assert DISS.add_dissipation_source(b, sc, 0.0) is b
+
+
+def test_cfl_policy(ref):
+    from specmc_gb300 import cfl_policy as CFL
+    m = O.ConstModel(Ra=1e4, Nx=32, Nz=24)
+    th = m.seed(amp=3e-2, m=1, n=1)
+    got = [CFL.cfl_dt(m, th, safety=sf, dtmax=dm, clamp=cl)
+           for sf in (0.4, 40.0, 500.0, -1.0) for dm in (4e-5, 1.0) for cl in (True, False)
+           if not (sf < 0 and not cl)]
+    assert _close(got, ref["cfl"], 1e-12)
+    assert [CFL.clamp_safety(v) for v in (-3.0, 0.5, 40.0, 100.0)] == ref["clamp_safety"]
+    assert (CFL.CFL_SAFETY_DEFAULT, CFL.CFL_SAFETY_MAX) == (40.0, 80.0)

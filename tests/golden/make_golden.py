@@ -25,6 +25,8 @@ Fixtures (sizes chosen so the whole script runs in a few minutes):
 * ``config_cases.json`` -- ``ConvectionConfig`` on 300 seeded configurations:
   outcome class, warning classes, ``canonical()``.
 * ``ckpt/t_0.125000.npz`` -- a state written by ``specmc.io.checkpoint.save``.
+* ``rheology.npz`` -- ``physics/viscosity.py``, ``physics/arrhenius.py`` and
+  ``physics/eta_bounds.py`` on seeded sample points.
 * ``physics_helpers.json`` -- closed forms and helpers of
   ``physics/heating.py`` and ``physics/dissipation.py``.
 * ``drivers_32x24.npz`` -- ``RBC.run`` records and ``RBC.mirror_error``.
@@ -297,6 +299,43 @@ def physics_helpers_case(S):
     print('physics_helpers written', flush=True)
 
 
+def rheology_case(S):
+    """physics/viscosity.py, physics/arrhenius.py and physics/eta_bounds.py on
+    seeded sample points."""
+    from specmc.physics import arrhenius as AR, eta_bounds as EB, viscosity as VI
+    rng = np.random.default_rng(13)
+    T = np.concatenate(([0.0, 1.0, 2.0], rng.uniform(0.0, 2.0, 29)))
+    z = rng.uniform(0.0, 1.0, T.size)
+    eta = np.exp(rng.uniform(np.log(1e-5), np.log(1e5), 64))
+    eta[:4] = [1e-3, 1e-3 * (1.0 - 1e-13), 1e3 * (1.0 + 1e-13), 1e3]
+    E, V, Ts = AR.arrhenius_E(1e3, 0.3), 0.7, 0.3
+    rec = dict(
+        T=T, z=z, eta=eta,
+        eta_exp_T=VI.eta_exp_T(T, 1e3),
+        eta_background=VI.eta_conductive_background(z, 100.0),
+        eta_law_iso=VI.eta_from_law('isoviscous', 100.0, z),
+        eta_law_exp=VI.eta_from_law('exp_T_depth', 100.0, z),
+        arr_scalars=np.array([AR.arrhenius_E(1e3, 0.3), AR.arrhenius_C(1e3, 0.3),
+                              AR.cold_end_slope(1e3, 0.3), AR.slope_amplification(0.3),
+                              AR.infer_deta_T(5.0, 0.3), AR.infer_Ts(5.0, 1e3),
+                              AR.hot_end_contrast_V(T, z, E, V, Ts)]),
+        arr_exponent=AR.arrhenius_exponent(T, 1e3, 0.3),
+        arr_eta=AR.eta_arrhenius_T(T, 1e3, 0.3),
+        arr_exponent_V=AR.arrhenius_exponent_V(T, z, E, V, Ts),
+        arr_eta_V=AR.eta_arrhenius_V(T, z, E, V, Ts),
+        windows=np.array([*EB.reachable_window(1e3), *EB.reachable_window_arrhenius(1e3, 1.0),
+                          *EB.reachable_window_arrhenius(1e3, 0.05),
+                          *EB.reachable_window_pv(E, V, Ts), *EB.effective_bounds(1e-3, 1e3)]),
+        n_clipped=np.int64(EB.n_clipped(eta, 1e-3, 1e3)),
+        clip=EB.clip_eta(eta, 1e-3, 1e3)[0], clip_n=np.int64(EB.clip_eta(eta, 1e-3, 1e3)[1]),
+        smoothstep=EB.smoothstep5(np.linspace(-0.5, 1.5, 21)),
+        n_band=np.int64(EB.n_in_transition(eta, 1e-3, 1e3, 1.5)),
+        smooth=EB.smooth_clip_eta(eta, 1e-3, 1e3, 1.5)[0],
+        smooth_n=np.int64(EB.smooth_clip_eta(eta, 1e-3, 1e3, 1.5)[1]))
+    np.savez_compressed(os.path.join(HERE, 'rheology.npz'), **rec)
+    print('rheology written', flush=True)
+
+
 def pv_calibration_case(S):
     """reference_state.calibrate_pv for both anchors and a few V-tilde /
     contrast values (the pV(L) law's Ts, E-tilde, V-tilde, C, ln D)."""
@@ -442,6 +481,8 @@ def main(ref_root, only=()):
         drivers_case(S)
     if not only or 'physics_helpers' in only:
         physics_helpers_case(S)
+    if not only or 'rheology' in only:
+        rheology_case(S)
     base = dict(Ra=1e4, Nx=32, Nz=24)
     # configuration 1 of the headline table: isoviscous, march to t = 1e-3
     mc('const_32x24', dict(base, viscosity_model='const'), 25,

@@ -222,3 +222,41 @@ int main(void) {
     out = subprocess.run([str(exe)], env=env, capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
     assert out.stdout.startswith("ok ")
+
+
+def test_ctypes_mirrors_match_the_c_structs(tmp_path):
+    """Every field of the Python mirrors of smc_config, smc_diag,
+    smc_counters and smc_march_info sits at the offset the C compiler gives
+    it, and the structs have the same size (a mismatch would silently corrupt
+    every call)."""
+    import ctypes
+    import shutil
+    import subprocess
+    from specmc_gb300 import _lib
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"smc_config": _lib.SmcConfig, "smc_diag": _lib.SmcDiag,
+               "smc_counters": _lib.SmcCounters, "smc_march_info": _lib.SmcMarchInfo}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "specmc_gb300.h"',
+             'int main(void) {']
+    for cname, py in mirrors.items():
+        lines.append('  printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in py._fields_:
+            lines.append('  printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([gcc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    c = {}
+    for line in out:
+        if line:
+            cname, field, value = line.split()
+            c[(cname, field)] = int(value)
+    for cname, py in mirrors.items():
+        assert ctypes.sizeof(py) == c[(cname, "sizeof")], cname
+        for fname, _ in py._fields_:
+            assert getattr(py, fname).offset == c[(cname, fname)], (cname, fname)

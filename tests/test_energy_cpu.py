@@ -19,29 +19,13 @@ def _golden():
     return np.load(os.path.join(os.path.dirname(__file__), "golden", "energy_32x24.npz"))
 
 
-class _OracleBackend:
-    """The oracle model under the model-contract names the diagnostics use."""
-
-    def __init__(self, m):
-        self._m = m
-
-    def __getattr__(self, name):
-        return getattr(self._m, name)
-
-    def _synth_pad(self, cf):
-        return self._m.synth_pad(cf)
-
-    def _trunc_pad(self, g):
-        return self._m.trunc_pad(g)
-
-
 def _rel(a, b):
     return abs(a - b) / max(abs(b), 1e-300)
 
 
 def test_energy_diagnostics_match_reference():
     g = _golden()
-    m = _OracleBackend(O.build(ConvectionConfig(**CFG)))
+    m = O.build(ConvectionConfig(**CFG))
     a0, b0, b1 = g["abc"]
     hb = EN.heating_balance(m, g["s3"], g["s2"], g["s1"], a0, b0, b1, H=1.0)
     for k, v in hb.items():

@@ -83,3 +83,35 @@ def test_interrupted_and_corrupted_saves(tmp_path):
         ck.load(str(cut))
     assert not isinstance(err.value, AssertionError)
     assert ck.latest(str(tmp_path / "absent")) is None and ck.list_(str(tmp_path / "absent")) == []
+
+
+def test_bdf2_history_roundtrip(tmp_path):
+    """save(..., model=m) stores the BDF2 history the model reports;
+    resume() installs it in a model, or resets the model's history for a file
+    without one (a stand-in model records the calls)."""
+    class Model:
+        def __init__(self, have):
+            self.have, self.calls = have, []
+
+        def get_history(self):
+            return dict(have_prev=self.have, prev=np.full((2, 3), 1 + 2j),
+                        psi_prev=np.full((2, 3), 3j), dt_prev=2e-5)
+
+        def set_history(self, prev, psi_prev, dt_prev, have_prev):
+            self.calls.append(("set", prev.copy(), psi_prev.copy(), dt_prev, have_prev))
+
+        def reset_history(self):
+            self.calls.append(("reset",))
+
+    s = np.arange(6.0).reshape(2, 3) + 0j
+    p = ck.save(str(tmp_path), s, 1e-4, n=5, model=Model(True))
+    m = Model(False)
+    s2, meta = ck.resume(m, p)
+    assert np.array_equal(s2, s) and meta["n"] == 5 and meta["fac"] is None
+    kind, prev, psi_prev, dt_prev, have = m.calls[0]
+    assert kind == "set" and have and dt_prev == 2e-5
+    assert np.array_equal(prev, np.full((2, 3), 1 + 2j)) and np.array_equal(psi_prev, np.full((2, 3), 3j))
+    p2 = ck.save(str(tmp_path), s, 2e-4, model=Model(False))          # no history to store
+    m2 = Model(False)
+    _, meta2 = ck.resume(m2, p2)
+    assert meta2["history"] is None and m2.calls == [("reset",)]

@@ -109,3 +109,19 @@ def test_tala_march_matches_reference(gb, case, state_tol, diag_tol):
     for key in ("n_refresh", "n_defect", "n_defect_failed", "n_defect_double_fail", "n_steps"):
         if "ctr_" + key in g.files:
             assert c[key] == int(g["ctr_" + key]), (key, c[key], int(g["ctr_" + key]))
+
+
+@pytest.mark.parametrize("vm,kw", [("eta_z", dict(deta_T=100.0)), ("eta_T", dict(precond="legacy"))])
+def test_tala_at_zero_Di_is_boussinesq(gb, vm, kw):
+    """With Di = 0 (rho_bar = 1, a = 0) the TALA kernels reproduce the
+    Boussinesq route (the limit stokes_tala.py:523-548 checks): six steps of
+    both on the GPU agree to roundoff (3e-15 on the oracle)."""
+    api, CC, lib = gb
+    mb = api.build_model(CC(Ra=1e4, Nx=32, Nz=24, viscosity_model=vm, **kw))
+    mt = api.build_model(CC(Ra=1e4, Nx=32, Nz=24, viscosity_model=vm, compressibility="tala", **kw))
+    sb = mb.seed(amp=3e-2, m=1, n=1)
+    st = np.array(sb, copy=True)
+    for _ in range(6):
+        sb = mb.step(sb, api.production_dt(mb, sb))
+        st = mt.step(st, api.production_dt(mt, st))
+    assert _rel(st, sb) < 1e-9, _rel(st, sb)

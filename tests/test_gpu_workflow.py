@@ -85,3 +85,23 @@ def test_single_mode_analytic_solution_on_gpu(gb):
     phi_ref = Ra ** 2 * k * k / (4.0 * g ** 2) * Theta ** 2
     assert abs(energy.phi_integral(m, psi) - phi_ref) <= 1e-10 * phi_ref
     assert abs(energy.pi_theta(m, psi, that) - phi_ref) <= 1e-10 * phi_ref
+
+
+def test_forced_bfbt_rescue(gb):
+    """Failure injection on the host, the reference's own check
+    (models/coupled_model.py:955-969): with a one-iteration FGMRES budget the
+    BFBT Stokes solve cannot converge, so the rescue must fire once and
+    return the lagged-LU solution, equal to the legacy route's."""
+    from oracle import specmc_oracle as O
+    from specmc_gb300.solver import RBCCoupled
+    api, CC = gb
+    mr = RBCCoupled(Nx=16, Nz=12, deta_T=1000.0, precond="bfbt", stokes_maxiter=1)
+    th = mr.seed(amp=1e-2, m=1, n=1)
+    psi_r, _ = mr.stokes(th)
+    c = mr.counters()
+    assert c["n_bfbt_solves"] == 1 and c["n_bfbt_rescue"] == 1 and c["n_refresh"] == 1
+    ml = RBCCoupled(Nx=16, Nz=12, deta_T=1000.0, precond="legacy")
+    psi_l, _ = ml.stokes(th)
+    assert np.abs(psi_r - psi_l).max() <= 1e-12 * np.abs(psi_l).max()
+    psi_o, _ = O.CoupledModel(Nx=16, Nz=12, deta_T=1000.0, precond="legacy").stokes(th)
+    assert np.abs(psi_r - psi_o).max() <= 1e-8 * np.abs(psi_o).max()

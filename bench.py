@@ -36,11 +36,12 @@ METRIC = "steps/sec, mixed-precision vs FP64 GPU path at <=1e-6 rel Nu/Vrms erro
 WORKLOAD = dict(viscosity_model="eta_T", deta_T=1000.0, Ra=1e4, Nx=64, Nz=96)
 SEED = dict(amp=3e-2, m=1, n=1)
 L2_BYTES = 129 * 1024 * 1024
-# DRAM bytes (read + write) per launch of the dominant kernels, from ncu
-# captures of this workload (dram__bytes_read.sum + dram__bytes_write.sum,
-# mean over the captured launches); the captures and their commands are
-# summarised in profiles/engine_64x96.md
+# DRAM bytes (read + write) per launch of the dominant kernels: ncu
+# dram__bytes_read.sum + dram__bytes_write.sum, mean over the captured
+# launches of this workload (--clock-control none, a few launches of one
+# kernel after the warm-up steps); TRAFFIC_SOURCE names the committed summary
 DRAM_BYTES_PER_LAUNCH = {"engine_stokes": 28.38e6, "engine_theta": 3.46e6}
+TRAFFIC_SOURCE = "profiles/engine_64x96.md"
 
 
 def _peaks():
@@ -137,8 +138,9 @@ def run_reference(args, rank, world):
     if rank != 0:
         return 0
     cores = os.cpu_count()
-    steps = max(1, min(args.steps, args.ref_steps))
-    warm = min(args.warmup, args.ref_warmup)
+    # the same march steps as the GPU arm: warm-up steps 1..W, timed W+1..W+K
+    steps = args.steps if args.ref_steps is None else max(1, args.ref_steps)
+    warm = args.warmup if args.ref_warmup is None else args.ref_warmup
     rate, d = cpu_oracle_rate(steps, warm, threads=cores)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s",
@@ -299,6 +301,7 @@ def run_ours(args, rank, world):
             roof = {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                     "frac": ach / peaks["hbm_gbs"],
                     "traffic": DRAM_BYTES_PER_LAUNCH.get(dom["name"]),
+                    "traffic_source": TRAFFIC_SOURCE,
                     "algorithmic_bytes_per_launch": per_launch,
                     "peak_source": psrc + ", copy bandwidth (of measured)"}
         else:
@@ -321,7 +324,10 @@ def run_ours(args, rank, world):
         # shared host cores shows here first)
         "step_ms": {"min": M["step_ms"][0], "median": M["step_ms"][len(M["step_ms"]) // 2],
                     "max": M["step_ms"][-1]},
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        # the mixed form: FP32 (and double-float) inner Krylov iterations,
+        # FP64 residuals, solution updates, factorisations and reductions
+        "dtype": "fp32/fp64 mixed",
         "data": "synthetic (seeded conductive perturbation, random-free)",
         "config": dict(workload="eta_T 64x96 Ra=1e4 deta_T=1e3, 200-step adaptive march",
                        sample="steps %d..%d" % (args.warmup + 1, args.warmup + args.steps),
@@ -350,14 +356,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--cpu-steps", type=int, default=6)
-    ap.add_argument("--ref-steps", type=int, default=40)
-    ap.add_argument("--ref-warmup", type=int, default=3)
+    ap.add_argument("--ref-steps", type=int, default=None,
+                    help="reference arm: timed steps (default: --steps)")
+    ap.add_argument("--ref-warmup", type=int, default=None,
+                    help="reference arm: warm-up steps (default: --warmup)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--phases", action="store_true",
                     help="add the Krylov engine's per-phase times to kernel_regions")
     args = ap.parse_args()
-    if args.warmup < 3 and args.impl == "ours":
+    if args.warmup < 3:
         args.warmup = 3
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -18,6 +18,7 @@
 // nothing has to start at zero; but all calls share the one array, so calls
 // that overlap on the GPU (concurrent streams, or host threads issuing to
 // different streams without ordering) race and corrupt each other's results.
+#include <algorithm>
 #include <mutex>
 
 #include "../../include/specmc_gb300.h"
@@ -41,18 +42,20 @@ static void* g_noalloc_addr[64] = {nullptr};
 __global__ void smc_noalloc_zsynth_kernel(const double2* __restrict__ c, double2* __restrict__ X,
                                           int Nk, int N) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int k = blockIdx.y;
   if (j >= N) return;
-  const double2* ck = c + (long long)k * N;
   const long long period = 2LL * (N - 1);
-  double sr = 0.0, si = 0.0;
-  for (int n = 0; n < N; ++n) {
-    double t = cospi((double)(((long long)n * j) % period) / (double)(N - 1));
-    if (n & 1) t = -t;
-    sr += t * ck[n].x;
-    si += t * ck[n].y;
+  // rows k stride over gridDim.y (at most 65535), so every Nk is covered
+  for (int k = blockIdx.y; k < Nk; k += gridDim.y) {
+    const double2* ck = c + (long long)k * N;
+    double sr = 0.0, si = 0.0;
+    for (int n = 0; n < N; ++n) {
+      double t = cospi((double)(((long long)n * j) % period) / (double)(N - 1));
+      if (n & 1) t = -t;
+      sr += t * ck[n].x;
+      si += t * ck[n].y;
+    }
+    X[(long long)k * N + j] = make_double2(sr, si);
   }
-  X[(long long)k * N + j] = make_double2(sr, si);
 }
 
 // g[i][j] = Re X[0][j] + sum_{k>=1} w_k Re(X[k][j] e^{2 pi i k i / Ng}),
@@ -60,17 +63,19 @@ __global__ void smc_noalloc_zsynth_kernel(const double2* __restrict__ c, double2
 __global__ void smc_noalloc_xsynth_kernel(const double2* __restrict__ X, double* __restrict__ g,
                                           int Nk, int N, int Ng) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y;
   if (j >= N) return;
-  double acc = X[j].x;
-  for (int k = 1; k < Nk; ++k) {
-    double s, c;
-    sincospi(2.0 * (double)(((long long)k * i) % Ng) / (double)Ng, &s, &c);
-    double2 x = X[(long long)k * N + j];
-    double v = x.x * c - x.y * s;
-    acc += (2 * k == Ng) ? v : 2.0 * v;
+  // grid rows i stride over gridDim.y (at most 65535), so every Ng is covered
+  for (int i = blockIdx.y; i < Ng; i += gridDim.y) {
+    double acc = X[j].x;
+    for (int k = 1; k < Nk; ++k) {
+      double s, c;
+      sincospi(2.0 * (double)(((long long)k * i) % Ng) / (double)Ng, &s, &c);
+      double2 x = X[(long long)k * N + j];
+      double v = x.x * c - x.y * s;
+      acc += (2 * k == Ng) ? v : 2.0 * v;
+    }
+    g[(long long)i * N + j] = acc;
   }
-  g[(long long)i * N + j] = acc;
 }
 
 }  // namespace smc
@@ -106,10 +111,11 @@ extern "C" int smc_grid_noalloc(const double* that_dev, double* grid_dev, int Nx
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     double2* X = static_cast<double2*>(scratch);
     const int Ng = padded ? 2 * Nx : Nx;
-    smc_noalloc_zsynth_kernel<<<dim3(ceil_div(Nz, 128), Nk), 128, 0, s>>>(
+    // gridDim.y is capped at 65535; the kernels stride their rows over it
+    smc_noalloc_zsynth_kernel<<<dim3(ceil_div(Nz, 128), std::min(Nk, 65535)), 128, 0, s>>>(
         reinterpret_cast<const double2*>(that_dev), X, Nk, Nz);
     SMC_CUDA(cudaGetLastError());
-    smc_noalloc_xsynth_kernel<<<dim3(ceil_div(Nz, 128), Ng), 128, 0, s>>>(X, grid_dev, Nk, Nz, Ng);
+    smc_noalloc_xsynth_kernel<<<dim3(ceil_div(Nz, 128), std::min(Ng, 65535)), 128, 0, s>>>(X, grid_dev, Nk, Nz, Ng);
     SMC_CUDA(cudaGetLastError());
     return 0;
   } catch (const std::exception& e) {

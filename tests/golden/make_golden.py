@@ -2,7 +2,11 @@
 
 Run once, in a container where the reference package is importable:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference [case ...]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <reference checkout> [case ...]
+
+(the first argument is required: the directory that holds the reference's
+``specmc`` package; it may also be given as $SPECMC_REFERENCE with ``-`` in
+its place)
 
 (the optional case names restrict the run to those fixtures, e.g.
 ``arrhenius_pv_32x24``).
@@ -119,6 +123,48 @@ def march_case(name, cfg_kw, steps, ic, S):
     np.savez_compressed(os.path.join(HERE, 'march_%s.npz' % name), **rec)
     print('%-14s %3d steps  %.2f s  Nu_top=%.10f urms=%.10f'
           % (name, steps, el, d['Nu_top'], d['urms']), flush=True)
+
+
+def long_march_case(name, cfg_kw, steps, ic, S, every=20):
+    """A long adaptive march (the headline configurations at their own
+    lengths): every step's dt, the diagnostics and the state every `every`
+    steps and at the end, and the counters.  Written as ``long_<name>.npz``."""
+    api = S.api
+    cfg = S.ConvectionConfig(**cfg_kw)
+    m = api.build_model(cfg)
+    if ic[0] == 'seed':
+        th0 = m.seed(amp=ic[1], m=ic[2], n=ic[3])
+    else:
+        th0 = seeded_noise_theta(m, amp=ic[1], mmax=ic[2], nmax=ic[3],
+                                 seed=ic[4], Lx=cfg.Lx,
+                                 H=cfg.internal_heating)
+    keys = ('Nu_top', 'Nu_bot', 'Nu_energy', 'urms', 'umax', 'amp')
+    dts, trace_steps, trace, trace_states, ts = [], [], [], [], []
+    s = np.array(th0, copy=True)
+    t = 0.0
+    t0 = time.perf_counter()
+    for i in range(steps):
+        dt = api.production_dt(m, s)
+        s = m.step(s, dt)
+        t += dt
+        dts.append(dt)
+        if (i + 1) % every == 0 or i + 1 == steps:
+            d = m.diagnostics(s)
+            trace_steps.append(i + 1)
+            ts.append(t)
+            trace.append([d[k] for k in keys])
+            trace_states.append(s.copy())
+    el = time.perf_counter() - t0
+    rec = dict(that0=th0, dts=np.array(dts), trace_steps=np.array(trace_steps),
+               trace_t=np.array(ts), trace=np.array(trace),
+               trace_keys=np.array(keys), trace_states=np.array(trace_states),
+               state=s, t=np.float64(t), wall_s=np.float64(el), **counters(m))
+    for k, v in cfg_kw.items():
+        rec['cfg_' + k] = np.asarray(v)
+    np.savez_compressed(os.path.join(HERE, 'long_%s.npz' % name), **rec)
+    d = m.diagnostics(s)
+    print('long %-14s %4d steps  %.1f s  t=%.6g Nu_top=%.10f urms=%.10f'
+          % (name, steps, el, t, d['Nu_top'], d['urms']), flush=True)
 
 
 def transforms_case(S):
@@ -533,7 +579,26 @@ def main(ref_root, only=()):
     mc('etaT_64x96', dict(Ra=1e4, Nx=64, Nz=96,
                                   viscosity_model='eta_T'), 6,
                ('seed', 3e-2, 1, 1), S)
+    # the headline configurations at their own lengths (long_<name>.npz):
+    # configuration 2, 200 adaptive steps on the default (legacy) route
+    if not only or 'long_etaT_64x96' in only:
+        long_march_case('etaT_64x96', dict(Ra=1e4, Nx=64, Nz=96, viscosity_model='eta_T',
+                                           deta_T=1000.0), 200, ('seed', 3e-2, 1, 1), S)
+    # configuration 3 (internally heated 2:1 box, Lx = 4 the mirror-doubled
+    # carrier, seeded noise 1e-2 in m, n <= 8): its first 60 steps
+    if not only or 'long_heated_2to1_64x96' in only:
+        long_march_case('heated_2to1_64x96',
+                        dict(Ra=1.25e4, Nx=64, Nz=96, viscosity_model='eta_T', deta_T=1000.0,
+                             Lx=4.0, internal_heating=1.5), 60,
+                        ('noise', 1e-2, 8, 8, 2025), S, every=10)
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference', tuple(sys.argv[2:]))
+    if len(sys.argv) < 2:
+        sys.exit('usage: make_golden.py <reference checkout | -> [case ...]')
+    root = sys.argv[1]
+    if root == '-':
+        root = os.environ.get('SPECMC_REFERENCE', '')
+    if not os.path.isdir(os.path.join(root, 'specmc')):
+        sys.exit('no specmc package under %r' % root)
+    main(root, tuple(sys.argv[2:]))

@@ -60,7 +60,9 @@ def test_tala_operators_match_reference(gb):
              dissipation_number=0.7, precond="legacy")
     m = api.build_model(cfg)
     assert m.tala_active and m.tala_a == g["tala_a"].item()
-    assert np.array_equal(m.rho_grid, g["rho_grid"])
+    # a host-side exp: the libm of the machine that wrote the fixture may
+    # round the last bit differently
+    np.testing.assert_allclose(m.rho_grid, g["rho_grid"], rtol=4.5e-16, atol=0.0)
     assert _rel(m.rho_c, g["rho_c"]) < 1e-15 and _rel(m.rho2_c, g["rho2_c"]) < 1e-15
     eta = m.eta_of(g["that"])
     assert _rel(eta, g["eta"]) < 1e-13

@@ -27,7 +27,8 @@ def test_basis_and_transforms():
     g = _load("transforms_16x12.npz")
     m = O.ConstModel(Ra=1e4, Nx=16, Nz=12)
     assert np.array_equal(m.D, g["D"])
-    assert np.array_equal(m.V, g["V"])
+    # cos of the host libm (CGL nodes): within an ulp of the fixture's machine
+    np.testing.assert_allclose(m.V, g["V"], rtol=0.0, atol=1e-15)
     assert _rel(m.Vi, g["Vi"]) < 1e-15
     assert _rel(m.wq, g["wq"]) < 1e-14
     assert _rel(m.grid(g["cf"]), g["grid"]) < 1e-14
@@ -76,7 +77,7 @@ def test_tala_operators():
                            dissipation_number=0.7, precond="legacy")
     m = O.build(cfg)
     assert m.tala and m.tala_a == g["tala_a"].item()
-    assert np.array_equal(m.rho_grid, g["rho_grid"])
+    np.testing.assert_allclose(m.rho_grid, g["rho_grid"], rtol=4.5e-16, atol=0.0)
     assert _rel(m.rho_c, g["rho_c"]) < 1e-15 and _rel(m.rho2_c, g["rho2_c"]) < 1e-15
     eta = m.eta_of(g["that"])
     assert _rel(eta, g["eta"]) < 1e-14

@@ -50,6 +50,39 @@ def test_noalloc_grid_matches_transform_twice(Nx, Nz):
             assert _rel(out, ref) < 1e-13, (padded, call, _rel(out, ref))
 
 
+def test_noalloc_grid_beyond_the_launch_row_limit():
+    """More Fourier modes (Nk = 65,538) and grid rows (Ng = 131,074) than one
+    launch dimension holds (65,535): the kernels stride their rows, so the
+    whole field is synthesised.  Checked against an FFT synthesis in torch
+    (Chebyshev values at the ascending CGL nodes, then irfft * Ng)."""
+    import math
+
+    import torch
+    from specmc_gb300 import _lib
+    _lib.build()
+    lib = _lib.load()
+    Nx, Nz = 131074, 4
+    Nk = Nx // 2 + 1
+    gen = torch.Generator(device="cpu").manual_seed(7)
+    cf = torch.complex(torch.randn(Nk, Nz, generator=gen, dtype=torch.float64),
+                       torch.randn(Nk, Nz, generator=gen, dtype=torch.float64))
+    cf /= (1.0 + torch.arange(Nk, dtype=torch.float64))[:, None]
+    cf = cf.cuda()
+    j = torch.arange(Nz, dtype=torch.float64)
+    xi = -torch.cos(math.pi * j / (Nz - 1))                   # 2 z_j - 1
+    T = torch.cos(torch.arange(Nz, dtype=torch.float64)[:, None] * torch.arccos(xi)[None, :])
+    X = cf @ T.to(torch.complex128).cuda()                     # (Nk, Nz) values per mode
+    ref = torch.fft.irfft(X, n=Nx, dim=0) * Nx
+    out = torch.full((Nx, Nz), float("nan"), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = lib.smc_grid_noalloc(ctypes.c_void_p(cf.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                              Nx, Nz, 0, ctypes.c_void_p(stream))
+    assert rc == 0, lib.smc_last_error()
+    torch.cuda.synchronize()
+    assert torch.isfinite(out).all()
+    assert _rel(out, ref) < 1e-11, _rel(out, ref)
+
+
 def test_noalloc_rejects_oversize_request():
     import torch
     from specmc_gb300 import _lib

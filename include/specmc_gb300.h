@@ -235,7 +235,15 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
  * "engine_phase_profile" (0/1, default 0): while the profiler is on, add the
  * engine's time between grid barriers, per phase, as profile regions named
  * "engine_stokes.<phase>" / "engine_theta.<phase>" (SM cycles of one CTA at
- * the peak clock, so a lower bound on wall time). */
+ * the peak clock, so a lower bound on wall time).
+ * "engine_batch" (0/1, SMC_MIXED handles, default 0): send the refinement
+ * solves to the device's batcher, which runs the solves of many handles in
+ * one cooperative launch (each on its own CTAs and group barrier) instead of
+ * one launch per solve; for handles stepped concurrently from several host
+ * threads (smc_march_many sets it).  "engine_batch_ctas" (>= 0): CTAs of one
+ * batched solve (0: one per Fourier row, at least 32).
+ * "engine_batch_hold_us" (>= 0, default 50; applies to the handle's device):
+ * how long the oldest queued solve waits for others before a batch starts. */
 int smc_set_option(smc_handle* h, const char* key, double value);
 
 /* RBCImplicitTheta.reset_history (implicit_theta.py:601-606). */
@@ -260,6 +268,50 @@ int smc_shape(smc_handle* h, int* Nk, int* Nx, int* Nz, int* Np);
 /* The handle's CUDA stream (cudaStream_t), for callers that order their own
  * work after the handle's. */
 void* smc_stream(smc_handle* h);
+
+/* ------------------------------------------------------------- many runs
+ * An ensemble of independent runs (uneven grids, viscosity models, Rayleigh
+ * numbers) on one GPU.  The reference runs one model per Python process and
+ * has no batch API; its driver loop per run is api.march_adaptive
+ * (specmc/api.py:169-190) with the amplitude abort threshold AMP_LIMIT
+ * (specmc/_numerics.py:139-140). */
+
+/* smc_create for each of cfgs[0 .. nruns-1] -> out[0 .. nruns-1]; on a
+ * failure every handle already made is destroyed and the error names the run. */
+int smc_create_many(const smc_config* cfgs, int nruns, smc_handle** out);
+
+enum smc_run_status {
+  SMC_RUN_OK = 0,          /* marched its steps */
+  SMC_RUN_AMPLITUDE = 1,   /* max|theta| passed amp_limit x its initial value; marched on */
+  SMC_RUN_NONFINITE = 2,   /* the state went non-finite; stopped */
+  SMC_RUN_ERROR = 3        /* a hard error; stopped (smc_march_many returns < 0) */
+};
+
+typedef struct smc_run_result {
+  long long steps;
+  double t, dt;            /* march clock and last step size */
+  double amp0, amp;        /* max |theta| on the (Nx, Nz) grid at the start / last check */
+  double seconds;          /* wall time of this run's march */
+  int status;              /* enum smc_run_status */
+  int reserved;
+} smc_run_result;
+
+/* March the resident states (smc_set_state) of nruns handles nsteps
+ * CFL-limited steps each (production_dt + step, api.march_adaptive),
+ * checking finiteness and amplitude every check_every steps.  `concurrency`
+ * host threads take the runs in order, each run on its own handle's stream.
+ * batched != 0: the SMC_MIXED handles send their Krylov refinement solves to
+ * the device's batcher, which runs the solves of many runs in one
+ * cooperative launch, each on its own CTAs (option "engine_batch"); plain
+ * handles step as usual.  Every run gets a result; the call returns < 0 if
+ * any run met a hard error (the message names the first). */
+int smc_march_many(smc_handle* const* hs, int nruns, long long nsteps, double safety,
+                   double dtmax, double amp_limit, int check_every, int concurrency,
+                   int batched, smc_run_result* res);
+
+/* Batcher statistics of `device` since the process started: cooperative
+ * launches, solves and CTAs they ran (no reference counterpart). */
+int smc_batch_stats(int device, long long* launches, long long* solves, long long* ctas);
 
 /* Grid synthesis that allocates nothing (no counterpart in the reference,
  * which has no device memory at all).  For callers that cannot allocate

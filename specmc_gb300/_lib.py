@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libspecmc_gb300.so")
 SOURCES = ("smc_spectral.cu", "smc_dense.cu", "smc_schur.cu", "smc_krylov.cu",
-           "smc_pseudo.cu", "smc_fastops.cu", "smc_engine.cu", "smc_noalloc.cu", "smc_tala.cu",
+           "smc_pseudo.cu", "smc_fastops.cu", "smc_engine.cu", "smc_noalloc.cu", "smc_tala.cu", "smc_batch.cu",
            "smc_runtime.cu")
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
               "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -123,6 +123,17 @@ class SmcMarchInfo(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_longlong), ("t", ctypes.c_double), ("dt", ctypes.c_double)]
 
 
+SMC_RUN_OK, SMC_RUN_AMPLITUDE, SMC_RUN_NONFINITE, SMC_RUN_ERROR = 0, 1, 2, 3
+RUN_STATUS = {SMC_RUN_OK: "ok", SMC_RUN_AMPLITUDE: "amplitude", SMC_RUN_NONFINITE: "non-finite",
+              SMC_RUN_ERROR: "error"}
+
+
+class SmcRunResult(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_longlong), ("t", ctypes.c_double), ("dt", ctypes.c_double),
+                ("amp0", ctypes.c_double), ("amp", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("status", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
 #: every entry point include/specmc_gb300.h declares
 EXPORTED = ("smc_config_defaults", "smc_create", "smc_destroy", "smc_step", "smc_cfl_dt",
             "smc_production_dt", "smc_march_adaptive", "smc_march", "smc_diagnostics",
@@ -130,7 +141,8 @@ EXPORTED = ("smc_config_defaults", "smc_create", "smc_destroy", "smc_step", "smc
             "smc_eta_of", "smc_schur_matvec", "smc_reset_history", "smc_counters_get",
             "smc_shape", "smc_stream", "smc_last_error", "smc_set_state", "smc_get_state",
             "smc_advance", "smc_profile", "smc_profile_get", "smc_set_option",
-            "smc_grid_noalloc", "smc_get_history", "smc_set_history", "smc_dissipation_eta")
+            "smc_grid_noalloc", "smc_get_history", "smc_set_history", "smc_dissipation_eta",
+            "smc_create_many", "smc_march_many", "smc_batch_stats")
 
 _LIB = None
 
@@ -179,6 +191,9 @@ def load(path=None):
         "smc_set_option": (i, [vp, ctypes.c_char_p, d]),
         "smc_grid_noalloc": (i, [vp, vp, i, i, i, vp]),
         "smc_profile_get": (i, [vp, i, P(ctypes.c_char_p), dp, P(ll), dp, P(i)]),
+        "smc_create_many": (i, [P(SmcConfig), i, P(vp)]),
+        "smc_march_many": (i, [P(vp), i, ll, d, d, d, i, i, i, P(SmcRunResult)]),
+        "smc_batch_stats": (i, [i, P(ll), P(ll), P(ll)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

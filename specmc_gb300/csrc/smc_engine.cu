@@ -987,23 +987,87 @@ struct EngShared {
   double b64;
 };
 
-__device__ __forceinline__ EngCtx eng_ctx(const EngineOps& op) {
+// The CTAs of one solve: the whole grid (single-solve launches) or the
+// group [cta0, cta0 + G) of a batched launch, CTA b of G.
+__device__ __forceinline__ EngCtx eng_ctx_group(const EngineOps& op, int G, int b) {
   EngCtx e;
-  e.G = gridDim.x; e.b = blockIdx.x; e.tid = threadIdx.x; e.lane = e.tid & 31; e.warp = e.tid >> 5;
+  e.G = G; e.b = b; e.tid = threadIdx.x; e.lane = e.tid & 31; e.warp = e.tid >> 5;
   e.gw = e.b * ENG_WARPS + e.warp;
   e.nw = e.G * ENG_WARPS;
   e.R = op.Nk <= e.G ? e.G / op.Nk : 1;
   e.ntask = op.Nk * e.R;
   return e;
 }
+__device__ __forceinline__ EngCtx eng_ctx(const EngineOps& op) {
+  return eng_ctx_group(op, gridDim.x, blockIdx.x);
+}
+
+// Barrier over the CTAs of one solve.  GridBar: the cooperative grid barrier
+// of a single-solve launch.  GroupBar: the CTAs of one solve inside a batched
+// launch (every CTA of the launch is co-resident: cooperative launch) meet on
+// an arrival counter and a generation word of their own in global memory, so
+// the solves of a batch never wait for one another.  Thread 0 of each CTA
+// arrives (release), the last arrival resets the counter and advances the
+// generation (release), the others wait for the generation to move
+// (acquire).  The wait is bounded: after timeout_ns of %globaltimer the CTA
+// raises the group's *err (and the launch's *any) and stops waiting, and
+// every later barrier of that group returns at once, so a group whose
+// barrier could not complete still ends (all loops of a solve are bounded),
+// its result is marked failed and the host reports the error; the other
+// groups of the launch are not affected.
+struct GridBar {
+  cg::grid_group g;
+  __device__ void sync() { g.sync(); }
+};
+
+struct GroupBar {
+  unsigned int* cnt;
+  unsigned int* gen;
+  int G;
+  int* err;
+  int* any;
+  long long timeout_ns;
+  __device__ void sync() {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned int my;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(my) : "l"(gen) : "memory");
+      __threadfence();
+      unsigned int arrived;
+      asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;"
+                   : "=r"(arrived) : "l"(cnt) : "memory");
+      if (arrived == (unsigned int)G - 1) {
+        asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(cnt) : "memory");
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(gen), "r"(my + 1u) : "memory");
+      } else {
+        const long long t0 = global_ns();
+        unsigned int now = my;
+        int spins = 0;
+        while (true) {
+          asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(now) : "l"(gen) : "memory");
+          if (now != my) break;
+          if (*(volatile int*)err) break;
+          if ((++spins & 63) == 0 && global_ns() - t0 > timeout_ns) {
+            atomicExch(err, 1);
+            atomicExch(any, 1);
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+      __threadfence();
+    }
+    __syncthreads();
+  }
+};
 
 // One right-preconditioned FGMRES solve of A x = io.b (x -> io.x, FP64) to
 // the relative tolerance io.rtol within io.maxiter Arnoldi steps; every CTA
 // of the cooperative grid calls it.  -> info (0 converged, 1 not, 2
 // breakdown, 3 non-finite data) and the Arnoldi steps taken.
-template <class T>
+template <class T, class Bar>
 __device__ void fgmres_solve(const EngineOps& op, const EngineIO& io, EngShared<T>& Q,
-                             unsigned char* smraw, const EngCtx& e, cg::grid_group& grid,
+                             unsigned char* smraw, const EngCtx& e, Bar& grid,
                              PhaseClock& pc, int& info_out, int& total_out) {
   using C = Cx<T>;
   T* sh = Q.sh;
@@ -1252,14 +1316,14 @@ __device__ void fgmres_solve(const EngineOps& op, const EngineIO& io, EngShared<
 
 template <class T>
 __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(EngineOps op, EngineIO io) {
-  cg::grid_group grid = cg::this_grid();
+  GridBar grid{cg::this_grid()};
   extern __shared__ __align__(256) unsigned char smraw[];
   __shared__ EngShared<T> Q;
   const EngCtx e = eng_ctx(op);
   PhaseClock pc;
   pc.init(io.phase_cycles, e);
   int info = 1, total = 0;
-  fgmres_solve<T>(op, io, Q, smraw, e, grid, pc, info, total);
+  fgmres_solve<T, GridBar>(op, io, Q, smraw, e, grid, pc, info, total);
   if (e.b == 0 && e.tid == 0) {
     io.result[0] = info;
     io.result[1] = total;
@@ -1267,21 +1331,27 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_fgmres_engine_kernel(Engin
   pc.finish();
 }
 
-// Iterative refinement in one launch: FP64 outer residuals r = b - A64 x
+// Iterative refinement of one solve: FP64 outer residuals r = b - A64 x
 // (the FP64 operator phases), FP32 inner FGMRES solves of A32 e = r to
 // max(0.3 tol / ||r||, floor), x += e, until ||r|| <= rtol ||b||, at most 12
-// outer passes and maxiter inner Arnoldi steps in all.
-__global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_engine_kernel(EngineOps op32, EngineOps op64,
-                                                                           EngineIO io, RefineIO rf) {
-  cg::grid_group grid = cg::this_grid();
-  extern __shared__ __align__(256) unsigned char smraw[];
-  __shared__ EngShared<float> Q;
-  __shared__ double s_red[8];
-  __shared__ double s_part[ENG_WARPS];
-  __shared__ double s_nacc64;
-  const EngCtx e = eng_ctx(op32);
-  PhaseClock pc;
-  pc.init(io.phase_cycles, e);
+// outer passes and maxiter inner Arnoldi steps in all.  -> info, inner
+// steps, outer passes, final relative residual (in the caller's registers).
+struct RefineShared {
+  EngShared<float> Q;
+  double red[8];
+  double part[ENG_WARPS];
+  double nacc64;
+};
+
+template <class Bar>
+__device__ void refine_solve(const EngineOps& op32, const EngineOps& op64, const EngineIO& io,
+                             const RefineIO& rf, RefineShared& RS, unsigned char* smraw,
+                             const EngCtx& e, Bar& grid, PhaseClock& pc, int& info_out,
+                             int& total_out, int& outer_out, double& rel_out) {
+  EngShared<float>& Q = RS.Q;
+  double* s_red = RS.red;
+  double* s_part = RS.part;
+  double& s_nacc64 = RS.nacc64;
   const long long n = io.n;
   const long long per = (n + e.G - 1) / e.G;
   const long long lo = (long long)e.b * per, hi = min(n, lo + per);
@@ -1324,7 +1394,7 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_engine_kernel(Engin
     in.rtol = fmax(0.3 * tol / beta, rf.floor);
     in.maxiter = rf.maxiter - total;
     int inf = 1, its = 0;
-    fgmres_solve<float>(op32, in, Q, smraw, e, grid, pc, inf, its);
+    fgmres_solve<float, Bar>(op32, in, Q, smraw, e, grid, pc, inf, its);
     total += its;
     if (inf == 3) { info = 3; break; }
     for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
@@ -1354,13 +1424,66 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_engine_kernel(Engin
     if (its == 0 && beta > tol) break;             // no progress possible
   }
   if (beta <= tol && info != 3) info = 0;
+  info_out = info;
+  total_out = total;
+  outer_out = outer;
+  rel_out = beta / fmax(bn, 1e-300);
+}
+
+// The whole refinement of one solve in one cooperative launch.
+__global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_engine_kernel(EngineOps op32, EngineOps op64,
+                                                                           EngineIO io, RefineIO rf) {
+  GridBar grid{cg::this_grid()};
+  extern __shared__ __align__(256) unsigned char smraw[];
+  __shared__ RefineShared RS;
+  const EngCtx e = eng_ctx(op32);
+  PhaseClock pc;
+  pc.init(io.phase_cycles, e);
+  int info = 1, total = 0, outer = 0;
+  double rel = 0.0;
+  refine_solve<GridBar>(op32, op64, io, rf, RS, smraw, e, grid, pc, info, total, outer, rel);
   if (e.b == 0 && e.tid == 0) {
     io.result[0] = info;
     io.result[1] = total;
     io.result[2] = outer;
-    rf.res[0] = beta / fmax(bn, 1e-300);
+    rf.res[0] = rel;
   }
   pc.finish();
+}
+
+// The refinement solves of up to ENGINE_BATCH_MAX independent systems (any
+// mix of Schur and temperature operators and grid sizes) in one cooperative
+// launch: job j owns the CTAs [cta0, cta0 + G) and its own group barrier.
+// When its solve has ended, CTA 0 of the group -- after a last group barrier,
+// so no CTA of the group touches the job's buffers any more -- writes the
+// result block to host-mapped memory and then the done word, so the host
+// thread that owns the job can go on while the other solves of the batch run.
+__global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_batch_kernel(
+    const __grid_constant__ RefineBatch B) {
+  extern __shared__ __align__(256) unsigned char smraw[];
+  __shared__ RefineShared RS;
+  int j = 0;
+  while (j + 1 < B.njobs && (int)blockIdx.x >= B.job[j + 1].cta0) ++j;
+  const RefineJob& J = B.job[j];
+  const EngCtx e = eng_ctx_group(J.op32, J.G, (int)blockIdx.x - J.cta0);
+  GroupBar bar{J.bar, J.bar + 1, J.G, reinterpret_cast<int*>(J.bar + 2), B.err, B.timeout_ns};
+  PhaseClock pc;
+  pc.init(nullptr, e);
+  int info = 1, total = 0, outer = 0;
+  double rel = 0.0;
+  refine_solve<GroupBar>(J.op32, J.op64, J.io, J.rf, RS, smraw, e, bar, pc, info, total, outer,
+                         rel);
+  bar.sync();
+  if (e.b == 0 && e.tid == 0) {
+    volatile EngineJobResult* out = J.out;
+    out->info = info;
+    out->iters = total;
+    out->outer = outer;
+    out->rel = rel;
+    out->failed = *(volatile int*)(J.bar + 2);
+    __threadfence_system();
+    out->done = J.seq;
+  }
 }
 
 template <class T>
@@ -1425,6 +1548,35 @@ void fgmres_refine_engine(const Ctx& c, const EngineOps& op32, const EngineOps& 
   CoopGuard guard(c.s);
   SMC_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(G), dim3(ENG_THREADS), args, sm, c.s));
   SMC_LAUNCH_CHECK(c);
+}
+
+size_t refine_engine_smem(const EngineOps& op32, const EngineOps& op64) {
+  const size_t s32 = engine_smem<float>(op32), s64 = engine_smem<double>(op64);
+  return s32 > s64 ? s32 : s64;
+}
+
+int refine_batch_capacity(size_t smem, int num_sms) {
+  auto kern = smc_refine_batch_kernel;
+  allow_max_smem((const void*)kern);
+  int per_sm = 0;
+  SMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ENG_THREADS, smem));
+  return per_sm * num_sms;
+}
+
+void refine_batch_launch(cudaStream_t s, const RefineBatch& B, size_t smem) {
+  auto kern = smc_refine_batch_kernel;
+  allow_max_smem((const void*)kern);
+  int G = 0;
+  for (int j = 0; j < B.njobs; ++j) {
+    if (B.job[j].cta0 != G) throw std::runtime_error("refine batch: CTA ranges not contiguous");
+    if (B.job[j].io.restart + 1 > ENG_MAXM) throw std::runtime_error("refine batch: restart above 99");
+    if (B.job[j].G > B.job[j].io.max_grid) throw std::runtime_error("refine batch: partials too small");
+    G += B.job[j].G;
+  }
+  RefineBatch b = B;
+  void* args[] = {(void*)&b};
+  SMC_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(G), dim3(ENG_THREADS), args, smem, s));
+  SMC_CUDA(cudaGetLastError());
 }
 
 void fgmres_engine(const Ctx& c, const EngineOps& op, const EngineIO& io, bool fp32) {

@@ -116,6 +116,46 @@ struct RefineIO {
 void fgmres_refine_engine(const Ctx& c, const EngineOps& op32, const EngineOps& op64,
                           const EngineIO& io, const RefineIO& rf);
 
+// ------------------------------------------------------ batched refinement
+// Result block of one batched solve, in host-mapped pinned memory: the
+// kernel writes the fields, then (after a system-scope fence) `done` = the
+// job's sequence number, which the owning host thread polls.
+struct EngineJobResult {
+  volatile int done;
+  int info, iters, outer, failed;
+  double rel;
+};
+
+// One solve of a batched launch: the operators and workspace of its handle
+// (exactly what fgmres_refine_engine takes), its CTA range [cta0, cta0 + G),
+// three zero-initialised words of global memory for its group barrier
+// (arrivals, generation, timeout flag), and the device address of its
+// result block.
+struct RefineJob {
+  EngineOps op32, op64;
+  EngineIO io;
+  RefineIO rf;
+  unsigned int* bar = nullptr;
+  EngineJobResult* out = nullptr;
+  int seq = 0;
+  int cta0 = 0, G = 0;
+};
+
+constexpr int ENGINE_BATCH_MAX = 16;
+struct RefineBatch {
+  RefineJob job[ENGINE_BATCH_MAX];
+  int njobs = 0;
+  int* err = nullptr;             // raised when any group barrier timed out
+  long long timeout_ns = 2000000000LL;
+};
+
+// dynamic shared memory of a refinement solve (the larger of its two operators)
+size_t refine_engine_smem(const EngineOps& op32, const EngineOps& op64);
+// co-resident CTAs of the batched kernel at `smem` bytes of dynamic smem
+int refine_batch_capacity(size_t smem, int num_sms);
+// one cooperative launch of the jobs of B (cta0 contiguous from 0) on stream s
+void refine_batch_launch(cudaStream_t s, const RefineBatch& B, size_t smem);
+
 // out[b][c][r] = (To) in[b][r][c] for batch matrices of rows x cols
 void transpose_as(const Ctx& c, const double* in, float* out, long long rows, long long cols, int batch);
 void transpose_as(const Ctx& c, const double* in, double* out, long long rows, long long cols, int batch);

@@ -10,6 +10,8 @@
 // exactly where the reference takes them; all vector and matrix work stays
 // on the device, on the handle's stream.
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -19,6 +21,8 @@
 #include <type_traits>
 #include <vector>
 #include <set>
+#include <mutex>
+#include <thread>
 
 #include "../../include/specmc_gb300.h"
 #include "smc_internal.cuh"
@@ -27,6 +31,7 @@
 #include "smc_pseudo.cuh"
 #include "smc_fastops.cuh"
 #include "smc_engine.cuh"
+#include "smc_batch.cuh"
 #include "smc_tala.cuh"
 
 namespace smc {
@@ -407,6 +412,70 @@ struct Model {
   long long* dEngPhase = nullptr;    // ENGINE_PHASES accumulators
   double* dEngRes = nullptr;         // final relative residual of a refinement launch
   double sm_khz = 0.0;               // peak SM clock (cycles -> ms)
+  // batched mode: the refinement solves go to the device's batcher, which
+  // runs the solves of many handles in one cooperative launch (smc_batch.cu)
+  bool batch_mode = false;
+  int batch_ctas = 0;                // CTAs of one solve in a batch (0: the default)
+  unsigned int* dBatchBar = nullptr; // group barrier words (zeroed)
+  EngineJobResult* hBatchRes = nullptr;   // host-mapped result block
+  EngineJobResult* dBatchRes = nullptr;   // its device address
+  cudaEvent_t batch_ready = nullptr;
+  int batch_seq = 0;
+  long long n_batched = 0;           // solves this handle ran through the batcher
+
+  void enable_batch(bool on) {
+    if (on && !fast) throw std::runtime_error("engine_batch needs a SMC_MIXED handle");
+    if (on && !dBatchBar) {
+      dBatchBar = mem.alloc<unsigned int>(4);
+      SMC_CUDA(cudaHostAlloc((void**)&hBatchRes, sizeof(EngineJobResult), cudaHostAllocMapped));
+      std::memset((void*)hBatchRes, 0, sizeof(EngineJobResult));
+      SMC_CUDA(cudaHostGetDevicePointer((void**)&dBatchRes, (void*)hBatchRes, 0));
+      SMC_CUDA(cudaEventCreateWithFlags(&batch_ready, cudaEventDisableTiming));
+      SMC_CUDA(cudaStreamSynchronize(stream));       // the zeroed barrier words
+    }
+    batch_mode = on;
+  }
+
+  // CTAs of one batched solve: a share of the GPU that lets several solves
+  // run side by side -- one CTA per Fourier row, and at least 32
+  int batch_grid(int kind) const {
+    if (batch_ctas > 0) return batch_ctas;
+    (void)kind;
+    return std::max(32, std::min(Nk, 2 * ctx.num_sms));
+  }
+
+  // one refinement solve through the batcher: queue it, wait for its result
+  FgmresResult batch_refine(int kind, const EngineOps& op32, const EngineOps& op64,
+                            const EngineIO& io, const RefineIO& rf, double* true_res) {
+    BatchReq r;
+    r.job.op32 = op32;
+    r.job.op64 = op64;
+    r.job.io = io;
+    r.job.rf = rf;
+    r.job.bar = dBatchBar;
+    r.job.out = dBatchRes;
+    r.job.seq = ++batch_seq;
+    r.G = std::min(batch_grid(kind), io.max_grid);
+    r.smem = refine_engine_smem(op32, op64);
+    r.ready = batch_ready;
+    r.host = hBatchRes;
+    hBatchRes->failed = 0;
+    SMC_CUDA(cudaEventRecord(batch_ready, stream));
+    batch_submit(device, &r);
+    batch_wait(&r, 600.0);
+    if (hBatchRes->failed)
+      throw std::runtime_error(hBatchRes->failed == 1
+                                   ? "batched engine: a group barrier timed out"
+                                   : "batched engine: the batch could not be launched");
+    ctx.count();
+    ++n_batched;
+    FgmresResult fr;
+    fr.info = hBatchRes->info;
+    fr.iters = hBatchRes->iters;
+    n_outer += hBatchRes->outer;
+    if (true_res) *true_res = hBatchRes->rel;
+    return fr;
+  }
 
   // ------------------------------------------------------------ utilities
   void sync_read(const double* d, int count) {
@@ -1068,6 +1137,11 @@ struct Model {
     RefineIO rf;
     rf.b = b; rf.x = x; rf.r = dRefR; rf.e = dRefE;
     rf.rtol = rtol; rf.floor = inner_floor[kind]; rf.maxiter = maxiter; rf.res = dEngRes;
+    if (batch_mode) {
+      FgmresResult fr = batch_refine(kind, op32, op64, io, rf, true_res);
+      ps.work = engine_bytes(kind, true, fr.iters, io.restart);
+      return fr;
+    }
     const bool phases = eng_phase && prof.enabled;
     if (phases) {
       SMC_CUDA(cudaMemsetAsync(dEngPhase, 0, ENGINE_PHASES * sizeof(long long), stream));
@@ -1935,6 +2009,8 @@ struct Model {
     if (stream) { cudaStreamSynchronize(stream); cudaStreamDestroy(stream); }
     if (hbuf) cudaFreeHost(hbuf);
     if (hpin) cudaFreeHost(hpin);
+    if (hBatchRes) cudaFreeHost((void*)hBatchRes);
+    if (batch_ready) cudaEventDestroy(batch_ready);
   }
 };
 
@@ -2076,6 +2152,7 @@ int smc_destroy(smc_handle* h) {
 int smc_step(smc_handle* h, const double* in, double* out, int mem, double dt) {
   SMC_GUARD(h, {
     Model& m = h->m;
+    smc::BatchScope bs(m.device, m.batch_mode);
     copy_in(m, m.dIn, in, mem, m.n);
     m.step(m.dIn, m.dOut, dt);
     copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
@@ -2086,6 +2163,7 @@ int smc_cfl_dt(smc_handle* h, const double* in, int mem, double safety, double d
                double* dt_out) {
   SMC_GUARD(h, {
     Model& m = h->m;
+    smc::BatchScope bs(m.device, m.batch_mode);
     copy_in(m, m.dIn, in, mem, m.n);
     *dt_out = m.cfl_dt(m.dIn, safety, dtmax, dtmin);
   })
@@ -2095,6 +2173,7 @@ int smc_production_dt(smc_handle* h, const double* in, int mem, double safety, d
                       double* dt_out) {
   SMC_GUARD(h, {
     Model& m = h->m;
+    smc::BatchScope bs(m.device, m.batch_mode);
     copy_in(m, m.dIn, in, mem, m.n);
     *dt_out = m.production_dt(m.dIn, safety, dtmax);
   })
@@ -2104,6 +2183,7 @@ int smc_march_adaptive(smc_handle* h, const double* in, double* out, int mem, do
                        double safety, double dtmax, long long max_steps, smc_march_info* info) {
   SMC_GUARD(h, {
     Model& m = h->m;
+    smc::BatchScope bs(m.device, m.batch_mode);
     copy_in(m, m.dS0, in, mem, m.n);
     double2* cur = m.dS0;
     double2* nxt = m.dS1;
@@ -2138,10 +2218,11 @@ int smc_get_state(smc_handle* h, double* out, int mem) {
   })
 }
 
-int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety, double dtmax,
-                smc_march_info* info) {
-  SMC_GUARD(h, {
-    Model& m = h->m;
+namespace smc {
+// CFL-limited steps of the resident state until t >= tstop or max_steps
+// (the loop of api.march_adaptive, api.py:179-189)
+void advance_resident(Model& m, double tstop, long long max_steps, double safety, double dtmax,
+                      smc_march_info* info) {
     double2* cur = m.resident_cur0 ? m.dS0 : m.dS1;
     double2* nxt = m.resident_cur0 ? m.dS1 : m.dS0;
     double dt = NAN;
@@ -2161,6 +2242,15 @@ int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety,
       ++steps;
     }
     if (info) { info->steps = steps; info->t = m.t_resident; info->dt = dt; }
+}
+}  // namespace smc
+
+int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety, double dtmax,
+                smc_march_info* info) {
+  SMC_GUARD(h, {
+    Model& m = h->m;
+    smc::BatchScope bs(m.device, m.batch_mode);
+    smc::advance_resident(m, tstop, max_steps, safety, dtmax, info);
   })
 }
 
@@ -2193,6 +2283,7 @@ int smc_profile_get(smc_handle* h, int slot, const char** name, double* ms, long
 int smc_march(smc_handle* h, const double* in, double* out, int mem, double dt, long long nsteps) {
   SMC_GUARD(h, {
     Model& m = h->m;
+    smc::BatchScope bs(m.device, m.batch_mode);
     copy_in(m, m.dS0, in, mem, m.n);
     double2* cur = m.dS0;
     double2* nxt = m.dS1;
@@ -2338,6 +2429,14 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
       h->m.eng_ctas = (int)value;
     } else if (k == "engine_phase_profile") {
       h->m.eng_phase = value != 0.0;
+    } else if (k == "engine_batch") {
+      h->m.enable_batch(value != 0.0);
+    } else if (k == "engine_batch_ctas") {
+      if (!(value >= 0.0 && value <= 1e6)) throw std::runtime_error("engine_batch_ctas must be >= 0");
+      h->m.batch_ctas = (int)value;
+    } else if (k == "engine_batch_hold_us") {
+      if (!(value >= 0.0 && value <= 1e6)) throw std::runtime_error("engine_batch_hold_us must be >= 0");
+      smc::batch_set_hold_us(h->m.device, value);
     } else throw std::runtime_error("unknown option " + k);
   })
 }
@@ -2393,3 +2492,141 @@ void* smc_stream(smc_handle* h) { return h ? (void*)h->m.stream : nullptr; }
 const char* smc_last_error(void) { return smc::g_last_error.c_str(); }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ many runs
+namespace smc {
+
+// out[0] = max |g|, out[1] = number of non-finite entries (one CTA)
+__global__ void smc_maxabs_finite_kernel(const double* __restrict__ g, long long n,
+                                         double* __restrict__ out) {
+  __shared__ double sm[32];
+  __shared__ int sb[32];
+  double m = 0.0;
+  int bad = 0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = g[i];
+    if (!isfinite(v)) ++bad;
+    else m = fmax(m, fabs(v));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    bad += __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) { sm[threadIdx.x >> 5] = m; sb[threadIdx.x >> 5] = bad; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0;
+    int b = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a = fmax(a, sm[w]); b += sb[w]; }
+    out[0] = a;
+    out[1] = (double)b;
+  }
+}
+
+// max |theta| on the (Nx, Nz) grid of the resident state; -1 if any value
+// of the state's grid is not finite
+double resident_amplitude(Model& m) {
+  const double2* cur = m.resident_cur0 ? m.dS0 : m.dS1;
+  m.synth(cur, m.dV, KFactor(), m.gr[0], m.Nx, m.sp[0]);
+  smc_maxabs_finite_kernel<<<1, 512, 0, m.stream>>>(m.gr[0], (long long)m.Nx * m.N, m.dScal);
+  SMC_LAUNCH_CHECK(m.ctx);
+  m.sync_read(m.dScal, 2);
+  return m.hbuf[1] > 0.0 ? -1.0 : m.hbuf[0];
+}
+
+}  // namespace smc
+
+int smc_create_many(const smc_config* cfgs, int nruns, smc_handle** out) {
+  if (!cfgs || !out || nruns < 0) {
+    smc::set_last_error("smc_create_many: null argument or negative count");
+    return -1;
+  }
+  for (int i = 0; i < nruns; ++i) out[i] = nullptr;
+  for (int i = 0; i < nruns; ++i) {
+    const int rc = smc_create(&cfgs[i], &out[i]);
+    if (rc != 0) {
+      const std::string msg = "run " + std::to_string(i) + ": " + smc_last_error();
+      for (int j = 0; j < i; ++j) { smc_destroy(out[j]); out[j] = nullptr; }
+      smc::set_last_error(msg.c_str());
+      return rc;
+    }
+  }
+  return 0;
+}
+
+int smc_march_many(smc_handle* const* hs, int nruns, long long nsteps, double safety,
+                   double dtmax, double amp_limit, int check_every, int concurrency,
+                   int batched, smc_run_result* res) {
+  using namespace smc;
+  try {
+    if (!hs || !res || nruns < 0) throw std::runtime_error("smc_march_many: null argument");
+    for (int i = 0; i < nruns; ++i)
+      if (!hs[i]) throw std::runtime_error("smc_march_many: null handle " + std::to_string(i));
+    if (check_every < 1) check_every = 1;
+    if (concurrency < 1) concurrency = 1;
+    concurrency = std::min(concurrency, std::max(nruns, 1));
+    for (int i = 0; i < nruns; ++i) {
+      Model& m = hs[i]->m;
+      if (batched && m.fast) {
+        SMC_CUDA(cudaSetDevice(m.device));
+        m.enable_batch(true);
+      }
+    }
+    std::atomic<int> next{0};
+    std::mutex err_mu;
+    std::string first_err;
+    auto worker = [&]() {
+      while (true) {
+        const int i = next.fetch_add(1);
+        if (i >= nruns) break;
+        smc_run_result& r = res[i];
+        std::memset(&r, 0, sizeof(r));
+        r.status = SMC_RUN_OK;
+        Model& m = hs[i]->m;
+        try {
+          SMC_CUDA(cudaSetDevice(m.device));
+          BatchScope bs(m.device, m.batch_mode);
+          const auto t0 = std::chrono::steady_clock::now();
+          r.amp0 = resident_amplitude(m);
+          r.amp = r.amp0;
+          if (r.amp0 < 0.0) r.status = SMC_RUN_NONFINITE;
+          smc_march_info info{};
+          while (r.status != SMC_RUN_NONFINITE && r.steps < nsteps) {
+            const long long k = std::min<long long>(check_every, nsteps - r.steps);
+            advance_resident(m, INFINITY, k, safety, dtmax, &info);
+            r.steps += info.steps;
+            r.t = info.t;
+            r.dt = info.dt;
+            const double a = resident_amplitude(m);
+            if (a < 0.0 || !std::isfinite(info.t)) { r.status = SMC_RUN_NONFINITE; break; }
+            r.amp = a;
+            if (r.status == SMC_RUN_OK && amp_limit > 0.0 && a > amp_limit * r.amp0)
+              r.status = SMC_RUN_AMPLITUDE;
+            if (info.steps < k) break;
+          }
+          r.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        } catch (const std::exception& e) {
+          r.status = SMC_RUN_ERROR;
+          std::lock_guard<std::mutex> lk(err_mu);
+          if (first_err.empty()) first_err = "run " + std::to_string(i) + ": " + e.what();
+        }
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < concurrency; ++t) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    if (!first_err.empty()) throw std::runtime_error(first_err);
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(e);
+  }
+}
+
+int smc_batch_stats(int device, long long* launches, long long* solves, long long* ctas) {
+  try {
+    smc::batch_stats(device, launches, solves, ctas);
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(e);
+  }
+}

@@ -1,10 +1,12 @@
 """Ensembles of independent runs on one GPU (the batched workload).
 
-Each run is its own model handle with its own CUDA stream; a pool of host
-threads drives them (the native calls release the GIL), so the kernels of
-different runs overlap on the GPU.  The persistent Krylov engine of a handle
-normally spreads over every SM; in an ensemble each handle's engine is capped
-at its share of the SMs so that the concurrent runs fit side by side.
+Each run is its own model handle with its own CUDA stream.  The native
+driver (``smc_march_many``, the default) marches all handles from a pool of
+C++ threads; in the mixed form their Krylov refinement solves go to the
+device's batcher, which runs the solves of many runs in one cooperative
+launch, each run on its own CTAs with its own group barrier.  The Python
+driver (``native=False``) drives the handles from Python threads instead,
+each handle's engine capped at its share of the SMs.
 
 The runs are independent -- nothing is exchanged between them while they
 step -- so an ensemble shards across GPUs by partitioning the run list: one
@@ -28,8 +30,8 @@ from . import _lib, api
 from . import _numerics as NUM
 from .config import ConvectionConfig
 
-__all__ = ["GRIDS", "MODELS", "ensemble_configs", "march_ensemble", "march_ensemble_sharded",
-           "shard", "device_sms"]
+__all__ = ["GRIDS", "MODELS", "ensemble_configs", "march_ensemble", "march_ensemble_native",
+           "march_ensemble_sharded", "shard", "device_sms"]
 
 GRIDS = ((32, 24), (64, 48), (64, 96), (128, 96))
 MODELS = ("const", "eta_z", "eta_T")
@@ -114,6 +116,68 @@ def _march_one(run, nsteps, form, device, cap, safety, dtmax, chunk, max_wall, o
                     flagged=status != "ok", status=status, counters=model.counters())
     finally:
         model.close()
+
+
+def march_ensemble_native(runs, nsteps=100, form="mixed", concurrency=16, safety=None,
+                          dtmax=None, device=0, batched=True, check_every=5, overrides=None,
+                          batch_ctas=None, keep_states=True):
+    """March every run of ``runs`` for ``nsteps`` CFL-limited steps in one
+    native call (``smc_march_many``: ``concurrency`` C++ threads; with
+    ``batched`` the mixed form's refinement solves of all runs go through the
+    device's batcher).  Every run is checked every ``check_every`` steps: a
+    non-finite state stops it ('non-finite'); max|theta| above AMP_LIMIT x its
+    initial value flags it ('amplitude', the reference driver's abort
+    threshold, specmc/_numerics.py:139-140) and it marches on.  No run is cut
+    short for time.  Returns one result dict per run (as march_ensemble) and,
+    under the key ``"_timing"`` of the first, the march's wall time and the
+    batcher's launch statistics."""
+    safety = NUM.CFL_SAFETY if safety is None else float(safety)
+    dtmax = NUM.DTMAX if dtmax is None else float(dtmax)
+    lib = _lib.load()
+    models, t_build = [], []
+    try:
+        for run in runs:
+            t0 = time.perf_counter()
+            model = _build(run["cfg"], form, device, overrides)
+            models.append(model)
+            if batch_ctas and model.form == "mixed":
+                # CTAs per solve, batched or not
+                _lib.check(lib.smc_set_option(model._h, b"engine_batch_ctas", float(batch_ctas)))
+                _lib.check(lib.smc_set_option(model._h, b"engine_ctas", float(batch_ctas)))
+            th = np.ascontiguousarray(model.seed(amp=run["amp"], m=run["m"], n=run["n"]))
+            _lib.check(lib.smc_set_state(model._h, th.ctypes.data_as(ctypes.c_void_p),
+                                         _lib.SMC_HOST))
+            t_build.append(time.perf_counter() - t0)
+        hs = (ctypes.c_void_p * len(models))(*[m._h for m in models])
+        res = (_lib.SmcRunResult * len(models))()
+        b0 = [ctypes.c_longlong() for _ in range(3)]
+        _lib.check(lib.smc_batch_stats(int(device), *[ctypes.byref(x) for x in b0]))
+        t0 = time.perf_counter()
+        _lib.check(lib.smc_march_many(hs, len(models), int(nsteps), safety, dtmax,
+                                      float(NUM.AMP_LIMIT), int(check_every), int(concurrency),
+                                      1 if batched else 0, res))
+        wall = time.perf_counter() - t0
+        b1 = [ctypes.c_longlong() for _ in range(3)]
+        _lib.check(lib.smc_batch_stats(int(device), *[ctypes.byref(x) for x in b1]))
+        out = []
+        for i, (model, r) in enumerate(zip(models, res)):
+            s = np.empty((model.Nk, model.Nz), dtype=np.complex128)
+            _lib.check(lib.smc_get_state(model._h, s.ctypes.data_as(ctypes.c_void_p), _lib.SMC_HOST))
+            finite = bool(np.all(np.isfinite(s)))
+            status = _lib.RUN_STATUS[int(r.status)]
+            out.append(dict(steps=int(r.steps), t=float(r.t), dt=float(r.dt), build_s=t_build[i],
+                            march_s=float(r.seconds), state=s if keep_states else None,
+                            diag=model.diagnostics(s) if finite else {}, finite=finite,
+                            flagged=status != "ok", status=status, amp0=float(r.amp0),
+                            amp=float(r.amp), counters=model.counters()))
+        if out:
+            out[0]["_timing"] = dict(wall_s=wall, batch_launches=b1[0].value - b0[0].value,
+                                     batch_solves=b1[1].value - b0[1].value,
+                                     batch_ctas=b1[2].value - b0[2].value)
+        return out
+    finally:
+        for model in models:
+            model.close()
 
 
 def march_ensemble(runs, nsteps=100, form="mixed", concurrency=8, safety=None, dtmax=None,
@@ -218,7 +282,11 @@ def _main(argv=None):
     ap.add_argument("--concurrency", type=int, default=8)
     ap.add_argument("--engine-ctas", type=int, default=None)
     ap.add_argument("--max-wall", type=float, default=None,
-                    help="seconds after which a run stops, flagged 'time'")
+                    help="seconds after which a run stops, flagged 'time' (Python driver)")
+    ap.add_argument("--driver", default="native", choices=("native", "python"),
+                    help="native: smc_march_many (C++ threads, batched engine); "
+                         "python: Python threads, one engine launch per solve")
+    ap.add_argument("--no-batch", action="store_true", help="native driver without the batcher")
     a = ap.parse_args(argv)
     import os
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -231,9 +299,14 @@ def _main(argv=None):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", init_method="env://", world_size=world, rank=rank)
     t0 = time.perf_counter()
-    res = march_ensemble_sharded(runs, nsteps=a.steps, rank=rank, world=world, form=a.form,
-                                 concurrency=a.concurrency, engine_ctas=a.engine_ctas,
-                                 max_wall=a.max_wall, device=local)
+    if a.driver == "native":
+        res = march_ensemble_sharded(runs, nsteps=a.steps, rank=rank, world=world, form=a.form,
+                                     concurrency=a.concurrency, device=local,
+                                     batched=not a.no_batch, march=march_ensemble_native)
+    else:
+        res = march_ensemble_sharded(runs, nsteps=a.steps, rank=rank, world=world, form=a.form,
+                                     concurrency=a.concurrency, engine_ctas=a.engine_ctas,
+                                     max_wall=a.max_wall, device=local)
     wall = time.perf_counter() - t0
     if world > 1:
         import torch
@@ -249,8 +322,10 @@ def _main(argv=None):
     for run, r in zip(runs, res):
         by["%dx%d %s" % (run["cfg"].Nx, run["cfg"].Nz, run["cfg"].viscosity_model)].append(
             1e3 * r["march_s"] / max(r["steps"], 1))
+    timing = res[0].get("_timing") if res and res[0] else None
     print(json.dumps(dict(
         runs=len(runs), n_gpus=world, steps=steps, wall_s=wall, steps_per_s=steps / wall, form=a.form,
+        driver=a.driver, batched=a.driver == "native" and not a.no_batch, march=timing,
         concurrency=a.concurrency, build_s=sum(r["build_s"] for r in res),
         status=dict(collections.Counter(r["status"] for r in res)),
         median_ms_per_step={k: float(np.median(v)) for k, v in sorted(by.items())})))

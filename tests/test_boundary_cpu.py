@@ -226,7 +226,7 @@ int main(void) {
 
 def test_ctypes_mirrors_match_the_c_structs(tmp_path):
     """Every field of the Python mirrors of smc_config, smc_diag,
-    smc_counters and smc_march_info sits at the offset the C compiler gives
+    smc_counters, smc_march_info and smc_run_result sits at the offset the C compiler gives
     it, and the structs have the same size (a mismatch would silently corrupt
     every call)."""
     import ctypes
@@ -237,7 +237,8 @@ def test_ctypes_mirrors_match_the_c_structs(tmp_path):
     if gcc is None:
         pytest.skip("no C compiler")
     mirrors = {"smc_config": _lib.SmcConfig, "smc_diag": _lib.SmcDiag,
-               "smc_counters": _lib.SmcCounters, "smc_march_info": _lib.SmcMarchInfo}
+               "smc_counters": _lib.SmcCounters, "smc_march_info": _lib.SmcMarchInfo,
+               "smc_run_result": _lib.SmcRunResult}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "specmc_gb300.h"',
              'int main(void) {']
     for cname, py in mirrors.items():

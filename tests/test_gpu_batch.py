@@ -42,7 +42,9 @@ def test_batched_equals_one_launch_per_solve(ens):
     assert timing["batch_solves"] > timing["batch_launches"]
     b = ensemble.march_ensemble_native(runs, batched=False, overrides=None, **kw)
     for x, y, run in zip(a, b, runs):
-        assert x["status"] == y["status"] == "ok", (x["status"], y["status"])
+        # "amplitude" flags physical growth past 5x the seed (the run marches on)
+        assert x["status"] == y["status"] and x["status"] in ("ok", "amplitude"), \
+            (x["status"], y["status"])
         assert x["steps"] == y["steps"] == 6
         assert np.array_equal(x["state"], y["state"]), run["cfg"]
 
@@ -56,6 +58,6 @@ def test_batched_mixed_matches_plain(ens):
     p = ensemble.march_ensemble_native(runs, nsteps=6, form="plain", concurrency=len(runs),
                                        batched=False)
     for x, y, run in zip(m, p, runs):
-        assert x["status"] == "ok" and y["status"] == "ok"
+        assert x["status"] in ("ok", "amplitude") and y["status"] == x["status"]
         for key in ("Nu_top", "urms"):
             assert _rel(x["diag"][key], y["diag"][key]) <= 1e-6, (run["cfg"], key)

@@ -17,10 +17,11 @@
 // Launch policy: the launcher starts a batch as soon as every handle that is
 // stepping has a solve queued, or the oldest queued solve has waited `hold`
 // microseconds, or the queued solves fill the GPU.  Batches do not overlap
-// one another or any other cooperative kernel of the process (the process-
-// wide cooperative lock is held from a launch until its completion): two
-// partially resident grids whose CTAs wait for one another could otherwise
-// never finish.  Solves queued while a batch runs go into the next one.
+// one another or any other cooperative kernel of the process (every
+// cooperative launch is ordered on the GPU after the previous one, see
+// CoopGuard): two partially resident grids whose CTAs wait for one another
+// could otherwise never finish.  The launcher waits for a batch to finish
+// before it starts the next; solves queued meanwhile go into the next one.
 #include <algorithm>
 #include <atomic>
 #include <condition_variable>
@@ -138,7 +139,6 @@ class Batcher {
   }
 
   void launch(std::vector<BatchReq*>& take, size_t smem, int G) {
-    std::lock_guard<std::mutex> coop(coop_mutex());
     RefineBatch B;
     B.njobs = (int)take.size();
     B.err = d_err_;
@@ -151,7 +151,10 @@ class Batcher {
         B.job[j].G = take[j]->G;
         c0 += take[j]->G;
       }
-      refine_batch_launch(s_, B, smem);
+      {
+        CoopGuard guard(s_);           // ordered after every other cooperative grid
+        refine_batch_launch(s_, B, smem);
+      }
       const cudaError_t e = cudaStreamSynchronize(s_);
       if (e != cudaSuccess) throw CudaError(std::string("batched engine: ") + cudaGetErrorString(e));
       int err = 0;

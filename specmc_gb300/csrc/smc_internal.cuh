@@ -102,13 +102,20 @@ struct ProfScope {
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-// Cooperative grids (grid-wide barriers) of different handles never overlap:
-// a cooperative kernel needs all of its CTAs resident at once, and two of
-// them each holding SMs while waiting for the rest of their own CTAs would
-// never finish.  The guard holds a process-wide lock from the launch until
-// the kernel has completed on its stream; ordinary kernels of other streams
-// keep running beside it.
+// Cooperative grids (grid-wide or group barriers) never overlap on a GPU: a
+// cooperative kernel needs all of its CTAs resident at once, and two of them
+// each holding SMs while waiting for the rest of their own CTAs would never
+// finish.  Every cooperative launch of the process is made under one lock and
+// ordered on the GPU after the previous one of the same device (any stream)
+// by an event: the launch's stream waits for the event, the launch records
+// it.  So no host thread waits for a cooperative kernel to finish just to
+// release the lock, and ordinary kernels of other streams keep running beside
+// it.
 std::mutex& coop_mutex();
+// inside the lock: order stream s after the device's last cooperative launch /
+// record the launch just made on s as the device's last one
+void coop_order_before(cudaStream_t s);
+void coop_order_after(cudaStream_t s);
 
 // Let kernel `f` use up to the device's opt-in maximum of dynamic shared
 // memory.  The attribute is global to the process, so every caller sets the
@@ -118,8 +125,8 @@ void allow_max_smem(const void* f);
 struct CoopGuard {
   cudaStream_t s;
   std::unique_lock<std::mutex> lk;
-  explicit CoopGuard(cudaStream_t s_) : s(s_), lk(coop_mutex()) {}
-  ~CoopGuard() { cudaStreamSynchronize(s); }
+  explicit CoopGuard(cudaStream_t s_) : s(s_), lk(coop_mutex()) { coop_order_before(s); }
+  ~CoopGuard() { coop_order_after(s); }
 };
 
 // ------------------------------------------------------- complex helpers

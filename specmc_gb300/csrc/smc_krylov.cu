@@ -233,16 +233,22 @@ void krylov_update(const Ctx& c, double2* x, const double2* Z, const double2* y,
 
 // RBC.diagnostics (rbc_galerkin.py:439-453) from the grids ux, uz, th (Nx, N)
 // and the k = 0 row of that.  out = {Nu_top, Nu_bot, Nu_energy, urms, umax, amp}
-__global__ void smc_diag_kernel(const double* __restrict__ ux, const double* __restrict__ uz,
-                                const double* __restrict__ th, const double2* __restrict__ that0,
-                                const double* __restrict__ D, const double* __restrict__ V,
-                                const double* __restrict__ wq, int Nx, int N,
-                                double* __restrict__ out) {
+// One CTA of DIAG_THREADS threads: column sums with threads over columns
+// (coalesced rows), the boundary fluxes V[end] (D theta_0) and V[0] (D
+// theta_0) with one warp per row of D (lanes over its columns), then warp 0
+// reduces the Clenshaw-Curtis sums and the maxima with lanes over columns.
+constexpr int DIAG_THREADS = 256;
+__global__ void __launch_bounds__(DIAG_THREADS) smc_diag_kernel(
+    const double* __restrict__ ux, const double* __restrict__ uz, const double* __restrict__ th,
+    const double2* __restrict__ that0, const double* __restrict__ D, const double* __restrict__ V,
+    const double* __restrict__ wq, int Nx, int N, double* __restrict__ out) {
   extern __shared__ double sm[];
   double* s1 = sm;            // column means of ux^2 + uz^2
   double* s2 = sm + N;        // column means of uz th
   double* mx = sm + 2 * N;    // column max |ux|,|uz|
   double* ma = sm + 3 * N;    // column max |th|
+  double* dd = sm + 4 * N;    // (D theta_0)[r]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     double a = 0, b = 0, m = 0, t = 0;
     for (int i = 0; i < Nx; ++i) {
@@ -258,35 +264,47 @@ __global__ void smc_diag_kernel(const double* __restrict__ ux, const double* __r
     mx[j] = m;
     ma[j] = t;
   }
+  for (int r = warp; r < N; r += nw) {
+    double d = 0;
+    for (int q = lane; q < N; q += 32) d += D[(long long)r * N + q] * that0[q].x;
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (lane == 0) dd[r] = d;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double v1 = 0, v2 = 0, m = 0, t = 0;
-    for (int j = 0; j < N; ++j) {
+  if (warp == 0) {
+    double v1 = 0, v2 = 0, m = 0, t = 0, ntop = 0, nbot = 0;
+    for (int j = lane; j < N; j += 32) {
       v1 += wq[j] * s1[j];
       v2 += wq[j] * s2[j];
       m = fmax(m, mx[j]);
       t = fmax(t, ma[j]);
+      ntop += V[(long long)(N - 1) * N + j] * dd[j];
+      nbot += V[j] * dd[j];
     }
-    double ntop = 0, nbot = 0;
-    for (int r = 0; r < N; ++r) {
-      double d = 0;
-      for (int q = 0; q < N; ++q) d += D[(long long)r * N + q] * that0[q].x;
-      ntop += V[(long long)(N - 1) * N + r] * d;
-      nbot += V[r] * d;
+    for (int o = 16; o > 0; o >>= 1) {
+      v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+      v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+      ntop += __shfl_xor_sync(0xffffffffu, ntop, o);
+      nbot += __shfl_xor_sync(0xffffffffu, nbot, o);
+      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
     }
-    out[0] = 1.0 - ntop;
-    out[1] = 1.0 - nbot;
-    out[2] = 1.0 + v2;
-    out[3] = sqrt(fmax(v1, 0.0));
-    out[4] = m;
-    out[5] = t;
+    if (lane == 0) {
+      out[0] = 1.0 - ntop;
+      out[1] = 1.0 - nbot;
+      out[2] = 1.0 + v2;
+      out[3] = sqrt(fmax(v1, 0.0));
+      out[4] = m;
+      out[5] = t;
+    }
   }
 }
 
 void diagnostics_reduce(const Ctx& c, const double* ux, const double* uz, const double* th,
                         const double2* that0, const double* D, const double* V, const double* wq,
                         int Nx, int N, double* out) {
-  smc_diag_kernel<<<1, 128, 4 * N * sizeof(double), c.s>>>(ux, uz, th, that0, D, V, wq, Nx, N, out);
+  smc_diag_kernel<<<1, DIAG_THREADS, 5 * N * sizeof(double), c.s>>>(ux, uz, th, that0, D, V, wq,
+                                                                     Nx, N, out);
   SMC_LAUNCH_CHECK(c);
 }
 

@@ -197,6 +197,25 @@ std::mutex& coop_mutex() {
   return mu;
 }
 
+// the last cooperative launch per device (guarded by coop_mutex)
+static cudaEvent_t g_coop_last[64] = {nullptr};
+static bool g_coop_recorded[64] = {false};
+
+void coop_order_before(cudaStream_t s) {
+  int dev = 0;
+  SMC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) throw std::runtime_error("cooperative launch: device ordinal >= 64");
+  if (!g_coop_last[dev])
+    SMC_CUDA(cudaEventCreateWithFlags(&g_coop_last[dev], cudaEventDisableTiming));
+  if (g_coop_recorded[dev]) SMC_CUDA(cudaStreamWaitEvent(s, g_coop_last[dev], 0));
+}
+
+void coop_order_after(cudaStream_t s) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || !g_coop_last[dev]) return;
+  if (cudaEventRecord(g_coop_last[dev], s) == cudaSuccess) g_coop_recorded[dev] = true;
+}
+
 void allow_max_smem(const void* f) {
   static std::mutex mu;
   static std::set<std::pair<const void*, int>> done;

@@ -283,6 +283,47 @@ def run_ours(args, rank, world):
     e2e = {"value": world * args.steps / el, "unit": "steps/s",
            "h2d_bytes_per_step": 2 * n_c * 16, "d2h_bytes_per_step": n_c * 16 + 8}
 
+    # the batched form (the ensemble workload, a bounded sample of it): the
+    # first B runs of the seeded 256-run list (uneven grids, models, Ra and
+    # viscosity contrast), S steps each, in one native call -- mixed form
+    # with the batched engine vs the FP64 plain form, both with the same host
+    # concurrency; states resident in HBM, device synchronised on both sides
+    batched = None
+    if not args.no_batched:
+        import collections
+
+        from specmc_gb300 import ensemble
+        runs = ensemble.ensemble_configs(256, seed=0)[:args.batch_runs]
+        ensemble.march_ensemble_native(runs[:4], nsteps=2, concurrency=4, device=local,
+                                       keep_states=False)                      # warm-up
+        out = {}
+        for form in ("mixed", "plain"):
+            if form == "plain" and args.no_plain:
+                continue
+            torch.cuda.synchronize()
+            res = ensemble.march_ensemble_native(runs, nsteps=args.batch_steps, form=form,
+                                                 concurrency=args.batch_concurrency,
+                                                 batched=(form == "mixed"), device=local,
+                                                 keep_states=False)
+            torch.cuda.synchronize()
+            tm = res[0]["_timing"]
+            nst = sum(r["steps"] for r in res)
+            out[form] = dict(value=world * nst / tm["wall_s"], steps=nst, wall_s=tm["wall_s"],
+                             status=dict(collections.Counter(r["status"] for r in res)),
+                             batch_launches=tm["batch_launches"], batch_solves=tm["batch_solves"],
+                             ctas_per_launch=(tm["batch_ctas"] / tm["batch_launches"]
+                                              if tm["batch_launches"] else None))
+        batched = {
+            "metric": "aggregate steps/s of independent runs (batched ensemble sample)",
+            "unit": "steps/s", "value": out["mixed"]["value"],
+            "sample": "the first %d runs of the seeded 256-run ensemble (grids 32x24..128x96, "
+                      "const/eta_z/eta_T, Ra 1e4..1e6, deta_T 1..1e4), %d steps each"
+                      % (len(runs), args.batch_steps),
+            "mixed_batched": out["mixed"], "plain": out.get("plain"),
+            "batched_vs_plain": (out["mixed"]["value"] / out["plain"]["value"]
+                                 if out.get("plain") else None),
+            "concurrency": args.batch_concurrency}
+
     # roofline of the dominant kernel of the headline (mixed) form: the leaf
     # profile region with the largest share of the timed steps (aggregates
     # "step.*" / the memoised Stokes bracket and the engine's per-phase
@@ -343,6 +384,7 @@ def run_ours(args, rank, world):
         "diag_after": {k: M["diag"][k] for k in ("Nu_top", "urms")},
         "kernel_regions": [dict(p, ms_per_step=p["ms"] / args.steps) for p in R["prof"]],
         "kernel_regions_ms_per_step": R["ms"] / args.steps,
+        "batched": batched,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -362,6 +404,10 @@ def main():
                     help="reference arm: warm-up steps (default: --warmup)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble leg")
+    ap.add_argument("--batch-runs", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--batch-concurrency", type=int, default=16)
     ap.add_argument("--phases", action="store_true",
                     help="add the Krylov engine's per-phase times to kernel_regions")
     args = ap.parse_args()

@@ -61,13 +61,17 @@ struct Profiler {
   ~Profiler();
 };
 
+struct TcCache;
+
 // Launch context: the stream every kernel of a handle goes to, the launch
-// counter the handle reports, and the optional profiler.
+// counter the handle reports, the optional profiler, and the tensor-core
+// operators of the z-contractions (null: FP64 SIMT contractions only).
 struct Ctx {
   cudaStream_t s = nullptr;
   long long* nlaunch = nullptr;
   int num_sms = 152;
   Profiler* prof = nullptr;
+  TcCache* tc = nullptr;
   void count(int n = 1) const { if (nlaunch) *nlaunch += n; }
 };
 

@@ -32,6 +32,7 @@
 #include "smc_fastops.cuh"
 #include "smc_engine.cuh"
 #include "smc_batch.cuh"
+#include "smc_tc.cuh"
 #include "smc_tala.cuh"
 
 namespace smc {
@@ -441,6 +442,32 @@ struct Model {
   cudaEvent_t batch_ready = nullptr;
   int batch_seq = 0;
   long long n_batched = 0;           // solves this handle ran through the batcher
+  // tensor-core z-contractions (smc_tc.cu) of the basis operators
+  std::unique_ptr<TcCache> tc_cache;
+
+  void enable_tc(bool on) {
+    if (on && N > TC_KMAX)
+      throw std::runtime_error("tc_transforms needs Nz <= " + std::to_string(TC_KMAX));
+    if (on && !tc_cache) {
+      tc_cache.reset(new TcCache);
+      tc_cache->K = N;
+      tc_cache->err = mem.alloc<int>(1);
+      for (const double* Z : {dV, dVi, dD, dD2, dVD, dVD2}) tc_cache->add(Z, N);
+    }
+    ctx.tc = on ? tc_cache.get() : nullptr;
+  }
+  // a tensor-core CTA that gave up waiting wrote NaN and raised the flag
+  void check_tc() {
+    if (!tc_cache || !tc_cache->err) return;
+    int e = 0;
+    SMC_CUDA(cudaMemcpyAsync(hbuf, tc_cache->err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    SMC_CUDA(cudaStreamSynchronize(stream));
+    std::memcpy(&e, hbuf, sizeof(int));
+    if (e) {
+      SMC_CUDA(cudaMemsetAsync(tc_cache->err, 0, sizeof(int), stream));
+      throw std::runtime_error("tensor-core contraction: an mbarrier wait timed out");
+    }
+  }
 
   void enable_batch(bool on) {
     if (on && !fast) throw std::runtime_error("engine_batch needs a SMC_MIXED handle");
@@ -2175,6 +2202,7 @@ int smc_step(smc_handle* h, const double* in, double* out, int mem, double dt) {
     copy_in(m, m.dIn, in, mem, m.n);
     m.step(m.dIn, m.dOut, dt);
     copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
+    m.check_tc();
   })
 }
 
@@ -2216,6 +2244,7 @@ int smc_march_adaptive(smc_handle* h, const double* in, double* out, int mem, do
       ++steps;
     }
     copy_out(m, out, cur, mem, m.n * sizeof(double2));
+    m.check_tc();
     if (info) { info->steps = steps; info->t = t; info->dt = dt; }
   })
 }
@@ -2270,6 +2299,7 @@ int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety,
     Model& m = h->m;
     smc::BatchScope bs(m.device, m.batch_mode);
     smc::advance_resident(m, tstop, max_steps, safety, dtmax, info);
+    m.check_tc();
   })
 }
 
@@ -2311,6 +2341,7 @@ int smc_march(smc_handle* h, const double* in, double* out, int mem, double dt, 
       std::swap(cur, nxt);
     }
     copy_out(m, out, cur, mem, m.n * sizeof(double2));
+    m.check_tc();
   })
 }
 
@@ -2379,6 +2410,7 @@ int smc_transform(smc_handle* h, int kind, const double* in, double* out, int me
     } else {
       throw std::runtime_error("unknown transform kind");
     }
+    m.check_tc();
   })
 }
 
@@ -2448,6 +2480,8 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
       h->m.eng_ctas = (int)value;
     } else if (k == "engine_phase_profile") {
       h->m.eng_phase = value != 0.0;
+    } else if (k == "tc_transforms") {
+      h->m.enable_tc(value != 0.0);
     } else if (k == "engine_batch") {
       h->m.enable_batch(value != 0.0);
     } else if (k == "engine_batch_ctas") {
@@ -2613,6 +2647,7 @@ int smc_march_many(smc_handle* const* hs, int nruns, long long nsteps, double sa
           while (r.status != SMC_RUN_NONFINITE && r.steps < nsteps) {
             const long long k = std::min<long long>(check_every, nsteps - r.steps);
             advance_resident(m, INFINITY, k, safety, dtmax, &info);
+            m.check_tc();
             r.steps += info.steps;
             r.t = info.t;
             r.dt = info.dt;

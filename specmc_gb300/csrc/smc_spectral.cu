@@ -8,6 +8,7 @@
 // direct sums with precomputed twiddles instead of FFTs; the results agree
 // with numpy's pocketfft to roundoff.
 #include "smc_internal.cuh"
+#include "smc_tc.cuh"
 
 namespace smc {
 
@@ -63,6 +64,9 @@ __global__ void __launch_bounds__(CSPLIT * ZOUT) smc_zmat_kernel(ZJobs4 jobs, in
 
 void zmat_apply(const Ctx& c, const ZJob* jobs, int njobs, int Nk, int N, const double* kx) {
   if (njobs < 1 || njobs > 4) throw std::runtime_error("zmat_apply: 1..4 jobs");
+  // shared operators of up to 128 columns go to the tensor cores when the
+  // handle has them enabled (same result to FP64 roundoff, smc_tc.cu)
+  if (c.tc && tc_zmat_apply(c, *c.tc, jobs, njobs, Nk, N, kx)) return;
   ZJobs4 js;
   for (int i = 0; i < njobs; ++i) js.j[i] = jobs[i];
   dim3 blk(CSPLIT * ZOUT), grd(ceil_div(N, ZOUT), Nk, njobs);

@@ -134,6 +134,8 @@ def march_ensemble_native(runs, nsteps=100, form="mixed", concurrency=16, safety
     safety = NUM.CFL_SAFETY if safety is None else float(safety)
     dtmax = NUM.DTMAX if dtmax is None else float(dtmax)
     lib = _lib.load()
+    from . import tune
+    table = tune.load() if batch_ctas is None else {}
     models, t_build = [], []
     try:
         for run in runs:
@@ -144,6 +146,10 @@ def march_ensemble_native(runs, nsteps=100, form="mixed", concurrency=16, safety
                 # CTAs per solve, batched or not
                 _lib.check(lib.smc_set_option(model._h, b"engine_batch_ctas", float(batch_ctas)))
                 _lib.check(lib.smc_set_option(model._h, b"engine_ctas", float(batch_ctas)))
+            elif model.form == "mixed":
+                c = tune.batch_ctas_for(run["cfg"].Nx, run["cfg"].Nz, table)
+                if c:        # the autotuned count of this grid (specmc_gb300/tuned.json)
+                    _lib.check(lib.smc_set_option(model._h, b"engine_batch_ctas", float(c)))
             th = np.ascontiguousarray(model.seed(amp=run["amp"], m=run["m"], n=run["n"]))
             _lib.check(lib.smc_set_state(model._h, th.ctypes.data_as(ctypes.c_void_p),
                                          _lib.SMC_HOST))

@@ -20,16 +20,21 @@
 //     accumulator holds exactly, so the tensor cores return each level
 //     exactly;
 //   * the levels L = 2 .. TC_SLICES + 1 (the products whose weight reaches
-//     2^-63 relative to the row scales) are combined in FP64 by Horner's rule
-//     and scaled back: C = 2^(e_r + f_n) 2^-14 sum_L D_L 2^(-7 (L - 2)).
+//     2^-63 relative to the row scales) are combined in 64-bit integers,
+//     sum_L D_L 2^(52 - 7 L) (the two lowest levels shifted right; |D_L| <
+//     2^24, so the sum stays below 2^62.01), converted to FP64 once and
+//     scaled back with one FP64 product: C = 2^(e_r + f_n - 52) x that sum.
 //
-// The dropped terms and the operands' own 56-bit truncation leave a relative
-// error of about 2^-56 per product -- below FP64 roundoff, so the result is
-// as accurate as the FP64 SIMT contraction it replaces (both are compared
-// with the oracle in the tests).
+// The dropped terms, the operands' own 56-bit truncation and the bits
+// dropped in the combination leave an error of about 2^-52 of the row and
+// column scales -- the size of the FP64 SIMT contraction's own rounding, so
+// the result is as accurate as the contraction it replaces (both are
+// compared with the oracle in the tests).  The slices are cut with integer
+// arithmetic on the FP64 bit patterns (GB300's FP64 pipe is its narrowest
+// unit), so the only FP64 work is one conversion and one product per output.
 //
-// One CTA forms a 128 x 64 tile of C for every level in tensor memory (8
-// accumulators of 64 FP32 columns: all 512 TMEM columns of the SM).  The
+// One CTA forms a 128 x 32 tile of C for every level in tensor memory (8
+// accumulators of 32 FP32 columns: 256 TMEM columns, two CTAs per SM).  The
 // operator's slices (B) are split once and stored in the exact shared-memory
 // image of the MMA operand, so each 32-wide K chunk of a tile arrives in one
 // bulk copy (cp.async.bulk, the TMA's non-tensor form, completing on an
@@ -47,8 +52,8 @@ namespace smc {
 namespace {
 
 constexpr int TC_THREADS = 128;
-constexpr int TC_SMEM = 128 * 1024;          // > half the SM: one CTA per SM (512 TMEM columns)
-constexpr int TC_TMEM_COLS = 512;
+constexpr int TC_SMEM = TC_SLICES * (TC_A_SLICE_BYTES + TC_B_SLICE_BYTES);   // 80 KB: 2 CTAs per SM
+constexpr int TC_TMEM_COLS = 256;                                         // 2 x 256 = the SM's 512
 constexpr long long TC_WAIT_NS = 200000000LL; // 0.2 s: the MMAs of a tile take microseconds
 
 struct TcJob {
@@ -110,7 +115,29 @@ __device__ __forceinline__ unsigned short bf16_bits(double v) {
   return *reinterpret_cast<const unsigned short*>(&h);
 }
 
-// B operator split: one warp per row q (rows padded to ntiles * 64 stay zero)
+// trunc(|x| 2^(56 - e)) for |x| < 2^e, from the bit pattern (integer ops);
+// *neg = sign of x
+__device__ __forceinline__ unsigned long long fixed56(double x, int e, bool* neg) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  *neg = (b >> 63) != 0;
+  const int ex = (int)((b >> 52) & 0x7ff);
+  unsigned long long m = b & ((1ull << 52) - 1);
+  int sh;
+  if (ex == 0) sh = -1074 + 56 - e;                 // subnormal: m 2^-1074
+  else { m |= 1ull << 52; sh = ex - 1075 + 56 - e; }
+  if (sh >= 0) return m << sh;                       // sh <= 3 since |x| < 2^e
+  return sh > -64 ? (m >> (-sh)) : 0ull;
+}
+
+// bf16 bit pattern of the integer +-s, 0 <= s <= 127 (exact)
+__device__ __forceinline__ unsigned short bf16_int(unsigned s, bool neg) {
+  if (s == 0) return 0;
+  const int msb = 31 - __clz(s);
+  return (unsigned short)(((unsigned)neg << 15) | ((unsigned)(127 + msb) << 7) |
+                          ((s << (7 - msb)) & 0x7fu));
+}
+
+// B operator split: one warp per row q (rows padded to ntiles * TC_N stay zero)
 __global__ void smc_tc_pack_kernel(const double* __restrict__ Z, int rows, int K, int nchunks,
                                    unsigned char* __restrict__ out, double* __restrict__ scale) {
   const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -137,7 +164,7 @@ __global__ void smc_tc_pack_kernel(const double* __restrict__ Z, int rows, int K
   }
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1) smc_tc_zmat_kernel(
+__global__ void __launch_bounds__(TC_THREADS, 2) smc_tc_zmat_kernel(
     const __grid_constant__ TcJobs4 jobs, int Nk, int N, int nchunks,
     const double* __restrict__ kx, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -200,19 +227,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) smc_tc_zmat_kernel(
           "l"(src), "r"(TC_B_CHUNK_BYTES), "r"(btma)
           : "memory");
     }
-    // the 32 values of this chunk, cut into slices, 8 per 16-byte core row
+    // the 32 values of this chunk, cut into slices (integer arithmetic on
+    // the FP64 bits: the 56 bits below 2^e, 7 per slice), 8 per 16-byte row
     for (int kb = 0; kb < 4; ++kb) {
       unsigned short sl[TC_SLICES][8];
       for (int i = 0; i < 8; ++i) {
         const int m = ch * TC_KC + kb * 8 + i;
-        double a = 0.0;
-        if (rowok && m < N) a = ldexp(c ? xr[m].y : xr[m].x, -e);
-        for (int p = 0; p < TC_SLICES; ++p) {
-          const double tt = a * 128.0;
-          const double s = trunc(tt);
-          a = tt - s;
-          sl[p][i] = bf16_bits(s);
-        }
+        unsigned long long u = 0;
+        bool neg = false;
+        if (rowok && m < N) u = fixed56(c ? xr[m].y : xr[m].x, e, &neg);
+        for (int p = 0; p < TC_SLICES; ++p)
+          sl[p][i] = bf16_int((unsigned)((u >> (49 - 7 * p)) & 127u), neg);
       }
       const int off = tc_off(t, kb * 8);
       for (int p = 0; p < TC_SLICES; ++p) {
@@ -266,11 +291,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) smc_tc_zmat_kernel(
     if (t == 0) atomicExch(err, 1);
   }
 
-  // epilogue: warp w holds TMEM lanes 32w .. 32w + 31 = rows m0 + 32 w + lane
-  const double rs = ldexp(1.0, e - 14);
+  // epilogue: warp w holds TMEM lanes 32w .. 32w + 31 = rows m0 + 32 w + lane;
+  // level lv (weight 2^(-7 (lv + 2)) of the scales) enters the integer sum
+  // with weight 2^(38 - 7 lv), i.e. in units of 2^-52 of the scales (lv > 5:
+  // shifted right, dropping less than a unit each)
+  const double rs = ldexp(1.0, e - 52);
   for (int cg = 0; cg < TC_N / 16; ++cg) {
-    double acc[16];
-    for (int j = 0; j < 16; ++j) acc[j] = 0.0;
+    long long acc[16];
+    for (int j = 0; j < 16; ++j) acc[j] = 0;
     for (int lv = TC_SLICES - 1; lv >= 0; --lv) {
       uint32_t v[16];
       const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(lv * TC_N + cg * 16);
@@ -283,11 +311,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) smc_tc_zmat_kernel(
           : "r"(ta)
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      for (int j = 0; j < 16; ++j) acc[j] = acc[j] * 0.0078125 + (double)__uint_as_float(v[j]);
+      for (int j = 0; j < 16; ++j) {
+        const long long d = (long long)__float2int_rz(__uint_as_float(v[j]));   // exact: < 2^24
+        acc[j] += lv <= 5 ? (d << (38 - 7 * lv)) : (d >> (7 * lv - 38));
+      }
     }
     for (int j = 0; j < 16; ++j) {
       const int n = n0 + cg * 16 + j;
-      double val = failed ? NAN : acc[j] * rs * (n < N ? jb.bscale[n] : 0.0);
+      double val = failed ? NAN : __ll2double_rn(acc[j]) * rs * (n < N ? jb.bscale[n] : 0.0);
       const double im = __shfl_down_sync(0xffffffffu, val, 1);
       if (c == 0 && k < Nk && n < N) {
         double2* yp = jb.Y + (long long)k * N + n;

@@ -10,7 +10,7 @@ namespace smc {
 
 constexpr int TC_SLICES = 8;            // 7-bit slices: 56 bits of each operand
 constexpr int TC_M = 128;               // A rows per CTA (= TMEM lanes)
-constexpr int TC_N = 64;                // B rows (outputs) per CTA
+constexpr int TC_N = 32;                // B rows (outputs) per CTA
 constexpr int TC_KC = 32;               // K per chunk (two MMA k-steps of 16)
 constexpr int TC_A_SLICE_BYTES = TC_M * TC_KC * 2;
 constexpr int TC_B_SLICE_BYTES = TC_N * TC_KC * 2;
@@ -20,12 +20,12 @@ constexpr int TC_KMAX = 128;            // exactness bound of the FP32 accumulat
 // An operator Z (rows x K, FP64, row-major) split for the tensor cores:
 // per row q an exponent f_q with max_m |Z[q][m]| < 2^f_q, and TC_SLICES
 // bf16 slices of 7 bits each of Z[q][m] 2^-f_q, stored tile by tile in the
-// exact shared-memory image the MMA reads (64-row tiles, 32-column K chunks,
+// exact shared-memory image the MMA reads (32-row tiles, 32-column K chunks,
 // 8 x 16-byte core matrices), so a K chunk of a tile is one bulk copy.
 struct TcOperator {
   int rows = 0, K = 0, ntiles = 0, nchunks = 0;
   void* slices = nullptr;      // bf16, ntiles * nchunks * TC_B_CHUNK_BYTES
-  double* scale = nullptr;     // 2^f_q, rows (padded to ntiles * 64)
+  double* scale = nullptr;     // 2^f_q, rows (padded to ntiles * TC_N)
 };
 
 // The tensor-core operators of a model: registered once per immutable

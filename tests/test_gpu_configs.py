@@ -87,8 +87,12 @@ def _heated_ic(model, H=1.5, seed=7, amp=1e-2, modes=8):
 
 def test_heated_2to1_64x96_mixed_matches_plain():
     """Internally heated 2:1 box (Ra 1.25e4, H 1.5, eta_T deta 1e3, 64x96,
-    Lx = 4 for the physical 2:1 box on the mirror-doubled carrier): 15 CFL
-    steps, mixed vs plain, Nu_top / Nu_energy / Vrms within 1e-6."""
+    Lx = 4 for the physical 2:1 box on the mirror-doubled carrier): 300 CFL
+    steps (t ~ 1.5e-3, through the first overturn, where the Stokes solves
+    climb from ~25 to ~300 BFBT iterations and the mixed form takes a dense
+    rescue), mixed vs plain, Nu_top / Nu_energy / Vrms within 1e-6 every 50
+    steps.  The configuration's own end, t = 0.03, lies some 4000 steps of
+    growing cost further on (dt ~ 2e-6 .. 1e-5): beyond a test's time."""
     import specmc_gb300.api as api
     from specmc_gb300.config import ConvectionConfig
     cfg = ConvectionConfig(viscosity_model="eta_T", deta_T=1000.0, Ra=1.25e4, internal_heating=1.5,
@@ -97,12 +101,15 @@ def test_heated_2to1_64x96_mixed_matches_plain():
     for form in ("mixed", "plain"):
         m = api.build_model(cfg, form=form)
         s = _heated_ic(m)
-        for _ in range(15):
+        out[form] = []
+        for i in range(300):
             s = m.step(s, api.production_dt(m, s))
-        out[form] = m.diagnostics(s)
+            if (i + 1) % 50 == 0:
+                out[form].append(m.diagnostics(s))
         m.close()
-    for key in ("Nu_top", "Nu_energy", "urms"):
-        assert _rel(out["mixed"][key], out["plain"][key]) <= 1e-6, key
+    for dm, dp in zip(out["mixed"], out["plain"]):
+        for key in ("Nu_top", "Nu_energy", "urms"):
+            assert _rel(dm[key], dp[key]) <= 1e-6, (key, dm[key], dp[key])
 
 
 def test_large_nz_lu_matches_oracle():

@@ -233,31 +233,51 @@ void krylov_update(const Ctx& c, double2* x, const double2* Z, const double2* y,
 
 // RBC.diagnostics (rbc_galerkin.py:439-453) from the grids ux, uz, th (Nx, N)
 // and the k = 0 row of that.  out = {Nu_top, Nu_bot, Nu_energy, urms, umax, amp}
-// One CTA of DIAG_THREADS threads: column sums with threads over columns
-// (coalesced rows), the boundary fluxes V[end] (D theta_0) and V[0] (D
-// theta_0) with one warp per row of D (lanes over its columns), then warp 0
-// reduces the Clenshaw-Curtis sums and the maxima with lanes over columns.
-constexpr int DIAG_THREADS = 256;
+// One CTA of DIAG_THREADS threads: column sums with threads over (column,
+// row slice) pairs -- S = DIAG_THREADS / N slices of rows per column, each
+// thread's rows i = slice, slice + S, ... (coalesced across the columns of a
+// row), the slices then added in order -- the boundary fluxes V[end] (D
+// theta_0) and V[0] (D theta_0) with one warp per row of D (lanes over its
+// columns), then warp 0 reduces the Clenshaw-Curtis sums and the maxima with
+// lanes over columns.
+constexpr int DIAG_THREADS = 1024;
 __global__ void __launch_bounds__(DIAG_THREADS) smc_diag_kernel(
     const double* __restrict__ ux, const double* __restrict__ uz, const double* __restrict__ th,
     const double2* __restrict__ that0, const double* __restrict__ D, const double* __restrict__ V,
     const double* __restrict__ wq, int Nx, int N, double* __restrict__ out) {
   extern __shared__ double sm[];
+  const int S = max(1, (int)blockDim.x / N);     // row slices per column
   double* s1 = sm;            // column means of ux^2 + uz^2
   double* s2 = sm + N;        // column means of uz th
   double* mx = sm + 2 * N;    // column max |ux|,|uz|
   double* ma = sm + 3 * N;    // column max |th|
   double* dd = sm + 4 * N;    // (D theta_0)[r]
+  double* pt = sm + 5 * N;    // per-slice partials: 4 x S x N
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+  for (int u = threadIdx.x; u < S * N; u += blockDim.x) {
+    const int j = u % N, sl = u / N;
     double a = 0, b = 0, m = 0, t = 0;
-    for (int i = 0; i < Nx; ++i) {
+    for (int i = sl; i < Nx; i += S) {
       long long e = (long long)i * N + j;
       double x = ux[e], z = uz[e], h = th[e];
       a += x * x + z * z;
       b += z * h;
       m = fmax(m, fmax(fabs(x), fabs(z)));
       t = fmax(t, fabs(h));
+    }
+    pt[(0 * S + sl) * N + j] = a;
+    pt[(1 * S + sl) * N + j] = b;
+    pt[(2 * S + sl) * N + j] = m;
+    pt[(3 * S + sl) * N + j] = t;
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    double a = 0, b = 0, m = 0, t = 0;
+    for (int sl = 0; sl < S; ++sl) {
+      a += pt[(0 * S + sl) * N + j];
+      b += pt[(1 * S + sl) * N + j];
+      m = fmax(m, pt[(2 * S + sl) * N + j]);
+      t = fmax(t, pt[(3 * S + sl) * N + j]);
     }
     s1[j] = a / Nx;
     s2[j] = b / Nx;
@@ -303,8 +323,10 @@ __global__ void __launch_bounds__(DIAG_THREADS) smc_diag_kernel(
 void diagnostics_reduce(const Ctx& c, const double* ux, const double* uz, const double* th,
                         const double2* that0, const double* D, const double* V, const double* wq,
                         int Nx, int N, double* out) {
-  smc_diag_kernel<<<1, DIAG_THREADS, 5 * N * sizeof(double), c.s>>>(ux, uz, th, that0, D, V, wq,
-                                                                     Nx, N, out);
+  const int S = std::max(1, DIAG_THREADS / N);
+  const size_t sm = (size_t)(5 * N + 4 * S * N) * sizeof(double);
+  if (sm > 48 * 1024) allow_max_smem((const void*)smc_diag_kernel);
+  smc_diag_kernel<<<1, DIAG_THREADS, sm, c.s>>>(ux, uz, th, that0, D, V, wq, Nx, N, out);
   SMC_LAUNCH_CHECK(c);
 }
 

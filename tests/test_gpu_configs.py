@@ -87,12 +87,19 @@ def _heated_ic(model, H=1.5, seed=7, amp=1e-2, modes=8):
 
 def test_heated_2to1_64x96_mixed_matches_plain():
     """Internally heated 2:1 box (Ra 1.25e4, H 1.5, eta_T deta 1e3, 64x96,
-    Lx = 4 for the physical 2:1 box on the mirror-doubled carrier): 300 CFL
-    steps (t ~ 1.5e-3, through the first overturn, where the Stokes solves
-    climb from ~25 to ~300 BFBT iterations and the mixed form takes a dense
-    rescue), mixed vs plain, Nu_top / Nu_energy / Vrms within 1e-6 every 50
-    steps.  The configuration's own end, t = 0.03, lies some 4000 steps of
-    growing cost further on (dt ~ 2e-6 .. 1e-5): beyond a test's time."""
+    Lx = 4 for the physical 2:1 box on the mirror-doubled carrier): the first
+    200 CFL steps (t ~ 8.7e-4, into the first overturn, where the Stokes
+    solves climb from ~25 to ~300 BFBT iterations), mixed vs plain, Nu_top /
+    Nu_energy / Vrms within 1e-6 every 50 steps (measured ~1e-10).
+
+    Past step ~210 the overturn is unstable: it amplifies differences at the
+    solver tolerance ~1e7-fold in 40 steps.  Measured against the plain form
+    with 100x tighter tolerances, the plain form at its default tolerances is
+    7e-10 off in Nu_top at step 200, 1.4e-3 at step 240 and 52% at step 300 --
+    and the mixed form follows the same curve (2e-11, 3.3e-3, 50%).  So no
+    pointwise comparison of two solvers is meaningful beyond that point, and
+    the configuration's own end, t = 0.03, thousands of steps further on,
+    can only be compared statistically."""
     import specmc_gb300.api as api
     from specmc_gb300.config import ConvectionConfig
     cfg = ConvectionConfig(viscosity_model="eta_T", deta_T=1000.0, Ra=1.25e4, internal_heating=1.5,
@@ -102,7 +109,7 @@ def test_heated_2to1_64x96_mixed_matches_plain():
         m = api.build_model(cfg, form=form)
         s = _heated_ic(m)
         out[form] = []
-        for i in range(300):
+        for i in range(200):
             s = m.step(s, api.production_dt(m, s))
             if (i + 1) % 50 == 0:
                 out[form].append(m.diagnostics(s))

@@ -14,9 +14,18 @@
 // CTAs publish its results to host-mapped memory as soon as it ends, so its
 // thread goes on with the rest of its step while the batch runs on.
 //
+// Refill: while a launch runs, the launcher publishes the solves queued since
+// (once their inputs are complete) through a host-mapped feed; a slot whose
+// solve has ended claims the next one and runs it on its own CTAs, so a
+// launch does not idle down to its slowest solve.  A slot leaves when no
+// solve arrives for `idle` microseconds, and none is claimed after `life`
+// microseconds, so other cooperative kernels (ordered after the launch) are
+// not held off for long; solves published but never claimed go back to the
+// queue.
+//
 // Launch policy: the launcher starts a batch as soon as every handle that is
 // stepping has a solve queued, or the oldest queued solve has waited `hold`
-// microseconds, or the queued solves fill the GPU.  Batches do not overlap
+// microseconds, or the queued solves fill the GPU (or the cap set for it).  Batches do not overlap
 // one another or any other cooperative kernel of the process (every
 // cooperative launch is ordered on the GPU after the previous one, see
 // CoopGuard): two partially resident grids whose CTAs wait for one another
@@ -25,6 +34,7 @@
 #include <algorithm>
 #include <atomic>
 #include <condition_variable>
+#include <cstring>
 #include <deque>
 #include <mutex>
 #include <thread>
@@ -44,6 +54,13 @@ class Batcher {
     SMC_CUDA(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
     SMC_CUDA(cudaMalloc(&d_err_, sizeof(int)));
     SMC_CUDA(cudaMemsetAsync(d_err_, 0, sizeof(int), s_));
+    SMC_CUDA(cudaMalloc(&d_slot_bar_, 4 * ENGINE_BATCH_MAX * sizeof(unsigned int)));
+    SMC_CUDA(cudaMemsetAsync(d_slot_bar_, 0, 4 * ENGINE_BATCH_MAX * sizeof(unsigned int), s_));
+    SMC_CUDA(cudaMalloc(&d_claimed_, sizeof(int)));
+    SMC_CUDA(cudaMalloc(&d_slot_ticket_, ENGINE_BATCH_MAX * sizeof(int)));
+    SMC_CUDA(cudaHostAlloc((void**)&h_feed_, sizeof(BatchFeed), cudaHostAllocMapped));
+    std::memset((void*)h_feed_, 0, sizeof(BatchFeed));
+    SMC_CUDA(cudaHostGetDevicePointer((void**)&d_feed_, (void*)h_feed_, 0));
     SMC_CUDA(cudaStreamSynchronize(s_));
     th_ = std::thread([this] { loop(); });
   }
@@ -67,20 +84,39 @@ class Batcher {
     std::lock_guard<std::mutex> lk(mu_);
     hold_us_ = std::max(0.0, us);
   }
+  void set_refill(bool on, double idle_us, double life_us) {
+    std::lock_guard<std::mutex> lk(mu_);
+    refill_ = on;
+    if (idle_us >= 0.0) idle_us_ = idle_us;
+    if (life_us >= 0.0) life_us_ = life_us;
+  }
+  void set_cap(int ctas) {
+    std::lock_guard<std::mutex> lk(mu_);
+    cap_ctas_ = std::max(0, ctas);
+  }
   void stats(long long* l, long long* s, long long* c) {
     std::lock_guard<std::mutex> lk(mu_);
     if (l) *l = launches_;
     if (s) *s = solves_;
     if (c) *c = ctas_;
   }
+  long long refilled() {
+    std::lock_guard<std::mutex> lk(mu_);
+    return refilled_;
+  }
 
  private:
   int capacity(size_t smem) {
+    int c = -1;
     for (auto& p : caps_)
-      if (p.first == smem) return p.second;
-    const int c = refine_batch_capacity(smem, sms_);
-    caps_.push_back({smem, c});
-    return c;
+      if (p.first == smem) c = p.second;
+    if (c < 0) {
+      c = refine_batch_capacity(smem, sms_);
+      caps_.push_back({smem, c});
+    }
+    // a cap leaves SM room for the ordinary kernels of the runs while a
+    // refilling launch lives on
+    return cap_ctas_ > 0 ? std::min(c, cap_ctas_) : c;
   }
 
   void fail_all(std::vector<BatchReq*>& take, int code) {
@@ -142,6 +178,16 @@ class Batcher {
     RefineBatch B;
     B.njobs = (int)take.size();
     B.err = d_err_;
+    B.slot_bar = d_slot_bar_;
+    const bool refill = refill_;
+    if (refill) {
+      B.feed = d_feed_;
+      B.claimed = d_claimed_;
+      B.slot_ticket = d_slot_ticket_;
+      B.idle_ns = (long long)(idle_us_ * 1e3);
+      B.life_ns = (long long)(life_us_ * 1e3);
+    }
+    std::vector<BatchReq*> fed;          // fed[t]: the solve published as ticket t
     int c0 = 0;
     try {
       for (int j = 0; j < B.njobs; ++j) {
@@ -151,30 +197,67 @@ class Batcher {
         B.job[j].G = take[j]->G;
         c0 += take[j]->G;
       }
+      int gmin = c0;
+      for (int j = 0; j < B.njobs; ++j) gmin = std::min(gmin, B.job[j].G);
+      if (refill) {
+        h_feed_->published = 0;
+        SMC_CUDA(cudaMemsetAsync(d_claimed_, 0, sizeof(int), s_));
+      }
       {
         CoopGuard guard(s_);           // ordered after every other cooperative grid
         refine_batch_launch(s_, B, smem);
       }
+      // while the launch runs: publish the solves queued since, once their
+      // inputs are complete, for the slots that free up
+      while (refill) {
+        const cudaError_t q = cudaStreamQuery(s_);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady)
+          throw CudaError(std::string("batched engine: ") + cudaGetErrorString(q));
+        std::unique_lock<std::mutex> lk(mu_);
+        int pub = (int)fed.size();
+        for (auto it = q_.begin(); it != q_.end() && pub < BATCH_FEED_CAP;) {
+          BatchReq* r = *it;
+          if (r->smem <= smem && cudaEventQuery(r->ready) == cudaSuccess) {
+            h_feed_->ring[pub] = r->job;
+            fed.push_back(r);
+            ++pub;
+            it = q_.erase(it);
+          } else {
+            ++it;
+          }
+        }
+        if (pub != h_feed_->published) {
+          std::atomic_thread_fence(std::memory_order_seq_cst);
+          h_feed_->published = pub;
+        }
+        cv_.wait_for(lk, std::chrono::microseconds(20));
+      }
       const cudaError_t e = cudaStreamSynchronize(s_);
       if (e != cudaSuccess) throw CudaError(std::string("batched engine: ") + cudaGetErrorString(e));
-      int err = 0;
+      int err = 0, claimed = 0;
       SMC_CUDA(cudaMemcpy(&err, d_err_, sizeof(int), cudaMemcpyDeviceToHost));
+      if (refill) SMC_CUDA(cudaMemcpy(&claimed, d_claimed_, sizeof(int), cudaMemcpyDeviceToHost));
       if (err) {
-        // a group barrier timed out: reset every barrier word of the batch
-        // and the flag; the groups that timed out reported failed results
-        for (int j = 0; j < B.njobs; ++j)
-          SMC_CUDA(cudaMemsetAsync(B.job[j].bar, 0, 3 * sizeof(unsigned int), s_));
+        // a group barrier timed out: reset the slot words and the flag; the
+        // groups that timed out reported failed results
+        SMC_CUDA(cudaMemsetAsync(d_slot_bar_, 0, 4 * ENGINE_BATCH_MAX * sizeof(unsigned int), s_));
         SMC_CUDA(cudaMemsetAsync(d_err_, 0, sizeof(int), s_));
         SMC_CUDA(cudaStreamSynchronize(s_));
       }
       std::lock_guard<std::mutex> lk(mu_);
+      // published solves no group claimed go back to the front of the queue
+      for (int t = (int)fed.size() - 1; t >= claimed; --t) q_.push_front(fed[t]);
       ++launches_;
-      solves_ += B.njobs;
+      solves_ += B.njobs + std::min(claimed, (int)fed.size());
       ctas_ += G;
+      refilled_ += std::min(claimed, (int)fed.size());
     } catch (const std::exception&) {
       // nothing may be left waiting for a result that never comes
       std::vector<BatchReq*> pending;
       for (BatchReq* r : take)
+        if (r->host->done != r->job.seq) pending.push_back(r);
+      for (BatchReq* r : fed)
         if (r->host->done != r->job.seq) pending.push_back(r);
       fail_all(pending, 2);
     }
@@ -184,11 +267,20 @@ class Batcher {
   int sms_ = 0;
   cudaStream_t s_ = nullptr;
   int* d_err_ = nullptr;
+  unsigned int* d_slot_bar_ = nullptr;   // 4 words per slot (zero between launches)
+  int* d_claimed_ = nullptr;
+  int* d_slot_ticket_ = nullptr;
+  BatchFeed* h_feed_ = nullptr;          // host-mapped
+  BatchFeed* d_feed_ = nullptr;
+  bool refill_ = true;
+  double idle_us_ = 200.0, life_us_ = 20000.0;
+  long long refilled_ = 0;
   std::mutex mu_;
   std::condition_variable cv_;
   std::deque<BatchReq*> q_;
   int participants_ = 0;
   double hold_us_ = 50.0;
+  int cap_ctas_ = 0;
   long long launches_ = 0, solves_ = 0, ctas_ = 0;
   std::vector<std::pair<size_t, int>> caps_;
   std::thread th_;
@@ -212,6 +304,10 @@ void batch_enter(int device) { batcher(device).enter(); }
 void batch_leave(int device) { batcher(device).leave(); }
 void batch_submit(int device, BatchReq* r) { batcher(device).submit(r); }
 void batch_set_hold_us(int device, double us) { batcher(device).set_hold(us); }
+void batch_set_refill(int device, int on, double idle_us, double life_us) {
+  batcher(device).set_refill(on != 0, idle_us, life_us);
+}
+void batch_set_cap(int device, int ctas) { batcher(device).set_cap(ctas); }
 void batch_stats(int device, long long* l, long long* s, long long* c) {
   batcher(device).stats(l, s, c);
 }

@@ -31,8 +31,12 @@ void batch_submit(int device, BatchReq* r);
 // after `timeout_s` seconds.
 void batch_wait(const BatchReq* r, double timeout_s);
 // Batcher settings: how long the oldest queued solve may wait for others
-// (microseconds) before a launch.
+// (microseconds) before a launch; refill on/off with the idle and life
+// limits of a launch (microseconds; < 0 keeps the value); a cap on the CTAs
+// of one launch (0: the co-resident maximum).
 void batch_set_hold_us(int device, double us);
+void batch_set_refill(int device, int on, double idle_us, double life_us);
+void batch_set_cap(int device, int ctas);
 // Statistics of the device's batcher: launches, solves, CTAs launched in all.
 void batch_stats(int device, long long* launches, long long* solves, long long* ctas);
 

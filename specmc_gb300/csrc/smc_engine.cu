@@ -1451,38 +1451,85 @@ __global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_engine_kernel(Engin
   pc.finish();
 }
 
-// The refinement solves of up to ENGINE_BATCH_MAX independent systems (any
-// mix of Schur and temperature operators and grid sizes) in one cooperative
-// launch: job j owns the CTAs [cta0, cta0 + G) and its own group barrier.
-// When its solve has ended, CTA 0 of the group -- after a last group barrier,
-// so no CTA of the group touches the job's buffers any more -- writes the
-// result block to host-mapped memory and then the done word, so the host
-// thread that owns the job can go on while the other solves of the batch run.
+// The refinement solves of independent systems (any mix of Schur and
+// temperature operators and grid sizes) in one cooperative launch: slot j
+// owns the CTAs [cta0, cta0 + G) and a group barrier of its own, and starts
+// with its first solve.  When a solve has ended, CTA 0 of the group -- after a
+// last group barrier, so no CTA of the group touches the solve's buffers any
+// more -- writes the result block to host-mapped memory and then the done
+// word, so the host thread that owns the solve goes on while the batch runs.
+// With a feed, the group's leader then claims the next solve the host has
+// published (waiting up to idle_ns for one, claiming none after life_ns),
+// hands the ticket to its CTAs through the group barrier, and every CTA of
+// the group copies that solve's descriptor into shared memory and runs it on
+// the slot's CTAs: a slot whose solve converged in a few Arnoldi steps does
+// not idle until the slowest solve of the launch ends.
+__device__ __forceinline__ int ld_acquire_sys(const volatile int* p) {
+  int v;
+  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __global__ void __launch_bounds__(ENG_THREADS, 2) smc_refine_batch_kernel(
     const __grid_constant__ RefineBatch B) {
   extern __shared__ __align__(256) unsigned char smraw[];
   __shared__ RefineShared RS;
+  __shared__ __align__(16) RefineJob sJ;
   int j = 0;
   while (j + 1 < B.njobs && (int)blockIdx.x >= B.job[j + 1].cta0) ++j;
-  const RefineJob& J = B.job[j];
-  const EngCtx e = eng_ctx_group(J.op32, J.G, (int)blockIdx.x - J.cta0);
-  GroupBar bar{J.bar, J.bar + 1, J.G, reinterpret_cast<int*>(J.bar + 2), B.err, B.timeout_ns};
-  PhaseClock pc;
-  pc.init(nullptr, e);
-  int info = 1, total = 0, outer = 0;
-  double rel = 0.0;
-  refine_solve<GroupBar>(J.op32, J.op64, J.io, J.rf, RS, smraw, e, bar, pc, info, total, outer,
-                         rel);
-  bar.sync();
-  if (e.b == 0 && e.tid == 0) {
-    volatile EngineJobResult* out = J.out;
-    out->info = info;
-    out->iters = total;
-    out->outer = outer;
-    out->rel = rel;
-    out->failed = *(volatile int*)(J.bar + 2);
-    __threadfence_system();
-    out->done = J.seq;
+  const int cta0 = B.job[j].cta0, G = B.job[j].G;
+  unsigned int* sb = B.slot_bar + 4 * j;
+  GroupBar bar{sb, sb + 1, G, reinterpret_cast<int*>(sb + 2), B.err, B.timeout_ns};
+  const long long t_start = global_ns();
+  const RefineJob* J = &B.job[j];
+  while (true) {
+    const EngCtx e = eng_ctx_group(J->op32, G, (int)blockIdx.x - cta0);
+    PhaseClock pc;
+    pc.init(nullptr, e);
+    int info = 1, total = 0, outer = 0;
+    double rel = 0.0;
+    refine_solve<GroupBar>(J->op32, J->op64, J->io, J->rf, RS, smraw, e, bar, pc, info, total,
+                           outer, rel);
+    bar.sync();
+    if (e.b == 0 && e.tid == 0) {
+      volatile EngineJobResult* out = J->out;
+      out->info = info;
+      out->iters = total;
+      out->outer = outer;
+      out->rel = rel;
+      out->failed = *(volatile int*)(sb + 2);
+      __threadfence_system();
+      out->done = J->seq;
+    }
+    if (!B.feed) break;
+    // the next solve: the leader claims a published ticket (bounded wait)
+    if (e.b == 0 && e.tid == 0) {
+      int t = -1;
+      const long long t0 = global_ns();
+      while (true) {
+        const long long now = global_ns();
+        if (now - t_start > B.life_ns || now - t0 > B.idle_ns) break;
+        if (*(volatile int*)(sb + 2)) break;          // this group's barrier timed out
+        const int pub = ld_acquire_sys(&B.feed->published);
+        const int c = *(volatile int*)B.claimed;
+        if (c < pub) {
+          if (atomicCAS(B.claimed, c, c + 1) == c) { t = c; break; }
+          continue;
+        }
+        __nanosleep(256);
+      }
+      *(volatile int*)(B.slot_ticket + j) = t;
+    }
+    bar.sync();
+    const int t = *(volatile int*)(B.slot_ticket + j);
+    if (t < 0) break;
+    // every CTA copies the solve's descriptor (published before the ticket)
+    const volatile unsigned int* src =
+        reinterpret_cast<const volatile unsigned int*>(&B.feed->ring[t % BATCH_FEED_CAP]);
+    unsigned int* dst = reinterpret_cast<unsigned int*>(&sJ);
+    for (int w = threadIdx.x; w < (int)(sizeof(RefineJob) / 4); w += blockDim.x) dst[w] = src[w];
+    __syncthreads();
+    J = &sJ;
   }
 }
 
@@ -1566,6 +1613,7 @@ int refine_batch_capacity(size_t smem, int num_sms) {
 void refine_batch_launch(cudaStream_t s, const RefineBatch& B, size_t smem) {
   auto kern = smc_refine_batch_kernel;
   allow_max_smem((const void*)kern);
+  if (!B.slot_bar) throw std::runtime_error("refine batch: no slot barrier words");
   int G = 0;
   for (int j = 0; j < B.njobs; ++j) {
     if (B.job[j].cta0 != G) throw std::runtime_error("refine batch: CTA ranges not contiguous");

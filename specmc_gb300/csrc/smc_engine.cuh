@@ -127,26 +127,44 @@ struct EngineJobResult {
 };
 
 // One solve of a batched launch: the operators and workspace of its handle
-// (exactly what fgmres_refine_engine takes), its CTA range [cta0, cta0 + G),
-// three zero-initialised words of global memory for its group barrier
-// (arrivals, generation, timeout flag), and the device address of its
+// (exactly what fgmres_refine_engine takes), the CTA range [cta0, cta0 + G)
+// of its slot when it is a slot's first solve, and the device address of its
 // result block.
 struct RefineJob {
   EngineOps op32, op64;
   EngineIO io;
   RefineIO rf;
-  unsigned int* bar = nullptr;
   EngineJobResult* out = nullptr;
   int seq = 0;
   int cta0 = 0, G = 0;
 };
 
 constexpr int ENGINE_BATCH_MAX = 16;
+constexpr int BATCH_FEED_CAP = 256;
+
+// Solves handed to a running batch (host-mapped pinned memory): the host
+// writes ring[i] and then, after a release fence, published = i + 1; a group
+// that has finished its solve claims the next ticket (a device counter) and
+// runs that solve on its own CTAs.
+struct BatchFeed {
+  volatile int published;
+  int pad[63];
+  RefineJob ring[BATCH_FEED_CAP];
+};
+
 struct RefineBatch {
-  RefineJob job[ENGINE_BATCH_MAX];
+  RefineJob job[ENGINE_BATCH_MAX];   // the first solve of each group (slot)
   int njobs = 0;
   int* err = nullptr;             // raised when any group barrier timed out
   long long timeout_ns = 2000000000LL;
+  unsigned int* slot_bar = nullptr;  // 4 zeroed words per slot: arrivals, generation, time-out
+  // refill: null feed = each group runs its first solve only
+  BatchFeed* feed = nullptr;         // device address of the host-mapped feed
+  int* claimed = nullptr;            // tickets taken (device, zero at launch)
+  int* slot_ticket = nullptr;        // per slot: the ticket its leader claimed (-1: none)
+  long long idle_ns = 200000;        // a group leaves after this long without a queued solve
+  long long life_ns = 20000000;      // no solve is claimed after this long (other cooperative
+                                     // kernels wait for the launch to end)
 };
 
 // dynamic shared memory of a refinement solve (the larger of its two operators)

@@ -436,7 +436,6 @@ struct Model {
   // runs the solves of many handles in one cooperative launch (smc_batch.cu)
   bool batch_mode = false;
   int batch_ctas = 0;                // CTAs of one solve in a batch (0: the default)
-  unsigned int* dBatchBar = nullptr; // group barrier words (zeroed)
   EngineJobResult* hBatchRes = nullptr;   // host-mapped result block
   EngineJobResult* dBatchRes = nullptr;   // its device address
   cudaEvent_t batch_ready = nullptr;
@@ -471,13 +470,11 @@ struct Model {
 
   void enable_batch(bool on) {
     if (on && !fast) throw std::runtime_error("engine_batch needs a SMC_MIXED handle");
-    if (on && !dBatchBar) {
-      dBatchBar = mem.alloc<unsigned int>(4);
+    if (on && !hBatchRes) {
       SMC_CUDA(cudaHostAlloc((void**)&hBatchRes, sizeof(EngineJobResult), cudaHostAllocMapped));
       std::memset((void*)hBatchRes, 0, sizeof(EngineJobResult));
       SMC_CUDA(cudaHostGetDevicePointer((void**)&dBatchRes, (void*)hBatchRes, 0));
       SMC_CUDA(cudaEventCreateWithFlags(&batch_ready, cudaEventDisableTiming));
-      SMC_CUDA(cudaStreamSynchronize(stream));       // the zeroed barrier words
     }
     batch_mode = on;
   }
@@ -498,7 +495,6 @@ struct Model {
     r.job.op64 = op64;
     r.job.io = io;
     r.job.rf = rf;
-    r.job.bar = dBatchBar;
     r.job.out = dBatchRes;
     r.job.seq = ++batch_seq;
     r.G = std::min(batch_grid(kind), io.max_grid);
@@ -2490,6 +2486,15 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
     } else if (k == "engine_batch_hold_us") {
       if (!(value >= 0.0 && value <= 1e6)) throw std::runtime_error("engine_batch_hold_us must be >= 0");
       smc::batch_set_hold_us(h->m.device, value);
+    } else if (k == "engine_batch_refill") {
+      smc::batch_set_refill(h->m.device, value != 0.0 ? 1 : 0, -1.0, -1.0);
+    } else if (k == "engine_batch_idle_us" || k == "engine_batch_life_us") {
+      if (!(value >= 0.0 && value <= 1e7)) throw std::runtime_error(k + " must be >= 0");
+      smc::batch_set_refill(h->m.device, 1, k == "engine_batch_idle_us" ? value : -1.0,
+                            k == "engine_batch_life_us" ? value : -1.0);
+    } else if (k == "engine_batch_gpu_ctas") {
+      if (!(value >= 0.0 && value <= 1e6)) throw std::runtime_error("engine_batch_gpu_ctas must be >= 0");
+      smc::batch_set_cap(h->m.device, (int)value);
     } else throw std::runtime_error("unknown option " + k);
   })
 }

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libspecmc_gb300.so")
 SOURCES = ("smc_spectral.cu", "smc_dense.cu", "smc_schur.cu", "smc_krylov.cu",
-           "smc_pseudo.cu", "smc_fastops.cu", "smc_engine.cu", "smc_noalloc.cu", "smc_tala.cu", "smc_batch.cu", "smc_tc.cu",
+           "smc_pseudo.cu", "smc_fastops.cu", "smc_engine.cu", "smc_noalloc.cu", "smc_tala.cu", "smc_batch.cu", "smc_tc.cu", "smc_tclu.cu",
            "smc_runtime.cu")
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
               "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",

@@ -593,7 +593,8 @@ __global__ void __launch_bounds__(256) smc_zlu_gemm_kernel(double2* __restrict__
   }
 }
 
-void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work) {
+void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work, void* tcwork,
+               int* tcerr) {
   const size_t gsm = (size_t)2 * ZNB * GT * sizeof(double2);
   allow_max_smem((const void*)smc_zlu_gemm_kernel);
   int G = c.num_sms;
@@ -617,9 +618,13 @@ void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work) {
     if (rest > 0) {
       smc_zlu_trsm_kernel<<<ceil_div(rest, TRSM_WARPS), 32 * TRSM_WARPS, 0, c.s>>>(A, n, p0, nbp);
       SMC_LAUNCH_CHECK(c);
-      dim3 g(ceil_div(rest, GT), ceil_div(rest, GT));
-      smc_zlu_gemm_kernel<<<g, 256, gsm, c.s>>>(A, n, p0, nbp);
-      SMC_LAUNCH_CHECK(c);
+      if (tcwork) {
+        tclu_update(c, A, n, p0, nbp, tcwork, tcerr);
+      } else {
+        dim3 g(ceil_div(rest, GT), ceil_div(rest, GT));
+        smc_zlu_gemm_kernel<<<g, 256, gsm, c.s>>>(A, n, p0, nbp);
+        SMC_LAUNCH_CHECK(c);
+      }
     }
   }
 }

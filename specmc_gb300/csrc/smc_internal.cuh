@@ -270,8 +270,13 @@ void lu_small_solve(const Ctx& c, const double* LU, const int* piv, long long lu
                     const double2* b, double2* x, int N, int count, double alpha,
                     int zero_tau, const int* skip_mask);
 // dense complex LU (column-major n x n) with partial pivoting (|re|+|im| pivot
-// choice, as LAPACK zgetrf); piv 0-based
-void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work);
+// choice, as LAPACK zgetrf); piv 0-based.  With tcwork (tclu_work_bytes(n)
+// bytes) the trailing updates run on the tensor cores (smc_tclu.cu, FP64
+// accuracy; *tcerr raised if one of its CTAs timed out)
+void zlu_dense(const Ctx& c, double2* A, int* piv, int n, double2* work, void* tcwork = nullptr,
+               int* tcerr = nullptr);
+size_t tclu_work_bytes(int n);
+void tclu_update(const Ctx& c, double2* A, int n, int p0, int nbp, void* work, int* err);
 // inverses of the 64 x 64 diagonal blocks of L and U (column-major blocks)
 void zlu_diag_inverses(const Ctx& c, const double2* LU, int n, double2* invL, double2* invU);
 // x = A^{-1} b with a zlu_dense factor; perm = composed row permutation;

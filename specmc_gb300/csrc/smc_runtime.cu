@@ -455,16 +455,27 @@ struct Model {
     }
     ctx.tc = on ? tc_cache.get() : nullptr;
   }
-  // a tensor-core CTA that gave up waiting wrote NaN and raised the flag
+  // the dense Schur LU's trailing updates on the tensor cores (smc_tclu.cu)
+  bool tc_lu = false;
+  void* dTcLuWork = nullptr;
+  int* dTcLuErr = nullptr;
+  void enable_tc_lu(bool on) {
+    tc_lu = on;
+    if (on && !dTcLuErr) dTcLuErr = mem.alloc<int>(1);
+  }
+  // a tensor-core CTA that gave up waiting wrote NaN (contractions) or left
+  // its tile alone (LU update) and raised a flag
   void check_tc() {
-    if (!tc_cache || !tc_cache->err) return;
-    int e = 0;
-    SMC_CUDA(cudaMemcpyAsync(hbuf, tc_cache->err, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    SMC_CUDA(cudaStreamSynchronize(stream));
-    std::memcpy(&e, hbuf, sizeof(int));
-    if (e) {
-      SMC_CUDA(cudaMemsetAsync(tc_cache->err, 0, sizeof(int), stream));
-      throw std::runtime_error("tensor-core contraction: an mbarrier wait timed out");
+    for (int* flag : {tc_cache ? tc_cache->err : nullptr, dTcLuErr}) {
+      if (!flag) continue;
+      int e = 0;
+      SMC_CUDA(cudaMemcpyAsync(hbuf, flag, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      SMC_CUDA(cudaStreamSynchronize(stream));
+      std::memcpy(&e, hbuf, sizeof(int));
+      if (e) {
+        SMC_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), stream));
+        throw std::runtime_error("tensor-core kernel: an mbarrier wait timed out");
+      }
     }
   }
 
@@ -1442,7 +1453,8 @@ struct Model {
     {
       // algorithmic work: complex LU, 8/3 n^3 real flops
       ProfScope ps(ctx, "schur_lu", 8.0 / 3.0 * (double)n * n * n, 0);
-      zlu_dense(ctx, dSchur, dSchurPiv, (int)n, dAsmWork);
+      if (tc_lu && !dTcLuWork) dTcLuWork = mem.alloc<unsigned char>(tclu_work_bytes((int)n));
+      zlu_dense(ctx, dSchur, dSchurPiv, (int)n, dAsmWork, tc_lu ? dTcLuWork : nullptr, dTcLuErr);
       zlu_diag_inverses(ctx, dSchur, (int)n, dSchurInvL, dSchurInvU);
     }
     std::vector<int> piv(n), perm(n);
@@ -2478,6 +2490,8 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
       h->m.eng_phase = value != 0.0;
     } else if (k == "tc_transforms") {
       h->m.enable_tc(value != 0.0);
+    } else if (k == "tc_lu") {
+      h->m.enable_tc_lu(value != 0.0);
     } else if (k == "engine_batch") {
       h->m.enable_batch(value != 0.0);
     } else if (k == "engine_batch_ctas") {

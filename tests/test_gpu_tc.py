@@ -85,3 +85,38 @@ def test_tc_mixed_march_matches_simt(gb):
         m.close()
     for key in ("Nu_top", "urms", "Nu_energy"):
         assert abs(out[1.0][key] - out[0.0][key]) <= 1e-9 * abs(out[0.0][key]), key
+
+
+def _cfg_kw(g):
+    return {k[4:]: g[k].item() for k in g.files if k.startswith("cfg_")}
+
+
+@pytest.mark.parametrize("case,steps", [("march_etaT_32x24.npz", None), ("march_etaT_64x96.npz", None)])
+def test_tc_lu_plain_march_matches_reference(gb, case, steps):
+    """The plain form with the dense Schur LU's trailing updates on the tensor
+    cores (option "tc_lu") against the reference's own march records: the
+    same bars as the FP64 SIMT LU (state 1e-7, Nu / Vrms 1e-8) and the same
+    refresh and defect-correction counts (the 32x24 march refreshes its
+    factor 24 times in 25 steps)."""
+    import os
+    from conftest import GOLDEN
+    api, CC, lib = gb
+    g = np.load(os.path.join(GOLDEN, case))
+    m = api.build_model(CC(**_cfg_kw(g)))
+    lib.check(m._lib.smc_set_option(m._h, b"tc_lu", 1.0))
+    s = np.array(g["that0"], copy=True)
+    worst = 0.0
+    for n in range(len(g["dts"])):
+        dt = api.production_dt(m, s)
+        assert abs(dt - g["dts"][n]) <= 1e-9 * g["dts"][n]
+        s = m.step(s, dt)
+        worst = max(worst, _rel(s, g["states"][n]))
+    assert worst < 1e-7, worst
+    d = m.diagnostics(s)
+    for key in ("Nu_top", "urms"):
+        ref = g["diag_" + key].item()
+        assert abs(d[key] - ref) <= 1e-8 * abs(ref), (key, d[key], ref)
+    c = m.counters()
+    for key in ("n_refresh", "n_defect", "n_defect_failed"):
+        assert c[key] == int(g["ctr_" + key]), (key, c[key])
+    m.close()

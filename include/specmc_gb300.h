@@ -243,7 +243,19 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
  * threads (smc_march_many sets it).  "engine_batch_ctas" (>= 0): CTAs of one
  * batched solve (0: one per Fourier row, at least 32).
  * "engine_batch_hold_us" (>= 0, default 50; applies to the handle's device):
- * how long the oldest queued solve waits for others before a batch starts. */
+ * how long the oldest queued solve waits for others before a batch starts.
+ * "engine_batch_refill" (0/1, default 1), "engine_batch_idle_us" (default
+ * 200), "engine_batch_life_us" (default 20000): a running batch takes solves
+ * queued after its launch into slots that have finished theirs, until a slot
+ * has waited idle_us for one or the launch has lived life_us (per device).
+ * "engine_batch_gpu_ctas" (>= 0, default 0 = the co-resident maximum): cap on
+ * the CTAs of one batched launch (per device).
+ * "tc_transforms" (0/1, default 0): the z-contractions of the transforms by
+ * the basis operators on the tensor cores (tcgen05, bf16 Ozaki slices with
+ * exact FP32 accumulation: FP64-accurate; Nz <= 128).
+ * "tc_lu" (0/1, default 1): the trailing updates of the dense Schur LU
+ * (the legacy route's lagged factor, stokes/lagged_stokes.py:274-300) on the
+ * tensor cores, FP64-accurate by the same splitting; 0 = FP64 SIMT. */
 int smc_set_option(smc_handle* h, const char* key, double value);
 
 /* RBCImplicitTheta.reset_history (implicit_theta.py:601-606). */

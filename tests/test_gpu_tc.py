@@ -91,8 +91,8 @@ def _cfg_kw(g):
     return {k[4:]: g[k].item() for k in g.files if k.startswith("cfg_")}
 
 
-@pytest.mark.parametrize("case,steps", [("march_etaT_32x24.npz", None), ("march_etaT_64x96.npz", None)])
-def test_tc_lu_plain_march_matches_reference(gb, case, steps):
+@pytest.mark.parametrize("case", ["march_etaT_32x24.npz", "march_etaT_64x96.npz"])
+def test_tc_lu_plain_march_matches_reference(gb, case):
     """The plain form with the dense Schur LU's trailing updates on the tensor
     cores (option "tc_lu") against the reference's own march records: the
     same bars as the FP64 SIMT LU (state 1e-7, Nu / Vrms 1e-8) and the same

@@ -253,6 +253,10 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
  * "tc_transforms" (0/1, default 0): the z-contractions of the transforms by
  * the basis operators on the tensor cores (tcgen05, bf16 Ozaki slices with
  * exact FP32 accumulation: FP64-accurate; Nz <= 128).
+ * "warm_start" (0/1, SMC_MIXED handles, default 1): each refinement solve
+ * starts from the previous solve's solution (the last Stokes unknown, the
+ * last step's temperature) and its FP64 residual instead of from zero; the
+ * stopping test ||b - A x|| <= rtol ||b|| is unchanged.
  * "tc_lu" (0/1, default 1): the trailing updates of the dense Schur LU
  * (the legacy route's lagged factor, stokes/lagged_stokes.py:274-300) on the
  * tensor cores, FP64-accurate by the same splitting; 0 = FP64 SIMT. */

@@ -1356,12 +1356,12 @@ __device__ void refine_solve(const EngineOps& op32, const EngineOps& op64, const
   const long long per = (n + e.G - 1) / e.G;
   const long long lo = (long long)e.b * per, hi = min(n, lo + per);
   double* npr = io.npart + e.G;           // the inner solve uses io.npart[0, G)
-  // x = 0, r = b, ||b||
+  // x = 0 (or the guess the caller left in x), r = b, ||b||
   {
     double s = 0.0;
     for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
       const double2 bb = rf.b[t];
-      rf.x[t] = make_double2(0.0, 0.0);
+      if (!rf.warm) rf.x[t] = make_double2(0.0, 0.0);
       rf.r[t] = bb;
       s += bb.x * bb.x + bb.y * bb.y;
     }
@@ -1384,6 +1384,36 @@ __device__ void refine_solve(const EngineOps& op32, const EngineOps& op64, const
   o64.b = rf.b;
   o64.x = rf.x;
   o64.r = rf.r;
+  // r = b - A64 x and its norm: the FP64 pass that ends every outer iteration
+  auto residual64 = [&]() -> double {
+    phase_prep<double>(op64, o64, 2, 0, 1.0, nullptr, 0, S64, e, nullptr, 1.0);
+    grid.sync();
+    pc.mark(EP_REF_PREP);
+    if (op64.kind == 0) ph_schur_x<double>(op64, smraw, e);
+    else ph_theta_x<double>(op64, smraw, e);
+    grid.sync();
+    pc.mark(EP_REF_XCONV);
+    if (e.tid == 0) s_nacc64 = 0.0;
+    __syncthreads();
+    phase_post<double>(op64, o64, true, rf.x, 1.0, 0, S64, nullptr, &s_nacc64, e);
+    __syncthreads();
+    if (e.tid == 0) npr[e.b] = s_nacc64;
+    grid.sync();
+    return sqrt(reduce_scalar<double>(npr, e.G, s_red, e));
+  };
+  if (rf.warm && bn > 0.0 && isfinite(bn)) {
+    // start from the caller's guess (the previous solve's solution): its
+    // residual instead of b; a non-finite one falls back to x = 0
+    beta = residual64();
+    if (!isfinite(beta)) {
+      for (long long t = lo + e.tid; t < hi; t += blockDim.x) {
+        rf.x[t] = make_double2(0.0, 0.0);
+        rf.r[t] = rf.b[t];
+      }
+      grid.sync();
+      beta = bn;
+    }
+  }
   while (outer < 12) {
     if (beta <= tol) { info = 0; break; }
     if (!isfinite(beta)) { info = 3; break; }
@@ -1403,22 +1433,8 @@ __device__ void refine_solve(const EngineOps& op32, const EngineOps& op64, const
     }
     grid.sync();
     pc.mark(EP_REF_XUPD);
-    // r = b - A64 x
-    phase_prep<double>(op64, o64, 2, 0, 1.0, nullptr, 0, S64, e, nullptr, 1.0);
-    grid.sync();
-    pc.mark(EP_REF_PREP);
-    if (op64.kind == 0) ph_schur_x<double>(op64, smraw, e);
-    else ph_theta_x<double>(op64, smraw, e);
-    grid.sync();
-    pc.mark(EP_REF_XCONV);
-    if (e.tid == 0) s_nacc64 = 0.0;
-    __syncthreads();
-    phase_post<double>(op64, o64, true, rf.x, 1.0, 0, S64, nullptr, &s_nacc64, e);
-    __syncthreads();
-    if (e.tid == 0) npr[e.b] = s_nacc64;
-    grid.sync();
+    beta = residual64();                            // r = b - A64 x
     pc.mark(EP_REF_POST);
-    beta = sqrt(reduce_scalar<double>(npr, e.G, s_red, e));
     ++outer;
     pc.mark(EP_REFINE);
     if (its == 0 && beta > tol) break;             // no progress possible

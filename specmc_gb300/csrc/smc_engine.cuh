@@ -111,6 +111,7 @@ struct RefineIO {
   double floor = 1e-4;          // smallest inner relative tolerance
   int maxiter = 800;            // inner Arnoldi steps in all
   double* res = nullptr;        // -> final relative residual (device)
+  int warm = 0;                 // 1: x holds the initial guess (else x starts at 0)
 };
 // io: the engine workspace; io.result -> {info, inner steps, outer passes}
 void fgmres_refine_engine(const Ctx& c, const EngineOps& op32, const EngineOps& op64,

@@ -256,7 +256,11 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
  * "warm_start" (0/1, SMC_MIXED handles, default 1): each refinement solve
  * starts from the previous solve's solution (the last Stokes unknown, the
  * last step's temperature) and its FP64 residual instead of from zero; the
- * stopping test ||b - A x|| <= rtol ||b|| is unchanged.
+ * stopping test ||b - A x|| <= rtol ||b|| is unchanged.  "warm_extrapolate"
+ * (0..3, default 1): bit 0 extrapolates the Stokes guess linearly in time
+ * from the last two solves, bit 1 the temperature guess from the last two
+ * steps (off by default: such guesses stalled the FP32-refined temperature
+ * solves on the headline march).
  * "tc_lu" (0/1, default 1): the trailing updates of the dense Schur LU
  * (the legacy route's lagged factor, stokes/lagged_stokes.py:274-300) on the
  * tensor cores, FP64-accurate by the same splitting; 0 = FP64 SIMT. */

@@ -461,6 +461,14 @@ struct Model {
   // FP64 residual instead of b; the stopping test ||b - A x|| <= rtol ||b|| is
   // the same, so the same tolerance is met from a closer start
   bool warm_start = true;
+  // bit 0: the Stokes guess extrapolated linearly in time from the last two
+  // solves (measured: 19% fewer BFBT iterations over the 200-step headline
+  // march); bit 1: the temperature guess extrapolated from the last two steps
+  // -- off: from such guesses the FP32-refined temperature solves stopped
+  // converging within their budget (135 of 200 steps on the headline march,
+  // which then diverged), while the previous step's temperature alone as the
+  // guess converges as from zero
+  int warm_extrap = 1;
   // extrapolated guesses: the Stokes unknown of the last two solves (one per
   // step) and the steps' dt, for a linear extrapolation in time
   double2 *dSxHist = nullptr, *dSxTmp = nullptr;
@@ -472,7 +480,8 @@ struct Model {
     if (!warm_start) return;
     if (!dSxHist) { dSxHist = mem.alloc<double2>(n); dSxTmp = mem.alloc<double2>(n); }
     const long long cur = steps_done;
-    const bool extrap = sx_step == cur - 1 && sx_hist_step == cur - 2 && step_dt[1] > 0.0;
+    const bool extrap = (warm_extrap & 1) && sx_step == cur - 1 && sx_hist_step == cur - 2 &&
+                        step_dt[1] > 0.0;
     vec_copy(ctx, dSxTmp, x, n);                                  // x_n
     if (extrap) {
       const double r = step_dt[0] / step_dt[1];
@@ -1945,7 +1954,7 @@ struct Model {
       if (inner_fp32) {
         if (use_engine) {
           // guess: the last step's temperature extrapolated linearly in time
-          if (warm_start && have_prev && dt_prev > 0.0) {
+          if (warm_start && (warm_extrap & 2) && have_prev && dt_prev > 0.0) {
             const double r = dt / dt_prev;
             vec_axpby(ctx, dRhs, make_double2(-r, 0.0), dPrev, make_double2(1.0 + r, 0.0), n);
           }
@@ -2530,6 +2539,9 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
       h->m.eng_phase = value != 0.0;
     } else if (k == "warm_start") {
       h->m.warm_start = value != 0.0;
+    } else if (k == "warm_extrapolate") {
+      if (!(value >= 0.0 && value <= 3.0)) throw std::runtime_error("warm_extrapolate must be 0..3");
+      h->m.warm_extrap = (int)value;
     } else if (k == "tc_transforms") {
       h->m.enable_tc(value != 0.0);
     } else if (k == "tc_lu") {

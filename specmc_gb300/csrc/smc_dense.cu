@@ -91,6 +91,126 @@ __global__ void smc_lu_small_kernel(double* __restrict__ A, int* __restrict__ pi
   if (tid == 0 && info) info[blockIdx.x] = inf;
 }
 
+// bit-pattern tests: no FP64 instruction (GB300 issues those through a pipe
+// of about two lanes per clock per SM, compares included)
+__device__ __forceinline__ bool lus_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+
+// The explicit inverse operators G_k = A_k^{-1} P (P: the identity with the
+// two tau columns zeroed, vv_stokes.py:281-296) from the factors: CTA (k, b)
+// stages the factor of wavenumber k and the reciprocals of its diagonal in
+// shared memory and solves 2 W columns of G_k (W warps), each warp two
+// columns at a time with the columns in registers (lane l holds rows l,
+// l + 32, ...) and x_c broadcast by shuffle: the row interchanges (exact on a
+// unit vector: only the one moves), unit-lower forward substitution, upper
+// back substitution multiplying by the reciprocal of the diagonal.  A step
+// whose broadcast x_c is zero in both columns is skipped (it would change
+// entries by signed zeros at most): the forward substitution of a column
+// starts at the row its one moved to.  G is written row-major, its transpose
+// (GT64) and the transpose as (hi, lo) float pairs (GT32), each when not null.
+constexpr int GL_ROWS = 3;                         // rows a lane holds
+constexpr int GL_MAXN = 32 * GL_ROWS;              // 96
+
+template <int ROWS>
+__device__ __forceinline__ double gl_pick(const double (&x)[ROWS], int j) {
+  double v = x[0];
+#pragma unroll
+  for (int t = 1; t < ROWS; ++t)
+    if (j == t) v = x[t];
+  return v;
+}
+
+__global__ void __launch_bounds__(1024)
+smc_green_lu_kernel(const double* __restrict__ LU, const int* __restrict__ piv, double* __restrict__ G,
+                    double* __restrict__ GT64, float2* __restrict__ GT32, int N) {
+  extern __shared__ double a[];                   // N*N factor of wavenumber k, then N reciprocals
+  constexpr int ROWS = GL_ROWS;
+  __shared__ int s_piv[GL_MAXN];
+  double* rd = a + (long long)N * N;
+  const int k = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long NN = (long long)N * N, kb = (long long)k * NN;
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) a[i] = LU[kb + i];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    s_piv[i] = piv[(long long)k * N + i];
+    rd[i] = 1.0 / LU[kb + (long long)i * N + i];
+  }
+  __syncthreads();
+  const int q0 = blockIdx.y * 2 * (blockDim.x >> 5) + 2 * warp, q1 = q0 + 1;
+  if (q0 >= N) return;
+  int pos0 = q0, pos1 = q1;
+  for (int i = 0; i < N; ++i) {
+    const int pi = s_piv[i];
+    pos0 = pos0 == i ? pi : (pos0 == pi ? i : pos0);
+    pos1 = pos1 == i ? pi : (pos1 == pi ? i : pos1);
+  }
+  double x0[ROWS], x1[ROWS];
+#pragma unroll
+  for (int j = 0; j < ROWS; ++j) {
+    const int r = lane + 32 * j;
+    x0[j] = r == pos0 ? 1.0 : 0.0;
+    x1[j] = r == pos1 ? 1.0 : 0.0;
+  }
+  // (row chunks that need no update are skipped by warp-uniform branches: a
+  // warp-wide FP64 instruction costs its 32 lanes whatever the predicate)
+  for (int c = min(pos0, pos1); c < N; ++c) {     // unit lower
+    const int cj = c >> 5, cl = c & 31;
+    const double xc0 = __shfl_sync(0xffffffffu, gl_pick(x0, cj), cl);
+    const double xc1 = __shfl_sync(0xffffffffu, gl_pick(x1, cj), cl);
+    if (lus_zero(xc0) && lus_zero(xc1)) continue;
+#pragma unroll
+    for (int j = 0; j < ROWS; ++j) {
+      if (32 * j + 31 <= c) continue;
+      const int r = lane + 32 * j;
+      const double l = (r > c && r < N) ? a[r + c * N] : 0.0;
+      const bool need = !lus_zero(l);
+      if (__any_sync(0xffffffffu, need) && need) {
+        x0[j] -= l * xc0;
+        x1[j] -= l * xc1;
+      }
+    }
+  }
+  for (int c = N - 1; c >= 0; --c) {              // upper
+    const int cj = c >> 5, cl = c & 31;
+    double xc0 = __shfl_sync(0xffffffffu, gl_pick(x0, cj), cl);
+    double xc1 = __shfl_sync(0xffffffffu, gl_pick(x1, cj), cl);
+    if (lus_zero(xc0) && lus_zero(xc1)) continue;
+    const double r_c = rd[c];
+    xc0 *= r_c;
+    xc1 *= r_c;
+#pragma unroll
+    for (int j = 0; j < ROWS; ++j) {
+      if (32 * j > c) continue;
+      const int r = lane + 32 * j;
+      if (r == c) {
+        x0[j] = xc0;
+        x1[j] = xc1;
+      }
+      const double u = r < c ? a[r + c * N] : 0.0;
+      const bool need = !lus_zero(u);
+      if (__any_sync(0xffffffffu, need) && need) {
+        x0[j] -= u * xc0;
+        x1[j] -= u * xc1;
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < ROWS; ++j) {
+    const int r = lane + 32 * j;
+    if (r >= N) continue;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int q = q0 + h;
+      if (q >= N) continue;
+      const double g = q < N - 2 ? (h ? x1[j] : x0[j]) : 0.0;
+      if (G) G[kb + (long long)r * N + q] = g;
+      if (GT64) GT64[kb + (long long)q * N + r] = g;
+      if (GT32) {
+        const float hi = (float)g;
+        GT32[kb + (long long)q * N + r] = make_float2(hi, (float)(g - (double)hi));
+      }
+    }
+  }
+}
+
 // The same factorisation for matrices too large for shared memory (Nz of a
 // few hundred): one CTA per matrix working in place in global memory (the
 // matrix stays in L2 while its CTA factors it); the pivot column and the
@@ -162,6 +282,7 @@ __global__ void __launch_bounds__(512) smc_lu_medium_kernel(double* __restrict__
   if (tid == 0 && info) info[blockIdx.x] = inf;
 }
 
+
 void lu_small_batched(const Ctx& c, double* A, int* piv, int* info, int N, int count) {
   size_t smem = (size_t)N * N * sizeof(double);
   if (smem > 200 * 1024) {
@@ -172,6 +293,26 @@ void lu_small_batched(const Ctx& c, double* A, int* piv, int* info, int N, int c
   allow_max_smem((const void*)smc_lu_small_kernel);
   smc_lu_small_kernel<<<count, 256, smem, c.s>>>(A, piv, info, N);
   SMC_LAUNCH_CHECK(c);
+}
+
+bool lu_green_batched(const Ctx& c, const double* A, double* LU, int* piv, double* G, double* GT64,
+                      float2* GT32, int N, int count) {
+  if (N > GL_MAXN) return false;
+  if (A != LU)
+    SMC_CUDA(cudaMemcpyAsync(LU, A, sizeof(double) * N * N * (size_t)count, cudaMemcpyDeviceToDevice, c.s));
+  lu_small_batched(c, LU, piv, nullptr, N, count);
+  const size_t smem = (size_t)(N * N + N) * sizeof(double);
+  // columns per CTA: the CTAs that fit on the GPU at once share the count * N
+  // columns (two per warp, 4..32 warps)
+  const int fit = std::max(1, (int)((227 * 1024) / (smem + 1024)));
+  const int slots = c.num_sms * fit;
+  const int per = (int)((count * (long long)N + slots - 1) / slots);
+  const int warps = std::min(32, std::max(4, (per + 1) / 2));
+  const dim3 grd(count, (N + 2 * warps - 1) / (2 * warps));
+  allow_max_smem((const void*)smc_green_lu_kernel);
+  smc_green_lu_kernel<<<grd, 32 * warps, smem, c.s>>>(LU, piv, G, GT64, GT32, N);
+  SMC_LAUNCH_CHECK(c);
+  return true;
 }
 
 // In-place solve of one real LU factor (column-major, LAPACK ipiv) with a

@@ -58,6 +58,10 @@ struct Profiler {
   void reset();
   // a region timed on the device by other means (ms, launch count)
   void add(const char* name, double ms_, long long n_);
+  // work of a region known only after its launch (a deferred engine result)
+  void add_work(const char* name, double w) {
+    if (wants(name)) work[tag_of(name)] += w;
+  }
   ~Profiler();
 };
 
@@ -265,6 +269,14 @@ void memo_compare(const Ctx& c, const double2* that, const double2* cthat,
 // (column-major, stride N*N); piv 0-based LAPACK ipiv; info[b] = first zero pivot+1
 void lu_small_batched(const Ctx& c, double* A, int* piv, int* info, int N,
                       int count);
+// the same factorisation of A (may equal LU) into LU / piv, then the
+// explicit inverse operators G_k = A_k^{-1} P (P: identity with rows N-2, N-1
+// zeroed) from the factors over several CTAs per matrix: G row-major, GT64
+// its transpose, GT32 the transpose as (hi, lo) floats, each when not null.
+// False, with nothing launched, for N > 96 (the callers then run
+// green_from_lu and the transposes).
+bool lu_green_batched(const Ctx& c, const double* A, double* LU, int* piv, double* G,
+                      double* GT64, float2* GT32, int N, int count);
 // x_b = A_b^{-1} (alpha * P b_b): P zeroes rows N-2, N-1 when zero_tau
 void lu_small_solve(const Ctx& c, const double* LU, const int* piv, long long lu_stride,
                     const double2* b, double2* x, int N, int count, double alpha,

@@ -311,8 +311,13 @@ struct Model {
   bool resident_cur0 = true;
   DevMem mem;
   double* hbuf = nullptr;     // pinned scalars
-  unsigned char* hpin = nullptr;   // pinned: engine results (first 1 KB), BFBT profile
-  static_assert(64 + ENGINE_PHASES * sizeof(long long) <= 512, "engine phase slots overlap");
+  unsigned char* hpin = nullptr;   // pinned, 1 KB: engine results and phase counts
+  static_assert(64 + ENGINE_PHASES * sizeof(long long) <= 256, "engine phase slots overlap");
+  // pinned result slot of the refinement launches of kind k (0 Stokes, 1
+  // temperature): int info, iterations, outer passes at +0, the final relative
+  // residual at +16
+  int* eng_slot_res(int k) const { return reinterpret_cast<int*>(hpin + 256 + 64 * k); }
+  double* eng_slot_rel(int k) const { return reinterpret_cast<double*>(hpin + 256 + 64 * k + 16); }
   smc_counters ctr{};
 
   std::unique_ptr<HostBasis> hb;
@@ -359,6 +364,11 @@ struct Model {
   double2* sp[16];
   double* gr[10];
   double *dRed, *dScal;
+  // the viscosity pipeline's counters and the BFBT blocks' reuse state, kept
+  // on the device so that no step waits on them
+  EtaCtrDev* dEtaCtr = nullptr;
+  BfbtHold* dBfbtHold = nullptr;
+  double2* dBfbtHeld = nullptr;
   // Krylov
   int mmax = 0;
   double2 *dKV, *dKZ, *dKw, *dKx, *dKr, *dKh, *dKy, *dKb;
@@ -633,8 +643,11 @@ struct Model {
     // the isoviscous model keeps the constant-coefficient ChebTau operator
     if (tala && cfg.model != SMC_MODEL_CONST) tala_theta_ops(ctx, dD2, dkx, lam, dRho, slot->LU, N, Nk);
     else tau_ops(ctx, dD2, dkx, lam, slot->LU, N, Nk);
-    lu_small_batched(ctx, slot->LU, slot->piv, nullptr, N, Nk);
-    if (fast) {
+    if (!fast) {
+      lu_small_batched(ctx, slot->LU, slot->piv, nullptr, N, Nk);
+    } else if (!lu_green_batched(ctx, slot->LU, slot->LU, slot->piv, slot->Ginv, slot->GinvT64,
+                                 slot->GinvT32, N, Nk)) {
+      lu_small_batched(ctx, slot->LU, slot->piv, nullptr, N, Nk);
       green_from_lu(ctx, slot->LU, slot->piv, slot->Ginv, N, Nk);
       transpose_split(ctx, slot->Ginv, slot->GinvT32, N, N, Nk);
       transpose_as(ctx, slot->Ginv, slot->GinvT64, N, N, Nk);
@@ -656,7 +669,8 @@ struct Model {
     SMC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     ctx.s = stream; ctx.nlaunch = &nlaunch; ctx.num_sms = sms; ctx.prof = &prof;
     SMC_CUDA(cudaMallocHost(&hbuf, 4096 * sizeof(double)));
-    SMC_CUDA(cudaMallocHost(&hpin, 1024 + (size_t)N * sizeof(double2)));
+    SMC_CUDA(cudaMallocHost(&hpin, 1024));
+    for (auto& e : eng_done) SMC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     if (N < 4 || Nx < 4) throw std::runtime_error("Nx and Nz must be >= 4");
 
     hb.reset(new HostBasis(N));
@@ -713,6 +727,7 @@ struct Model {
     for (auto& p : gr) p = mem.alloc<double>((size_t)Np * N);
     dRed = mem.alloc<double>(4096);
     dScal = mem.alloc<double>(64);
+    dEtaCtr = mem.alloc<EtaCtrDev>(1);
     dPrev = mem.alloc<double2>(n); dPsiPrev = mem.alloc<double2>(n); dPsiN = mem.alloc<double2>(n);
     dMemoThat = mem.alloc<double2>(n); dMemoX = mem.alloc<double2>(n);
     dMemoPsi = mem.alloc<double2>(n); dMemoOm = mem.alloc<double2>(n);
@@ -889,6 +904,8 @@ struct Model {
         if (fast) setup_fused_schur();
         dBfbtRhs = mem.alloc<double2>(N);
         dBfbtProfC = mem.alloc<double2>(N);
+        dBfbtHeld = mem.alloc<double2>(N);
+        dBfbtHold = mem.alloc<BfbtHold>(1);
         // Galerkin mass matrix V^T W V and its LU (stokes/bfbt.py:74-84)
         std::vector<double> Mp(NN, 0.0);
         for (int a = 0; a < N; ++a)
@@ -985,6 +1002,12 @@ struct Model {
   // reduced operator LU from real Chebyshev coefficients `coef` (complex
   // storage, imaginary part ignored): P_k = (D2 - k^2) M + 2 k^2 [D,[D,M]] G_k
   void build_reduced_lu(const double2* coef, double* LU, int* piv) {
+    build_reduced_blocks(coef);
+    SMC_CUDA(cudaMemcpyAsync(LU, dPcm, sizeof(double) * Nk * NN, cudaMemcpyDeviceToDevice, stream));
+    lu_small_batched(ctx, LU, piv, nullptr, N, Nk);
+  }
+  // the reduced operators P_k (column-major) into dPcm
+  void build_reduced_blocks(const double2* coef) {
     // extract the real coefficient vector into dT3 (scratch), then M0
     realpart(coef, dT3, N);
     cheb_mult_real(ctx, dT3, dM0, N);
@@ -995,8 +1018,6 @@ struct Model {
     comm_combine(dDM0, dT2, dT3, dComm, (long long)NN);              // D2M - 2DMD + MD2
     bgemm(ctx, false, dComm, 0, false, dG, NN, dCommG, NN, N, Nk, 1.0);
     reduced_blocks(ctx, dDM0, dM0, dCommG, dV, dkx, dPcm, N, Nk);
-    SMC_CUDA(cudaMemcpyAsync(LU, dPcm, sizeof(double) * Nk * NN, cudaMemcpyDeviceToDevice, stream));
-    lu_small_batched(ctx, LU, piv, nullptr, N, Nk);
   }
 
   void realpart(const double2* in, double* out, int count);
@@ -1215,9 +1236,11 @@ struct Model {
   // The whole FP32-inner / FP64-outer refinement in one engine launch (the
   // device runs the outer loop of fgmres_refined below); -> (info, inner
   // Arnoldi steps), *true_res = final relative FP64 residual.
+  // defer: the launch's results are read at a later synchronisation
+  // (engine_result); the returned info is -1 and true_res is not written
   FgmresResult engine_refine(int kind, const double2* b, double2* x, double rtol, int maxiter,
                              int restart, const void* GpT32, const void* GpT64, double palpha,
-                             double* true_res) {
+                             double* true_res, bool defer = false) {
     ProfScope ps(ctx, kind == 0 ? "engine_stokes" : "engine_theta", 0.0, 1);
     const EngineOps op32 = engine_ops(kind, true, GpT32, palpha);
     const EngineOps op64 = engine_ops(kind, false, GpT64, palpha);
@@ -1240,11 +1263,19 @@ struct Model {
       io.phase_cycles = dEngPhase;
     }
     fgmres_refine_engine(ctx, op32, op64, io, rf);
-    int* res = reinterpret_cast<int*>(hpin);                     // pinned: no staged copies
+    int* res = eng_slot_res(kind);                               // pinned: no staged copies
     long long* cyc = reinterpret_cast<long long*>(hpin + 64);
-    double* relp = reinterpret_cast<double*>(hpin + 512);
+    double* relp = eng_slot_rel(kind);
     SMC_CUDA(cudaMemcpyAsync(res, eio.result, 3 * sizeof(int), cudaMemcpyDeviceToHost, stream));
     SMC_CUDA(cudaMemcpyAsync(relp, dEngRes, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (defer && !phases) {
+      SMC_CUDA(cudaEventRecord(eng_done[kind], stream));
+      eng_pending[kind] = true;
+      eng_pending_restart[kind] = io.restart;
+      FgmresResult fr;
+      fr.info = -1;
+      return fr;
+    }
     if (phases)
       SMC_CUDA(cudaMemcpyAsync(cyc, dEngPhase, ENGINE_PHASES * sizeof(long long),
                                cudaMemcpyDeviceToHost, stream));
@@ -1262,6 +1293,26 @@ struct Model {
     // inner solves plus one FP64 operator application per outer pass
     ps.work = engine_bytes(kind, true, fr.iters, io.restart) +
               res[2] * 2.0 * engine_bytes(kind, true, 1, io.restart);
+    return fr;
+  }
+  // deferred refinement launches: their results, the event after the copies
+  bool eng_pending[2] = {false, false};
+  int eng_pending_restart[2] = {0, 0};
+  cudaEvent_t eng_done[2] = {nullptr, nullptr};
+  // the results of a deferred launch of `kind` (waits for its copies, which a
+  // synchronisation of the stream has normally completed already)
+  FgmresResult engine_result(int kind, double* true_res) {
+    SMC_CUDA(cudaEventSynchronize(eng_done[kind]));
+    eng_pending[kind] = false;
+    const int* res = eng_slot_res(kind);
+    FgmresResult fr;
+    fr.info = res[0];
+    fr.iters = res[1];
+    n_outer += res[2];
+    if (true_res) *true_res = *eng_slot_rel(kind);
+    const int rs = eng_pending_restart[kind];
+    prof.add_work(kind == 0 ? "engine_stokes" : "engine_theta",
+                  engine_bytes(kind, true, fr.iters, rs) + res[2] * 2.0 * engine_bytes(kind, true, 1, rs));
     return fr;
   }
 
@@ -1323,39 +1374,16 @@ struct Model {
     ProfScope ps(ctx, "eta_of");
     synth(th, dV, KFactor(), gr[0], Np, sp[0]);              // theta on 2 Nx points
     eta_law(ctx, gr[0], dz, N, (long long)Np * N, law, dEtaP, dScal, dRed);
-    sync_read(dScal, 6);
-    double tmin = hbuf[0], tmax = hbuf[1];
-    ctr.max_T_excursion = std::max(ctr.max_T_excursion, std::max(std::max(0.0 - tmin, tmax - 1.0), 0.0));
-    ctr.n_T_out_of_range += (long long)hbuf[2];
-    ctr.n_clip_T += (long long)hbuf[3];
-    if (law.w > 0.0) {
-      ctr.n_clip_eta += (long long)hbuf[4];
-      ctr.n_smooth_eta += (long long)hbuf[5];
-    } else if (hbuf[4] > 0.0) {
-      eta_window(ctx, dEtaP, (long long)Np * N, law, 0, dScal + 8, dRed);
-      ctr.n_clip_eta += (long long)hbuf[4];
-    }
+    // the T / eta counters and the hard window of the padded field (applied
+    // iff some point lies outside its dead band), decided on the device
+    eta_stats_apply(ctx, dScal, dEtaP, (long long)Np * N, law, dEtaCtr);
     AnaJob a{dEtaP, sp[1]};
     analysis_x(ctx, &a, 1, Nk, N, Np, dtwNp, 1.0 / Np);
     SynthJob s{sp[1], dEta};
     synth_x(ctx, &s, 1, Nk, N, Nx, dtwNx);
     min_and_drift(ctx, dEta, nullptr, (long long)Nx * N, dScal, dRed);
-    sync_read(dScal, 1);
-    if (!(hbuf[0] > 0.0)) {
-      // positivity guard (coupled_model.py:451-496)
-      eta_window(ctx, dEta, (long long)Nx * N, law, 1, dScal, dRed);
-      sync_read(dScal, 2);
-      double c = hbuf[0];
-      if (law.w > 0.0) {
-        eta_window(ctx, dEta, (long long)Nx * N, law, 0, dScal, dRed);
-        sync_read(dScal, 2);
-        ctr.n_clip_eta_proj += (long long)c;
-        ctr.n_smooth_eta_proj += (long long)hbuf[1];
-      } else if (c > 0) {
-        eta_window(ctx, dEta, (long long)Nx * N, law, 0, dScal, dRed);
-        ctr.n_clip_eta_proj += (long long)c;
-      }
-    }
+    // positivity guard (coupled_model.py:451-496), gated on min(eta) <= 0
+    eta_guard(ctx, dScal, dEta, (long long)Nx * N, law, dEtaCtr, dRed);
   }
 
   // Md (dense blocks, for the Schur assembly) and the pseudo-spectral eta
@@ -1572,9 +1600,10 @@ struct Model {
   // The fast form keeps the blocks while the Galerkin profile stays within
   // 2% (max-norm, relative) of the one they were built from and for at most
   // 16 solves: the blocks only precondition, so the solution is unchanged.
-  std::vector<double> bfbt_prof_h, bfbt_prof_new;
-  int bfbt_age = 1 << 30;
-  long long n_bfbt_builds = 0;
+  // The decision is taken on the device (bfbt_decide) inside a CUDA graph
+  // whose rebuild runs under a conditional node the decision sets: one graph
+  // launch per solve, the host enqueues the solve without waiting for it,
+  // and a skipped rebuild launches none of its kernels.
   void bfbt_build() {
     ProfScope psp(ctx, "bfbt_profile");
     harm_profile_rhs(ctx, dEta, Nx, N, dwq, dBfbtHw);
@@ -1583,32 +1612,69 @@ struct Model {
     zmat_apply(ctx, &j, 1, 1, N, dkx);
     if (fast) kgemv(ctx, dMpInv, dBfbtProfC, dBfbtRhs, 1, N, 1.0);
     else lu_small_solve(ctx, dMpLU, dMpPiv, NN, dBfbtProfC, dBfbtRhs, N, 1, 1.0, 0, nullptr);
-    if (fast) {
-      double* hp = reinterpret_cast<double*>(hpin + 1024);      // pinned
-      SMC_CUDA(cudaMemcpyAsync(hp, dBfbtRhs, N * sizeof(double2), cudaMemcpyDeviceToHost, stream));
-      SMC_CUDA(cudaStreamSynchronize(stream));
-      bfbt_prof_new.assign(hp, hp + 2 * N);
-      bool reuse = !bfbt_prof_h.empty() && bfbt_age < 16;
-      if (reuse) {
-        double mx = 0.0, md = 0.0;
-        for (int q = 0; q < N; ++q) {
-          mx = std::max(mx, std::fabs(bfbt_prof_h[2 * q]));
-          md = std::max(md, std::fabs(bfbt_prof_new[2 * q] - bfbt_prof_h[2 * q]));
-        }
-        reuse = std::isfinite(md) && md <= 0.02 * mx;
-      }
-      if (reuse) { ++bfbt_age; return; }
-      bfbt_prof_h = bfbt_prof_new;
-      bfbt_age = 1;
-    }
-    ++n_bfbt_builds;
     ProfScope ps(ctx, "bfbt_build");
-    build_reduced_lu(dBfbtRhs, dRedLU, dRedPiv);
-    if (fast) {
-      green_from_lu(ctx, dRedLU, dRedPiv, dRedG, N, Nk);
-      transpose_split(ctx, dRedG, dRedGT32, N, N, Nk);
-      transpose_as(ctx, dRedG, dRedGT64, N, N, Nk);
+    if (!fast) {
+      build_reduced_lu(dBfbtRhs, dRedLU, dRedPiv);
+      return;
     }
+    if (!bfbt_exec) bfbt_graph_make();
+    SMC_CUDA(cudaGraphLaunch(bfbt_exec, stream));
+    ctx.count();
+  }
+  // the fast form's blocks from dBfbtRhs: reduced operators, their LU, the
+  // explicit inverses and the engine's transposed copies
+  void bfbt_rebuild_launches() {
+    build_reduced_blocks(dBfbtRhs);
+    if (lu_green_batched(ctx, dPcm, dRedLU, dRedPiv, dRedG, dRedGT64, dRedGT32, N, Nk)) return;
+    SMC_CUDA(cudaMemcpyAsync(dRedLU, dPcm, sizeof(double) * Nk * NN, cudaMemcpyDeviceToDevice, stream));
+    lu_small_batched(ctx, dRedLU, dRedPiv, nullptr, N, Nk);
+    green_from_lu(ctx, dRedLU, dRedPiv, dRedG, N, Nk);
+    transpose_split(ctx, dRedG, dRedGT32, N, N, Nk);
+    transpose_as(ctx, dRedG, dRedGT64, N, N, Nk);
+  }
+  cudaGraph_t bfbt_graph = nullptr;
+  cudaGraphExec_t bfbt_exec = nullptr;
+  // records f's launches on the stream into g (the capture ends on an
+  // exception too, so the stream is usable afterwards)
+  template <class F>
+  void capture_into(cudaGraph_t g, F&& f) {
+    SMC_CUDA(cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal));
+    try {
+      f();
+    } catch (...) {
+      cudaGraph_t dummy = nullptr;
+      cudaStreamEndCapture(stream, &dummy);
+      throw;
+    }
+    cudaGraph_t out = nullptr;
+    SMC_CUDA(cudaStreamEndCapture(stream, &out));
+  }
+  // graph: [bfbt_decide] -> IF (cond) { bfbt_rebuild_launches }
+  void bfbt_graph_make() {
+    SMC_CUDA(cudaGraphCreate(&bfbt_graph, 0));
+    cudaGraphConditionalHandle cond;
+    SMC_CUDA(cudaGraphConditionalHandleCreate(&cond, bfbt_graph, 0, cudaGraphCondAssignDefault));
+    capture_into(bfbt_graph, [&] { bfbt_decide(ctx, dBfbtRhs, dBfbtHeld, N, 16, 0.02, dBfbtHold, cond); });
+    cudaGraphNode_t decide = nullptr;
+    size_t nn = 1;
+    SMC_CUDA(cudaGraphGetNodes(bfbt_graph, &decide, &nn));
+    if (nn != 1) throw std::runtime_error("bfbt graph: expected one decision node");
+    // zeroed storage: the struct's union has no default constructor
+    alignas(cudaGraphNodeParams) unsigned char pbuf[sizeof(cudaGraphNodeParams)] = {};
+    cudaGraphNodeParams& p = *reinterpret_cast<cudaGraphNodeParams*>(pbuf);
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = cond;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    SMC_CUDA(cudaGraphAddNode(&node, bfbt_graph, &decide, nullptr, 1, &p));
+    capture_into(p.conditional.phGraph_out[0], [&] { bfbt_rebuild_launches(); });
+    SMC_CUDA(cudaGraphInstantiate(&bfbt_exec, bfbt_graph, 0));
+  }
+  // the next build runs whatever the profile (held profile invalid)
+  void bfbt_invalidate() {
+    if (dBfbtHold) SMC_CUDA(cudaMemsetAsync(&dBfbtHold->valid, 0, sizeof(int), stream));
   }
   void to_complex(const double* in, double2* out, int count);
 
@@ -1651,6 +1717,16 @@ struct Model {
       if (fp32_now) {
         if (use_engine) {
           stokes_guess(x);
+          if (defer_stokes && !batch_mode && !(eng_phase && prof.enabled)) {
+            // the host goes on enqueueing (velocity, CFL reduction) while
+            // the engine runs; stokes_finish() completes this solve after
+            // the CFL synchronisation
+            engine_refine(0, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, cfg.stokes_restart,
+                          dRedGT32, dRedGT64, 1.0, nullptr, true);
+            stokes_pend_th = th;
+            stokes_pend_x = x;
+            return;
+          }
           fr = engine_refine(0, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, cfg.stokes_restart,
                              dRedGT32, dRedGT64, 1.0, &res);
         } else {
@@ -1660,22 +1736,7 @@ struct Model {
           fr = fgmres_refined(A64, inner, dSb, x, cfg.stokes_rtol, cfg.stokes_maxiter, inner_floor[0],
                               &res);
         }
-        if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
-          // the FP32 operator cannot resolve this system (viscosity contrast
-          // too large for its rounding): solve it in FP64 and stay in FP64
-          // for the next solves
-          ctr.n_bfbt_iters += fr.iters;
-          ++n_fp64_fallback;
-          stokes_fp64_solves = 16;
-          if (use_engine)
-            fr = engine_solve(0, false, dSb, x, cfg.stokes_rtol, cfg.stokes_restart,
-                              cfg.stokes_maxiter, dRedGT64, 1.0);
-          else
-            fr = fgmres(A64, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
-          schur_matvec_fast(x, dSAx, false);
-          vec_axpby(ctx, dSAx, make_double2(1.0, 0.0), dSb, make_double2(-1.0, 0.0), n);
-          res = norm(dSAx) / std::max(norm(dSb), 1e-300);
-        }
+        stokes_fp64_fallback(fr, res, x);
       } else {
         if (use_engine)
           fr = engine_solve(0, false, dSb, x, cfg.stokes_rtol, cfg.stokes_restart,
@@ -1690,6 +1751,34 @@ struct Model {
       fr = fgmres(A, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
       res = schur_true_res(dSb, x);
     }
+    bfbt_finish(th, x, fr, res);
+  }
+
+  // fast form: the FP32-refined solve did not reach the tolerance (viscosity
+  // contrast too large for the FP32 operator's rounding): solve the system in
+  // FP64 and stay in FP64 for the next 16 solves.  True when it ran.
+  bool stokes_fp64_fallback(FgmresResult& fr, double& res, double2* x) {
+    if (!(fr.info != 0 && !(res <= cfg.stokes_rtol))) return false;
+    ctr.n_bfbt_iters += fr.iters;
+    ++n_fp64_fallback;
+    stokes_fp64_solves = 16;
+    if (use_engine) {
+      fr = engine_solve(0, false, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter,
+                        dRedGT64, 1.0);
+    } else {
+      Op A64 = [&](const double2* v, double2* o) { schur_matvec_fast(v, o, false); };
+      Op M = [&](const double2* r, double2* z) { kgemv(ctx, dRedG, r, z, Nk, N, 1.0); };
+      fr = fgmres(A64, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, cfg.stokes_maxiter);
+    }
+    schur_matvec_fast(x, dSAx, false);
+    vec_axpby(ctx, dSAx, make_double2(1.0, 0.0), dSb, make_double2(-1.0, 0.0), n);
+    res = norm(dSAx) / std::max(norm(dSb), 1e-300);
+    return true;
+  }
+
+  // counters of a BFBT solve and, when it failed, the rescue chain.  True
+  // when a rescue changed x.
+  bool bfbt_finish(const double2* th, double2* x, const FgmresResult& fr, double res) {
     ctr.n_bfbt_solves++;
     ctr.n_bfbt_iters += fr.iters;
     ctr.last_bfbt_true_res = res;
@@ -1699,8 +1788,7 @@ struct Model {
       // BFBT blocks for the current eta and solve in FP64 with four times the
       // iteration budget; counted as a weak rescue
       ctr.n_bfbt_rescue++;
-      bfbt_age = 1 << 30;
-      bfbt_prof_h.clear();
+      bfbt_invalidate();
       bfbt_build();
       Op A64 = [&](const double2* v, double2* o) {
         if (fast) schur_matvec_fast(v, o, false);
@@ -1716,7 +1804,9 @@ struct Model {
       ctr.n_bfbt_rescue_weak++;
       res = schur_true_res(dSb, x);
       ctr.last_bfbt_true_res = res;
-    } else if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
+      return true;
+    }
+    if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
       // rescue chain (coupled_model.py:613-654)
       ctr.n_bfbt_rescue++;
       if (fast) legacy_after_rescue = cfg.lag;
@@ -1737,7 +1827,109 @@ struct Model {
           ctr.n_bfbt_rescue_direct++;
         }
       }
+      return true;
     }
+    return false;
+  }
+
+  // deferred solves.  A Stokes solve launched inside cfl_dt (defer_stokes)
+  // is completed after the CFL synchronisation; a temperature solve launched
+  // inside a march (defer_theta) at the next synchronisation (the next dt
+  // selection's memo test) or when any other entry point is called (settle)
+  bool defer_stokes = false, defer_theta = false;
+  const double2* stokes_pend_th = nullptr;
+  double2* stokes_pend_x = nullptr;
+  double2* theta_pend_out = nullptr;
+  const double* theta_pend_gi = nullptr;
+  bool theta_pend_sym = false;
+  struct FlagScope {
+    bool& f;
+    explicit FlagScope(bool& f_, bool on = true) : f(f_) { f = on; }
+    ~FlagScope() { f = false; }
+  };
+
+  // true when x changed after the deferred launch (an FP64 fallback or a
+  // rescue): what was computed from it is stale
+  bool stokes_finish() {
+    double res = 0.0;
+    FgmresResult fr = engine_result(0, &res);
+    double2* x = stokes_pend_x;
+    const double2* th = stokes_pend_th;
+    stokes_pend_x = nullptr;
+    stokes_pend_th = nullptr;
+    bool changed = stokes_fp64_fallback(fr, res, x);
+    changed = bfbt_finish(th, x, fr, res) || changed;
+    return changed;
+  }
+
+  // counters of a temperature solve
+  void theta_account(const FgmresResult& fr, double tr) {
+    ctr.theta_last_res = tr;
+    ctr.theta_last_iters = fr.iters;
+    ctr.n_theta_iters += fr.iters;
+    if (fr.info != 0) ctr.n_theta_nonconv++;
+  }
+  // non-finite values in the FP32 inner solves (info 3): the temperature
+  // solve redone in FP64 with the step's operator and preconditioner
+  void theta_fp64_redo(FgmresResult& fr, double& tr, const double* Gi) {
+    ++n_fp64_fallback;
+    Op A64 = [&](const double2* v, double2* o) { theta_matvec_fast(v, o, false); };
+    Op M = [&](const double2* r, double2* z) { kgemv(ctx, Gi, r, z, Nk, N, -1.0); };
+    fr = fgmres(A64, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
+    theta_matvec_fast(dRhs, sp[13], false);
+    vec_axpby(ctx, sp[13], make_double2(1.0, 0.0), dKb, make_double2(-1.0, 0.0), n);
+    tr = norm(sp[13]) / std::max(norm(dKb), 1e-300);
+  }
+  // true when the step's output changed after the deferred launch (the
+  // FP64 redo); nothing between the launch and here touches the operator
+  // state of that step (frozen velocity, BDF2 coefficients, rhs)
+  bool theta_finish() {
+    double tr = 0.0;
+    FgmresResult fr = engine_result(1, &tr);
+    double2* out = theta_pend_out;
+    theta_pend_out = nullptr;
+    bool redo = false;
+    if (fr.info == 3) {
+      theta_fp64_redo(fr, tr, theta_pend_gi);
+      if (theta_pend_sym) project(dRhs, out);
+      else vec_copy(ctx, out, dRhs, n);
+      redo = true;
+    }
+    theta_account(fr, tr);
+    return redo;
+  }
+  // completes deferred work before an entry point other than the march's
+  void settle() {
+    mpf.valid = false;
+    if (stokes_pend_x) {           // left by an exception inside cfl_dt
+      eng_pending[0] = false;
+      stokes_pend_x = nullptr;
+    }
+    if (theta_pend_out) theta_finish();
+  }
+  // the step's memo test, prefetched by cfl_dt inside a march: the values of
+  // memo_compare for the step's projected temperature
+  bool want_memo_prefetch = false;
+  struct MemoPrefetch {
+    bool valid = false;
+    const double2* src = nullptr;
+    double v[3] = {0, 0, 0};
+  } mpf;
+  const double* memo_pre = nullptr;
+  bool uses_memo() const { return cfg.model != SMC_MODEL_CONST && cfg.model != SMC_MODEL_ETA_Z; }
+  // enqueues what step_theta(th) computes before its memo test: the mirror
+  // projections (dTh1, dTh2), V th2 (sp[3]) and memo_compare into dScal[16..18]
+  bool memo_prefetch_enqueue(const double2* th) {
+    if (!uses_memo() || !memo_valid) return false;
+    const double2* th2 = th;
+    if (cfg.symmetrize != 0) {
+      project(th, dTh1);
+      project(dTh1, dTh2);
+      th2 = dTh2;
+    }
+    zop(dV, 0, th2, sp[3]);
+    memo_compare(ctx, th2, dMemoThat, sp[3], dMemoX, n, dScal + 16, dRed);
+    return true;
   }
 
   void stokes_coupled(const double2* th, double2* psi, double2* om) {
@@ -1747,6 +1939,9 @@ struct Model {
     eta_operator();
     if (cfg.precond == SMC_PRECOND_BFBT || fast) bfbt_solve(th, dSx);
     else legacy_solve(th, dSx);
+    stokes_coupled_tail(psi, om);
+  }
+  void stokes_coupled_tail(double2* psi, double2* om) {
     zop(green_coupled(), NN, dSx, psi);
     // omega = -v (TALA: -v / rho_bar column by column, stokes_tala.py:327-340)
     if (tala) scale_cols(ctx, dSx, dRhoInv, -1.0, om, Nk, N);
@@ -1757,13 +1952,28 @@ struct Model {
   // memoised Stokes solve of the coupled model (coupled_model.py:725-765)
   void stokes_memo(const double2* th, double2* psi, double2* om) {
     ProfScope psm(ctx, "stokes_memo_check");
-    zop(dV, 0, th, sp[3]);
+    const double* pre = memo_pre;          // the test prefetched with the CFL reduction
+    memo_pre = nullptr;
+    if (!pre) zop(dV, 0, th, sp[3]);
     if (memo_valid) {
-      memo_compare(ctx, th, dMemoThat, sp[3], dMemoX, n, dScal, dRed);
-      sync_read(dScal, 3);
-      bool eq = hbuf[0] != 0.0;
-      double den = std::max(hbuf[2], 1e-300);
-      if (eq || hbuf[1] <= 1e-12 * den) {
+      double v[3];
+      if (pre) {
+        for (int q = 0; q < 3; ++q) v[q] = pre[q];
+      } else {
+        memo_compare(ctx, th, dMemoThat, sp[3], dMemoX, n, dScal, dRed);
+        sync_read(dScal, 3);
+        for (int q = 0; q < 3; ++q) v[q] = hbuf[q];
+        if (theta_pend_out && theta_finish()) {
+          // the temperature step that produced th was redone: test again
+          zop(dV, 0, th, sp[3]);
+          memo_compare(ctx, th, dMemoThat, sp[3], dMemoX, n, dScal, dRed);
+          sync_read(dScal, 3);
+          for (int q = 0; q < 3; ++q) v[q] = hbuf[q];
+        }
+      }
+      bool eq = v[0] != 0.0;
+      double den = std::max(v[2], 1e-300);
+      if (eq || v[1] <= 1e-12 * den) {
         if (!eq) ctr.n_memo_hits++;
         vec_copy(ctx, psi, dMemoPsi, n);
         vec_copy(ctx, om, dMemoOm, n);
@@ -1793,12 +2003,33 @@ struct Model {
   }
 
   double cfl_dt(const double2* th, double safety, double dtmax, double dtmin) {
-    stokes(th, dPsi, dOm);
+    mpf.valid = false;
+    if (theta_pend_out && !uses_memo()) settle();
+    {
+      FlagScope fs(defer_stokes);
+      stokes(th, dPsi, dOm);
+    }
     ProfScope ps(ctx, "cfl_velocity");
     velocity(dPsi, gr[0], gr[1]);
     reduce_maxabs2(ctx, gr[0], gr[1], (long long)Nx * N, dScal, dRed);
-    sync_read(dScal, 1);
+    const bool pre = want_memo_prefetch && memo_prefetch_enqueue(th);
+    sync_read(dScal, pre ? 19 : 1);
     double vmax = hbuf[0];
+    if (pre) {
+      mpf.valid = true;
+      mpf.src = th;
+      for (int q = 0; q < 3; ++q) mpf.v[q] = hbuf[16 + q];
+    }
+    if (stokes_pend_x && stokes_finish()) {
+      // the solve's x changed after its launch: psi, omega and the velocity again
+      stokes_coupled_tail(dMemoPsi, dMemoOm);
+      vec_copy(ctx, dPsi, dMemoPsi, n);
+      vec_copy(ctx, dOm, dMemoOm, n);
+      velocity(dPsi, gr[0], gr[1]);
+      reduce_maxabs2(ctx, gr[0], gr[1], (long long)Nx * N, dScal, dRed);
+      sync_read(dScal, 1);
+      vmax = hbuf[0];
+    }
     if (!(vmax >= 1e-12)) vmax = (vmax != vmax) ? vmax : 1e-12;
     double dt = safety * std::min(cfg.Lx / Nx, dzmin) / vmax;
     return std::min(std::max(dt, dtmin), dtmax);
@@ -1897,12 +2128,26 @@ struct Model {
   }
 
   void step_theta(const double2* th_in, double2* out, double dt) {
+    // a deferred solve of the step before (smc_march: no dt selection in
+    // between) is completed before th_in is read
+    if (theta_pend_out) theta_finish();
     const bool sym = cfg.symmetrize != 0;
+    // the projections and the memo test prefetched by cfl_dt for this state
+    const bool pre = mpf.valid && mpf.src == th_in;
+    mpf.valid = false;
     const double2* th1 = th_in;
-    if (sym) { project(th_in, dTh1); th1 = dTh1; }
-    const double2* th2 = th1;
-    if (sym) { project(th1, dTh2); th2 = dTh2; }
+    const double2* th2 = th_in;
+    if (sym) {
+      if (!pre) {
+        project(th_in, dTh1);
+        project(dTh1, dTh2);
+      }
+      th1 = dTh1;
+      th2 = dTh2;
+    }
+    if (pre) memo_pre = mpf.v;
     stokes(th2, dPsi, dOm);
+    memo_pre = nullptr;
     vec_copy(ctx, dPsiN, dPsi, n);
     const double2* ps = dPsi;
     if (have_prev) { extrapolate(ctx, dPsi, dPsiPrev, dPsiStar, n); ps = dPsiStar; }
@@ -1945,6 +2190,7 @@ struct Model {
       }
     };
     FgmresResult fr;
+    bool deferred = false;
     if (fast) {
       to_float(ctx, gr[0], dUx32, (long long)Np * N);
       to_float(ctx, gr[1], dUz32, (long long)Np * N);
@@ -1958,8 +2204,17 @@ struct Model {
             const double r = dt / dt_prev;
             vec_axpby(ctx, dRhs, make_double2(-r, 0.0), dPrev, make_double2(1.0 + r, 0.0), n);
           }
+          // inside a march the result is read at the next dt selection's
+          // memo test: the host enqueues the rest of the step meanwhile
+          deferred = defer_theta && uses_memo() && memo_valid && !batch_mode &&
+                     !(eng_phase && prof.enabled);
           fr = engine_refine(1, dKb, dRhs, cfg.theta_rtol, cfg.theta_maxiter, cfg.theta_restart,
-                             Lp->GinvT32, Lp->GinvT64, -1.0, &tr);
+                             Lp->GinvT32, Lp->GinvT64, -1.0, &tr, deferred);
+          if (deferred) {
+            theta_pend_out = out;
+            theta_pend_gi = Gi;
+            theta_pend_sym = sym;
+          }
         } else {
           InnerSolve inner = [&](const double2* r, double2* e, double tol, int mi) {
             return fgmres(A32, M, r, e, tol, cfg.theta_restart, mi);
@@ -1967,14 +2222,7 @@ struct Model {
           fr = fgmres_refined(A64, inner, dKb, dRhs, cfg.theta_rtol, cfg.theta_maxiter, inner_floor[1],
                               &tr);
         }
-        if (fr.info == 3) {
-          // non-finite values in the FP32 inner solves: redo the solve in FP64
-          ++n_fp64_fallback;
-          fr = fgmres(A64, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
-          theta_matvec_fast(dRhs, sp[13], false);
-          vec_axpby(ctx, sp[13], make_double2(1.0, 0.0), dKb, make_double2(-1.0, 0.0), n);
-          tr = norm(sp[13]) / std::max(norm(dKb), 1e-300);
-        }
+        if (!deferred && fr.info == 3) theta_fp64_redo(fr, tr, Gi);
       } else {
         if (use_engine)
           fr = engine_solve(1, false, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart,
@@ -1985,19 +2233,16 @@ struct Model {
         vec_axpby(ctx, sp[13], make_double2(1.0, 0.0), dKb, make_double2(-1.0, 0.0), n);
         tr = norm(sp[13]) / std::max(norm(dKb), 1e-300);
       }
-      ctr.theta_last_res = tr;
+      if (!deferred) theta_account(fr, tr);
     } else {
       fr = fgmres(A, M, dKb, dRhs, cfg.theta_rtol, cfg.theta_restart, cfg.theta_maxiter);
       // true relative residual of the accepted solution (implicit_theta.py:510-516)
       theta_matvec(dRhs, sp[13]);
       vec_axpby(ctx, sp[13], make_double2(1.0, 0.0), dKb, make_double2(-1.0, 0.0), n);
       double bn = std::max(norm(dKb), 1e-300);
-      ctr.theta_last_res = norm(sp[13]) / bn;
+      theta_account(fr, norm(sp[13]) / bn);
     }
-    ctr.theta_last_iters = fr.iters;
-    ctr.n_theta_iters += fr.iters;
     ctr.n_theta_solves++;
-    if (fr.info != 0) ctr.n_theta_nonconv++;
     ctr.n_steps++;
     if (sym) project(dRhs, out);
     else vec_copy(ctx, out, dRhs, n);
@@ -2114,6 +2359,10 @@ struct Model {
     if (hpin) cudaFreeHost(hpin);
     if (hBatchRes) cudaFreeHost((void*)hBatchRes);
     if (batch_ready) cudaEventDestroy(batch_ready);
+    for (auto e : eng_done)
+      if (e) cudaEventDestroy(e);
+    if (bfbt_exec) cudaGraphExecDestroy(bfbt_exec);
+    if (bfbt_graph) cudaGraphDestroy(bfbt_graph);
   }
 };
 
@@ -2242,23 +2491,32 @@ int smc_destroy(smc_handle* h) {
   return 0;
 }
 
-#define SMC_GUARD(h, ...)                                    \
+// every entry point but smc_advance first completes the deferred work of
+// the handle's last march (settle)
+#define SMC_GUARD_IMPL(h, settle_first, ...)                 \
   try {                                                      \
     if (!(h)) throw std::runtime_error("null handle");       \
     SMC_CUDA(cudaSetDevice((h)->m.device));                  \
+    if (settle_first) (h)->m.settle();                       \
     __VA_ARGS__;                                             \
     return 0;                                                \
   } catch (const std::exception& e) {                        \
     return fail(e);                                          \
   }
+#define SMC_GUARD(h, ...) SMC_GUARD_IMPL(h, true, __VA_ARGS__)
 
 int smc_step(smc_handle* h, const double* in, double* out, int mem, double dt) {
   SMC_GUARD(h, {
     Model& m = h->m;
     smc::BatchScope bs(m.device, m.batch_mode);
     copy_in(m, m.dIn, in, mem, m.n);
-    m.step(m.dIn, m.dOut, dt);
+    {
+      // the temperature solve's result is read with the copy of the output
+      Model::FlagScope df(m.defer_theta);
+      m.step(m.dIn, m.dOut, dt);
+    }
     copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
+    if (m.theta_pend_out && m.theta_finish()) copy_out(m, out, m.dOut, mem, m.n * sizeof(double2));
     m.check_tc();
   })
 }
@@ -2294,12 +2552,19 @@ int smc_march_adaptive(smc_handle* h, const double* in, double* out, int mem, do
     double t = 0.0, dt = NAN;
     long long steps = 0;
     while (t < tstop && (max_steps <= 0 || steps < max_steps)) {
-      dt = m.production_dt(cur, safety, dtmax);
-      m.step(cur, nxt, dt);
+      {
+        Model::FlagScope pf(m.want_memo_prefetch);
+        dt = m.production_dt(cur, safety, dtmax);
+      }
+      {
+        Model::FlagScope df(m.defer_theta);
+        m.step(cur, nxt, dt);
+      }
       std::swap(cur, nxt);
       t += dt;
       ++steps;
     }
+    m.settle();
     copy_out(m, out, cur, mem, m.n * sizeof(double2));
     m.check_tc();
     if (info) { info->steps = steps; info->t = t; info->dt = dt; }
@@ -2333,12 +2598,17 @@ void advance_resident(Model& m, double tstop, long long max_steps, double safety
     double dt = NAN;
     long long steps = 0;
     while (m.t_resident < tstop && (max_steps <= 0 || steps < max_steps)) {
+      // the step's projections and memo test travel with the CFL
+      // reduction, and the temperature solve's result is read at the next
+      // memo test: two synchronisations per step
       {
         smc::ProfScope ps(m.ctx, "step.dt_select");
+        Model::FlagScope pf(m.want_memo_prefetch);
         dt = m.production_dt(cur, safety, dtmax);
       }
       {
         smc::ProfScope ps(m.ctx, "step.advance");
+        Model::FlagScope df(m.defer_theta);
         m.step(cur, nxt, dt);
       }
       std::swap(cur, nxt);
@@ -2352,7 +2622,7 @@ void advance_resident(Model& m, double tstop, long long max_steps, double safety
 
 int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety, double dtmax,
                 smc_march_info* info) {
-  SMC_GUARD(h, {
+  SMC_GUARD_IMPL(h, false, {
     Model& m = h->m;
     smc::BatchScope bs(m.device, m.batch_mode);
     smc::advance_resident(m, tstop, max_steps, safety, dtmax, info);
@@ -2394,9 +2664,11 @@ int smc_march(smc_handle* h, const double* in, double* out, int mem, double dt, 
     double2* cur = m.dS0;
     double2* nxt = m.dS1;
     for (long long s = 0; s < nsteps; ++s) {
+      Model::FlagScope df(m.defer_theta);     // read at the next step's memo test
       m.step(cur, nxt, dt);
       std::swap(cur, nxt);
     }
+    m.settle();
     copy_out(m, out, cur, mem, m.n * sizeof(double2));
     m.check_tc();
   })
@@ -2602,8 +2874,20 @@ int smc_set_history(smc_handle* h, const double* prev, const double* psi_prev, i
 
 int smc_counters_get(smc_handle* h, smc_counters* out) {
   SMC_GUARD(h, {
-    *out = h->m.ctr;
-    out->n_kernel_launches = h->m.nlaunch;
+    Model& m = h->m;
+    *out = m.ctr;
+    out->n_kernel_launches = m.nlaunch;
+    // the viscosity pipeline's counters accumulate on the device
+    smc::EtaCtrDev* d = reinterpret_cast<smc::EtaCtrDev*>(m.hbuf);
+    SMC_CUDA(cudaMemcpyAsync(d, m.dEtaCtr, sizeof(smc::EtaCtrDev), cudaMemcpyDeviceToHost, m.stream));
+    SMC_CUDA(cudaStreamSynchronize(m.stream));
+    out->n_T_out_of_range += d->n_T_out_of_range;
+    out->n_clip_T += d->n_clip_T;
+    out->n_clip_eta += d->n_clip_eta;
+    out->n_smooth_eta += d->n_smooth_eta;
+    out->n_clip_eta_proj += d->n_clip_eta_proj;
+    out->n_smooth_eta_proj += d->n_smooth_eta_proj;
+    out->max_T_excursion = std::max(out->max_T_excursion, d->max_T_excursion);
   })
 }
 
@@ -2720,6 +3004,7 @@ int smc_march_many(smc_handle* const* hs, int nruns, long long nsteps, double sa
           while (r.status != SMC_RUN_NONFINITE && r.steps < nsteps) {
             const long long k = std::min<long long>(check_every, nsteps - r.steps);
             advance_resident(m, INFINITY, k, safety, dtmax, &info);
+            m.settle();
             m.check_tc();
             r.steps += info.steps;
             r.t = info.t;

@@ -357,6 +357,21 @@ void eta_law(const Ctx& c, const double* th, const double* z, int N, long long n
   SMC_LAUNCH_CHECK(c);
 }
 
+// the window applied to one value: the smooth C^2 clamp in ln eta (counting
+// the values strictly inside a band) or the hard clamp np.clip(eta, lo, hi)
+__device__ __forceinline__ double eta_window_value(double e, const EtaLaw& law, double& c_band) {
+  if (law.w > 0.0) {
+    double y = log(e);
+    if ((y > law.ylo && y < law.ylo + law.w) || (y > law.yhi - law.w && y < law.yhi)) c_band += 1.0;
+    double t1 = fmin(fmax((y - law.ylo) / law.w, 0.0), 1.0);
+    double Y = law.ylo + (y - law.ylo) * (t1 * t1 * t1 * (t1 * (6.0 * t1 - 15.0) + 10.0));
+    double t2 = fmin(fmax((law.yhi - Y) / law.w, 0.0), 1.0);
+    double yo = law.yhi - (law.yhi - Y) * (t2 * t2 * t2 * (t2 * (6.0 * t2 - 15.0) + 10.0));
+    return exp(yo);
+  }
+  return fmin(fmax(e, law.lo), law.hi);
+}
+
 // the window applied to an existing field (hard clamp, or smooth clamp with
 // counting) -- the padded-law clamp and the post-truncation guard
 __global__ void smc_eta_window_kernel(double* __restrict__ eta, long long npts, EtaLaw law,
@@ -367,17 +382,7 @@ __global__ void smc_eta_window_kernel(double* __restrict__ eta, long long npts, 
     double e = eta[idx];
     if (e < law.lo_eff || e > law.hi_eff) c_clip += 1.0;
     if (count_only) continue;
-    if (law.w > 0.0) {
-      double y = log(e);
-      if ((y > law.ylo && y < law.ylo + law.w) || (y > law.yhi - law.w && y < law.yhi)) c_band += 1.0;
-      double t1 = fmin(fmax((y - law.ylo) / law.w, 0.0), 1.0);
-      double Y = law.ylo + (y - law.ylo) * (t1 * t1 * t1 * (t1 * (6.0 * t1 - 15.0) + 10.0));
-      double t2 = fmin(fmax((law.yhi - Y) / law.w, 0.0), 1.0);
-      double yo = law.yhi - (law.yhi - Y) * (t2 * t2 * t2 * (t2 * (6.0 * t2 - 15.0) + 10.0));
-      eta[idx] = exp(yo);
-    } else {
-      eta[idx] = fmin(fmax(e, law.lo), law.hi);    // np.clip(eta, lo, hi)
-    }
+    eta[idx] = eta_window_value(e, law, c_band);
   }
   for (int o = 16; o > 0; o >>= 1) {
     c_clip += __shfl_xor_sync(0xffffffffu, c_clip, o);
@@ -476,6 +481,150 @@ void min_and_drift(const Ctx& c, const double* eta, const double* lag, long long
   smc_min_drift_kernel<<<nb, 256, 0, c.s>>>(eta, lag, n, scratch);
   SMC_LAUNCH_CHECK(c);
   smc_min_drift_final_kernel<<<1, 32, 0, c.s>>>(scratch, nb, dst);
+  SMC_LAUNCH_CHECK(c);
+}
+
+// ------------------------------------------- the eta counters on the device
+// std::max(a, b) of the host: b only when a < b (a NaN b is never taken)
+__device__ __forceinline__ double host_max(double a, double b) { return (a < b) ? b : a; }
+
+// block sum of one value per thread (256 threads); thread 0 returns it
+__device__ __forceinline__ double block_sum256(double v, double* ws) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += ws[q];
+  return s;
+}
+
+__global__ void smc_eta_stats_apply_kernel(const double* __restrict__ st, double* __restrict__ eta,
+                                           long long npts, EtaLaw law, EtaCtrDev* __restrict__ ctr) {
+  const double clip = st[4];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const double tmin = st[0], tmax = st[1];
+    ctr->max_T_excursion = host_max(ctr->max_T_excursion,
+                                    host_max(host_max(0.0 - tmin, tmax - 1.0), 0.0));
+    ctr->n_T_out_of_range += (long long)st[2];
+    ctr->n_clip_T += (long long)st[3];
+    if (law.w > 0.0) {
+      ctr->n_clip_eta += (long long)clip;
+      ctr->n_smooth_eta += (long long)st[5];
+    } else if (clip > 0.0) {
+      ctr->n_clip_eta += (long long)clip;
+    }
+  }
+  if (law.w > 0.0 || !(clip > 0.0)) return;     // smooth: already applied by the law
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < npts;
+       idx += (long long)gridDim.x * blockDim.x)
+    eta[idx] = fmin(fmax(eta[idx], law.lo), law.hi);
+}
+
+void eta_stats_apply(const Ctx& c, const double* stats, double* eta, long long npts,
+                     const EtaLaw& law, EtaCtrDev* ctr) {
+  int nb = (int)std::min<long long>(120, (npts + 255) / 256);
+  if (nb < 1) nb = 1;
+  smc_eta_stats_apply_kernel<<<nb, 256, 0, c.s>>>(stats, eta, npts, law, ctr);
+  SMC_LAUNCH_CHECK(c);
+}
+
+// guard, pass 1: per-CTA counts of the points outside the dead-band window
+__global__ void smc_eta_guard_count_kernel(const double* __restrict__ mn, const double* __restrict__ eta,
+                                           long long npts, EtaLaw law, double* __restrict__ part) {
+  if (mn[0] > 0.0) return;
+  __shared__ double ws[8];
+  double cnt = 0.0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < npts;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const double e = eta[idx];
+    if (e < law.lo_eff || e > law.hi_eff) cnt += 1.0;
+  }
+  cnt = block_sum256(cnt, ws);
+  if (threadIdx.x == 0) part[blockIdx.x] = cnt;
+}
+
+// guard, pass 2: every CTA sums the pass-1 counts (integers: exact in any
+// order), CTA 0 adds them to the counters, and the window is applied when it
+// is smooth or some point lies outside the dead band
+__global__ void smc_eta_guard_apply_kernel(const double* __restrict__ mn, double* __restrict__ eta,
+                                           long long npts, EtaLaw law, const double* __restrict__ part,
+                                           int np, EtaCtrDev* __restrict__ ctr) {
+  if (mn[0] > 0.0) return;
+  __shared__ double ws[8];
+  __shared__ double s_c;
+  if (threadIdx.x < 32) {
+    double c = 0.0;
+    for (int b = threadIdx.x; b < np; b += 32) c += part[b];
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (threadIdx.x == 0) s_c = c;
+  }
+  __syncthreads();
+  const double c = s_c;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctr->n_clip_eta_proj += (long long)c;
+  if (!(law.w > 0.0) && !(c > 0.0)) return;
+  double band = 0.0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < npts;
+       idx += (long long)gridDim.x * blockDim.x)
+    eta[idx] = eta_window_value(eta[idx], law, band);
+  if (!(law.w > 0.0)) return;
+  band = block_sum256(band, ws);
+  if (threadIdx.x == 0 && band > 0.0)
+    atomicAdd(reinterpret_cast<unsigned long long*>(&ctr->n_smooth_eta_proj),
+              (unsigned long long)(long long)band);
+}
+
+void eta_guard(const Ctx& c, const double* mn, double* eta, long long npts, const EtaLaw& law,
+               EtaCtrDev* ctr, double* scratch) {
+  int nb = (int)std::min<long long>(120, (npts + 255) / 256);
+  if (nb < 1) nb = 1;
+  smc_eta_guard_count_kernel<<<nb, 256, 0, c.s>>>(mn, eta, npts, law, scratch);
+  SMC_LAUNCH_CHECK(c);
+  smc_eta_guard_apply_kernel<<<nb, 256, 0, c.s>>>(mn, eta, npts, law, scratch, nb, ctr);
+  SMC_LAUNCH_CHECK(c);
+}
+
+// ------------------------------------------------ BFBT block reuse decision
+__global__ void smc_bfbt_decide_kernel(const double2* __restrict__ prof, double2* __restrict__ held,
+                                       int N, int max_age, double rel, BfbtHold* __restrict__ h,
+                                       cudaGraphConditionalHandle cond) {
+  __shared__ double wmx[8], wmd[8];
+  __shared__ int s_reuse;
+  const int valid = h->valid, age = h->age;
+  if (valid && age < max_age) {
+    double mx = 0.0, md = 0.0;       // fmax drops NaN operands, as host_max does
+    for (int q = threadIdx.x; q < N; q += blockDim.x) {
+      const double hq = held[q].x;
+      mx = fmax(mx, fabs(hq));
+      md = fmax(md, fabs(prof[q].x - hq));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+    }
+    if ((threadIdx.x & 31) == 0) { wmx[threadIdx.x >> 5] = mx; wmd[threadIdx.x >> 5] = md; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { mx = fmax(mx, wmx[q]); md = fmax(md, wmd[q]); }
+      s_reuse = isfinite(md) && md <= rel * mx;
+    }
+  } else if (threadIdx.x == 0) {
+    s_reuse = 0;
+  }
+  __syncthreads();
+  const int reuse = s_reuse;
+  if (!reuse)
+    for (int q = threadIdx.x; q < N; q += blockDim.x) held[q] = prof[q];
+  if (threadIdx.x == 0) {
+    h->valid = 1;
+    h->age = reuse ? age + 1 : 1;
+    cudaGraphSetConditional(cond, reuse ? 0u : 1u);
+  }
+}
+
+void bfbt_decide(const Ctx& c, const double2* prof, double2* held, int N, int max_age, double rel,
+                 BfbtHold* h, cudaGraphConditionalHandle cond) {
+  smc_bfbt_decide_kernel<<<1, 256, 0, c.s>>>(prof, held, N, max_age, rel, h, cond);
   SMC_LAUNCH_CHECK(c);
 }
 

@@ -41,4 +41,35 @@ void tau_ops(const Ctx& c, const double* D2, const double* kx, double lam, doubl
 // G_k = A_k^{-1} P (row-major), P = identity with rows N-2, N-1 zeroed
 void green_from_lu(const Ctx& c, const double* LUcm, const int* piv, double* G, int N, int Nk);
 
+// counters of the viscosity pipeline kept on the device (the step reads none
+// of them; the handle's counters add them in when read)
+struct EtaCtrDev {
+  long long n_T_out_of_range, n_clip_T, n_clip_eta, n_smooth_eta, n_clip_eta_proj,
+      n_smooth_eta_proj;
+  double max_T_excursion;
+};
+// after eta_law on the padded grid: adds its statistics to ctr and applies the
+// hard clamp iff the window is hard and some point lies outside its dead band
+void eta_stats_apply(const Ctx& c, const double* stats, double* eta, long long npts,
+                     const EtaLaw& law, EtaCtrDev* ctr);
+// positivity guard of a truncated field (coupled_model.py:451-496), decided on
+// the device: when min(eta) = mn[0] is not > 0, counts the points outside the
+// dead-band window into ctr and applies the window (smooth: always, counting
+// the points inside its bands; hard: iff any point is outside)
+void eta_guard(const Ctx& c, const double* mn, double* eta, long long npts, const EtaLaw& law,
+               EtaCtrDev* ctr, double* scratch);
+
+// reuse of the spectral BFBT blocks, decided on the device: whether the held
+// profile is valid, and its age in solves
+struct BfbtHold {
+  int valid, age;
+};
+// sets `cond` (a conditional node of the launching graph) to 0 and ages the
+// held profile when it is valid, younger than max_age solves, and
+// max_q |prof_q - held_q| <= rel max_q |held_q| (real parts, NaN entries
+// ignored as the host's std::max ignores them); otherwise held = prof, age 1
+// and cond = 1 (the rebuild runs)
+void bfbt_decide(const Ctx& c, const double2* prof, double2* held, int N, int max_age, double rel,
+                 BfbtHold* h, cudaGraphConditionalHandle cond);
+
 }  // namespace smc

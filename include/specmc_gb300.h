@@ -149,7 +149,12 @@ int smc_march(smc_handle* h, const double* that_in, double* that_out, int mem,
  * reference's march_adaptive keeps `s` between steps, api.py:179-189):
  * set_state uploads a state and restarts the march clock t = 0; advance runs
  * CFL-limited steps (production_dt + step) until t >= tstop or max_steps
- * (<= 0: unbounded); get_state downloads the current state. */
+ * (<= 0: unbounded); get_state downloads the current state.
+ * Inside a march a step waits on the device twice (the Stokes-memo test, and
+ * the CFL reduction that also carries the solve's result and the next memo
+ * test); the result of the last temperature solve of smc_advance is read by
+ * the next call's first wait, or by any other entry point of the handle before
+ * it does anything else -- an error of that solve surfaces there. */
 int smc_set_state(smc_handle* h, const double* that, int mem);
 int smc_get_state(smc_handle* h, double* that_out, int mem);
 int smc_advance(smc_handle* h, double tstop, long long max_steps, double safety,

@@ -233,100 +233,97 @@ void krylov_update(const Ctx& c, double2* x, const double2* Z, const double2* y,
 
 // RBC.diagnostics (rbc_galerkin.py:439-453) from the grids ux, uz, th (Nx, N)
 // and the k = 0 row of that.  out = {Nu_top, Nu_bot, Nu_energy, urms, umax, amp}
-// One CTA of DIAG_THREADS threads: column sums with threads over (column,
-// row slice) pairs -- S = DIAG_THREADS / N slices of rows per column, each
-// thread's rows i = slice, slice + S, ... (coalesced across the columns of a
-// row), the slices then added in order -- the boundary fluxes V[end] (D
-// theta_0) and V[0] (D theta_0) with one warp per row of D (lanes over its
-// columns), then warp 0 reduces the Clenshaw-Curtis sums and the maxima with
-// lanes over columns.
-constexpr int DIAG_THREADS = 1024;
+// CTA g takes DIAG_COLS columns of the grids (32 row slices per column,
+// summed in slice order) and the same rows of D theta_0 (one warp per row),
+// and writes its weighted sums and maxima; the last CTA to finish (a ticket,
+// reset for the next launch) adds the CTAs' partials in CTA order.  The
+// arithmetic is spread over ceil(N / 8) SMs: FP64 on GB300 runs at about two
+// lanes per clock per SM, so one CTA spent 33 us on it at 64x96.
+constexpr int DIAG_COLS = 8, DIAG_SLICES = 32, DIAG_THREADS = DIAG_COLS * DIAG_SLICES;
 __global__ void __launch_bounds__(DIAG_THREADS) smc_diag_kernel(
     const double* __restrict__ ux, const double* __restrict__ uz, const double* __restrict__ th,
     const double2* __restrict__ that0, const double* __restrict__ D, const double* __restrict__ V,
-    const double* __restrict__ wq, int Nx, int N, double* __restrict__ out) {
-  extern __shared__ double sm[];
-  const int S = max(1, (int)blockDim.x / N);     // row slices per column
-  double* s1 = sm;            // column means of ux^2 + uz^2
-  double* s2 = sm + N;        // column means of uz th
-  double* mx = sm + 2 * N;    // column max |ux|,|uz|
-  double* ma = sm + 3 * N;    // column max |th|
-  double* dd = sm + 4 * N;    // (D theta_0)[r]
-  double* pt = sm + 5 * N;    // per-slice partials: 4 x S x N
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int u = threadIdx.x; u < S * N; u += blockDim.x) {
-    const int j = u % N, sl = u / N;
+    const double* __restrict__ wq, int Nx, int N, double* __restrict__ part,
+    unsigned int* __restrict__ ticket, double* __restrict__ out) {
+  __shared__ double ps[4][DIAG_SLICES][DIAG_COLS];
+  __shared__ double fl[2][DIAG_COLS];
+  __shared__ int s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c0 = blockIdx.x * DIAG_COLS;
+  {
+    const int jc = threadIdx.x % DIAG_COLS, sl = threadIdx.x / DIAG_COLS, j = c0 + jc;
     double a = 0, b = 0, m = 0, t = 0;
-    for (int i = sl; i < Nx; i += S) {
-      long long e = (long long)i * N + j;
-      double x = ux[e], z = uz[e], h = th[e];
-      a += x * x + z * z;
-      b += z * h;
-      m = fmax(m, fmax(fabs(x), fabs(z)));
-      t = fmax(t, fabs(h));
-    }
-    pt[(0 * S + sl) * N + j] = a;
-    pt[(1 * S + sl) * N + j] = b;
-    pt[(2 * S + sl) * N + j] = m;
-    pt[(3 * S + sl) * N + j] = t;
+    if (j < N)
+      for (int i = sl; i < Nx; i += DIAG_SLICES) {
+        const long long e = (long long)i * N + j;
+        const double x = ux[e], z = uz[e], h = th[e];
+        a += x * x + z * z;
+        b += z * h;
+        m = fmax(m, fmax(fabs(x), fabs(z)));
+        t = fmax(t, fabs(h));
+      }
+    ps[0][sl][jc] = a;
+    ps[1][sl][jc] = b;
+    ps[2][sl][jc] = m;
+    ps[3][sl][jc] = t;
   }
-  __syncthreads();
-  for (int j = threadIdx.x; j < N; j += blockDim.x) {
-    double a = 0, b = 0, m = 0, t = 0;
-    for (int sl = 0; sl < S; ++sl) {
-      a += pt[(0 * S + sl) * N + j];
-      b += pt[(1 * S + sl) * N + j];
-      m = fmax(m, pt[(2 * S + sl) * N + j]);
-      t = fmax(t, pt[(3 * S + sl) * N + j]);
-    }
-    s1[j] = a / Nx;
-    s2[j] = b / Nx;
-    mx[j] = m;
-    ma[j] = t;
-  }
-  for (int r = warp; r < N; r += nw) {
+  {
+    // (D theta_0)[r] for this CTA's rows r = c0 + warp, and its boundary fluxes
+    const int r = c0 + warp;
     double d = 0;
-    for (int q = lane; q < N; q += 32) d += D[(long long)r * N + q] * that0[q].x;
+    if (r < N)
+      for (int q = lane; q < N; q += 32) d += D[(long long)r * N + q] * that0[q].x;
     for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    if (lane == 0) dd[r] = d;
+    if (lane == 0) {
+      fl[0][warp] = r < N ? V[(long long)(N - 1) * N + r] * d : 0.0;
+      fl[1][warp] = r < N ? V[r] * d : 0.0;
+    }
   }
   __syncthreads();
-  if (warp == 0) {
+  if (threadIdx.x == 0) {
     double v1 = 0, v2 = 0, m = 0, t = 0, ntop = 0, nbot = 0;
-    for (int j = lane; j < N; j += 32) {
-      v1 += wq[j] * s1[j];
-      v2 += wq[j] * s2[j];
-      m = fmax(m, mx[j]);
-      t = fmax(t, ma[j]);
-      ntop += V[(long long)(N - 1) * N + j] * dd[j];
-      nbot += V[j] * dd[j];
+    for (int jc = 0; jc < DIAG_COLS && c0 + jc < N; ++jc) {
+      double a = 0, b = 0, mm = 0, tt = 0;
+      for (int sl = 0; sl < DIAG_SLICES; ++sl) {
+        a += ps[0][sl][jc];
+        b += ps[1][sl][jc];
+        mm = fmax(mm, ps[2][sl][jc]);
+        tt = fmax(tt, ps[3][sl][jc]);
+      }
+      v1 += wq[c0 + jc] * (a / Nx);
+      v2 += wq[c0 + jc] * (b / Nx);
+      m = fmax(m, mm);
+      t = fmax(t, tt);
+      ntop += fl[0][jc];
+      nbot += fl[1][jc];
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      v1 += __shfl_xor_sync(0xffffffffu, v1, o);
-      v2 += __shfl_xor_sync(0xffffffffu, v2, o);
-      ntop += __shfl_xor_sync(0xffffffffu, ntop, o);
-      nbot += __shfl_xor_sync(0xffffffffu, nbot, o);
-      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-      t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
-    }
-    if (lane == 0) {
-      out[0] = 1.0 - ntop;
-      out[1] = 1.0 - nbot;
-      out[2] = 1.0 + v2;
-      out[3] = sqrt(fmax(v1, 0.0));
-      out[4] = m;
-      out[5] = t;
-    }
+    double* p = part + 6LL * blockIdx.x;
+    p[0] = v1; p[1] = v2; p[2] = m; p[3] = t; p[4] = ntop; p[5] = nbot;
+    __threadfence();
+    s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
   }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return;
+  __threadfence();
+  double v1 = 0, v2 = 0, m = 0, t = 0, ntop = 0, nbot = 0;
+  for (int g = 0; g < (int)gridDim.x; ++g) {
+    const volatile double* p = part + 6LL * g;
+    v1 += p[0]; v2 += p[1]; m = fmax(m, p[2]); t = fmax(t, p[3]); ntop += p[4]; nbot += p[5];
+  }
+  out[0] = 1.0 - ntop;
+  out[1] = 1.0 - nbot;
+  out[2] = 1.0 + v2;
+  out[3] = sqrt(fmax(v1, 0.0));
+  out[4] = m;
+  out[5] = t;
+  *ticket = 0u;
 }
 
 void diagnostics_reduce(const Ctx& c, const double* ux, const double* uz, const double* th,
                         const double2* that0, const double* D, const double* V, const double* wq,
-                        int Nx, int N, double* out) {
-  const int S = std::max(1, DIAG_THREADS / N);
-  const size_t sm = (size_t)(5 * N + 4 * S * N) * sizeof(double);
-  if (sm > 48 * 1024) allow_max_smem((const void*)smc_diag_kernel);
-  smc_diag_kernel<<<1, DIAG_THREADS, sm, c.s>>>(ux, uz, th, that0, D, V, wq, Nx, N, out);
+                        int Nx, int N, double* out, double* scratch, unsigned int* ticket) {
+  const int G = (N + DIAG_COLS - 1) / DIAG_COLS;
+  smc_diag_kernel<<<G, DIAG_THREADS, 0, c.s>>>(ux, uz, th, that0, D, V, wq, Nx, N, scratch, ticket, out);
   SMC_LAUNCH_CHECK(c);
 }
 

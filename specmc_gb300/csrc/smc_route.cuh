@@ -19,7 +19,9 @@ void vec_div(const Ctx& c, const double2* in, double h, double2* out, long long 
 void mgs(const Ctx& c, const double2* V, int j, long long n, double2* w, double2* hout);
 void krylov_update(const Ctx& c, double2* x, const double2* Z, const double2* y, int k,
                    long long n);
+// scratch: 6 ceil(N / 8) doubles; ticket: a zeroed word of the handle's
+// (the kernel leaves it zero)
 void diagnostics_reduce(const Ctx& c, const double* ux, const double* uz, const double* th,
                         const double2* that0, const double* D, const double* V, const double* wq,
-                        int Nx, int N, double* out);
+                        int Nx, int N, double* out, double* scratch, unsigned int* ticket);
 }  // namespace smc

@@ -367,6 +367,7 @@ struct Model {
   // the viscosity pipeline's counters and the BFBT blocks' reuse state, kept
   // on the device so that no step waits on them
   EtaCtrDev* dEtaCtr = nullptr;
+  unsigned int* dDiagTicket = nullptr;     // last-CTA ticket of the diagnostics reduction
   BfbtHold* dBfbtHold = nullptr;
   double2* dBfbtHeld = nullptr;
   // Krylov
@@ -728,6 +729,7 @@ struct Model {
     dRed = mem.alloc<double>(4096);
     dScal = mem.alloc<double>(64);
     dEtaCtr = mem.alloc<EtaCtrDev>(1);
+    dDiagTicket = mem.alloc<unsigned int>(1);
     dPrev = mem.alloc<double2>(n); dPsiPrev = mem.alloc<double2>(n); dPsiN = mem.alloc<double2>(n);
     dMemoThat = mem.alloc<double2>(n); dMemoX = mem.alloc<double2>(n);
     dMemoPsi = mem.alloc<double2>(n); dMemoOm = mem.alloc<double2>(n);
@@ -2681,7 +2683,8 @@ int smc_diagnostics(smc_handle* h, const double* in, int mem, smc_diag* out) {
     m.stokes(m.dIn, m.dPsi, m.dOm);
     m.velocity(m.dPsi, m.gr[0], m.gr[1]);
     m.synth(m.dIn, m.dV, smc::KFactor(), m.gr[2], m.Nx, m.sp[4]);
-    smc::diagnostics_reduce(m.ctx, m.gr[0], m.gr[1], m.gr[2], m.dIn, m.dD, m.dV, m.dwq, m.Nx, m.N, m.dScal);
+    smc::diagnostics_reduce(m.ctx, m.gr[0], m.gr[1], m.gr[2], m.dIn, m.dD, m.dV, m.dwq, m.Nx, m.N, m.dScal,
+                            m.dRed, m.dDiagTicket);
     m.sync_read(m.dScal, 6);
     out->Nu_top = m.hbuf[0]; out->Nu_bot = m.hbuf[1]; out->Nu_energy = m.hbuf[2];
     out->urms = m.hbuf[3]; out->umax = m.hbuf[4]; out->amp = m.hbuf[5];

@@ -1687,18 +1687,41 @@ struct Model {
     return norm(dSAx) / bn;
   }
 
-  // fast form: after a dense rescue the BFBT blocks have just failed for this
-  // eta field and the lagged dense factor is fresh, so the next solves use
-  // the lagged-LU defect route (the reference's legacy route,
-  // coupled_model.py:524-586) until its lag expires, then BFBT is tried again
-  int legacy_after_rescue = 0;
-  long long n_legacy_after_rescue = 0;
+  // fast form, after a dense rescue (the BFBT blocks have just failed for
+  // this eta field; the dense factor is fresh):
+  //  lu_mode 1: FP64 FGMRES preconditioned by the lagged factor, which is not
+  //    refactored however far eta drifts (the legacy route refactors at every
+  //    drifted step: tens to hundreds of ms at 64x48..128x96), while solves
+  //    converge within LU_PRECOND_SLOW iterations (then BFBT again); a solve
+  //    that does not converge within LU_PRECOND_MAXIT (eta moves too fast for
+  //    a stale factor) is solved by, and turns to,
+  //  lu_mode 2: the legacy lagged-LU route (coupled_model.py:524-586,
+  //    refactored as its drift test asks) for `lag` solves, then BFBT again.
+  static constexpr int LU_PRECOND_MAXIT = 40, LU_PRECOND_SLOW = 20;
+  int lu_mode = 0, legacy_left = 0;
 
   void bfbt_solve(const double2* th, double2* x) {
     rhs_schur(th, dSb);
-    if (fast && legacy_after_rescue > 0 && dSchur) {
-      --legacy_after_rescue;
-      ++n_legacy_after_rescue;
+    if (fast && lu_mode == 1 && dSchur && have_lag) {
+      Op A64 = [&](const double2* v, double2* o) { schur_matvec_fast(v, o, false); };
+      Op M = [&](const double2* r, double2* z) { lag_solve(r, z); };
+      FgmresResult fr = fgmres(A64, M, dSb, x, cfg.stokes_rtol, cfg.stokes_restart, LU_PRECOND_MAXIT);
+      schur_matvec_fast(x, dSAx, false);
+      vec_axpby(ctx, dSAx, make_double2(1.0, 0.0), dSb, make_double2(-1.0, 0.0), n);
+      const double res = norm(dSAx) / std::max(norm(dSb), 1e-300);
+      if (fr.info == 0 || res <= cfg.stokes_rtol) {
+        ctr.n_bfbt_solves++;
+        ctr.n_bfbt_iters += fr.iters;
+        ctr.last_bfbt_true_res = res;
+        ctr.last_K = 0;
+        if (fr.iters > LU_PRECOND_SLOW) lu_mode = 0;
+        return;
+      }
+      lu_mode = 2;
+      legacy_left = cfg.lag;
+    }
+    if (fast && lu_mode == 2 && dSchur) {
+      if (--legacy_left <= 0) lu_mode = 0;
       legacy_solve(th, x);
       return;
     }
@@ -1811,7 +1834,7 @@ struct Model {
     if (fr.info != 0 && !(res <= cfg.stokes_rtol)) {
       // rescue chain (coupled_model.py:613-654)
       ctr.n_bfbt_rescue++;
-      if (fast) legacy_after_rescue = cfg.lag;
+      if (fast) lu_mode = 1;
       refresh();
       defect_solve(th, x);
       if (last_failed) {

@@ -105,3 +105,29 @@ def test_forced_bfbt_rescue(gb):
     assert np.abs(psi_r - psi_l).max() <= 1e-12 * np.abs(psi_l).max()
     psi_o, _ = O.CoupledModel(Nx=16, Nz=12, deta_T=1000.0, precond="legacy").stokes(th)
     assert np.abs(psi_r - psi_o).max() <= 1e-8 * np.abs(psi_o).max()
+
+
+
+def test_mixed_rescue_then_lu_preconditioned(gb):
+    """The mixed form with a one-iteration BFBT budget: its first Stokes solve
+    fails (FP32, then FP64) and is rescued by the dense route (refresh +
+    defect correction); the later solves are FP64 FGMRES solves preconditioned
+    by that factor, refactored only when such a solve fails (then the legacy
+    route for a while).  The march equals the plain legacy route's to the
+    solver tolerances, and not every solve refactors."""
+    from specmc_gb300.solver import RBCCoupled
+    mm = RBCCoupled(Nx=32, Nz=24, deta_T=1000.0, stokes_maxiter=1, form="mixed")
+    mp = RBCCoupled(Nx=32, Nz=24, deta_T=1000.0, precond="legacy")
+    sm = mm.seed(amp=3e-2, m=1, n=1)
+    sp = np.array(sm, copy=True)
+    steps = 12
+    for _ in range(steps):
+        dt = mp.production_dt(sp)
+        sp = mp.step(sp, dt)
+        sm = mm.step(sm, dt)
+    c = mm.counters()
+    assert c["n_bfbt_rescue"] >= 1 and c["n_refresh"] < c["n_stokes"], c
+    assert np.abs(sm - sp).max() <= 1e-7 * np.abs(sp).max()
+    dm, dp = mm.diagnostics(sm), mp.diagnostics(sp)
+    for key in ("Nu_top", "urms"):
+        assert abs(dm[key] - dp[key]) <= 1e-7 * abs(dp[key]), (key, dm[key], dp[key])

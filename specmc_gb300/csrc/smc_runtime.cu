@@ -2020,10 +2020,20 @@ struct Model {
     else stokes_memo(th, psi, om);
   }
 
-  void velocity(const double2* psi, double* ux, double* uz) {
-    synth(psi, dVD, KFactor(), ux, Nx, sp[4]);
+  // the two syntheses of a velocity (ux = VD psi, uz = V (-i k psi)) as one
+  // two-job launch of each transform kernel (each job computes what its own
+  // launch would)
+  void synth_pair(const double2* psi, double* ux, double* uz, int Ng) {
     KFactor f; f.cre = 0.0; f.cim = -1.0; f.kpow = 1;       // -i k psi
-    synth(psi, dV, f, uz, Nx, sp[4]);
+    ZJob j[2];
+    j[0].Z = dVD; j[0].X = psi; j[0].Y = sp[4];
+    j[1].Z = dV; j[1].X = psi; j[1].Y = sp[9]; j[1].f = f;
+    zmat_apply(ctx, j, 2, Nk, N, dkx);
+    SynthJob s[2] = {{sp[4], ux}, {sp[9], uz}};
+    synth_x(ctx, s, 2, Nk, N, Ng, Ng == Np ? dtwNp : dtwNx);
+  }
+  void velocity(const double2* psi, double* ux, double* uz) {
+    synth_pair(psi, ux, uz, Nx);
     if (tala) grid_div_rho(ctx, ux, uz, dRho, (long long)Nx * N, N);   // u = curl(Psi) / rho_bar
   }
 
@@ -2179,9 +2189,7 @@ struct Model {
     // frozen velocity on the padded grid
     {
       ProfScope psa(ctx, "theta_rhs");
-      KFactor mik; mik.cre = 0.0; mik.cim = -1.0; mik.kpow = 1;
-      synth(ps, dVD, KFactor(), gr[0], Np, sp[12]);
-      synth(ps, dV, mik, gr[1], Np, sp[12]);
+      synth_pair(ps, gr[0], gr[1], Np);
     }
     const double2* phi = nullptr;
     if (cfg.dissipation_number != 0.0) { phi_source(ps, dPhi); phi = dPhi; }

@@ -7,8 +7,9 @@ headline   the mixed form on eta_T 64x96 (deta_T 1e3, Ra 1e4, seed amp 3e-2): 6 
            the seeded 256-run ensemble, 3 steps each, through the batched engine
 ensemble   the first 8 runs of the seeded ensemble, 3 steps each, batched engine with refill off
            (each cooperative launch a fixed set of solves)
-plain_lu   the plain form on eta_T 64x96 and 128x96, 4 steps each, with the dense Schur LU's
-           trailing update in FP64 SIMT and on the tensor cores (prints the factorisation times)
+plain_lu   the plain form on eta_T 32x24, 64x48, 64x96 and 128x96, 4 steps each, with the dense
+           Schur LU's trailing update in FP64 SIMT and on the tensor cores (prints the
+           factorisation times)
 """
 from __future__ import annotations
 
@@ -50,7 +51,7 @@ def ensemble_fixed():
 
 def plain_lu(steps=4):
     from . import _lib, api
-    for Nx, Nz in ((64, 96), (128, 96)):
+    for Nx, Nz in ((32, 24), (64, 48), (64, 96), (128, 96)):
         for tc in (0.0, 1.0):
             m = api.build_model(_eta_t(Nx, Nz), form="plain")
             lib = m._lib

@@ -376,7 +376,6 @@ struct Model {
   // Schur defect work
   double2 *dSb, *dSx, *dSr, *dSdx, *dSAx, *dSw, *dSf2, *dSf3, *dSf4, *dSt[4], *dSolveWork;
   double2 *dBfbtRhs, *dBfbtProfC;
-  double* dBfbtHw;
   // TALA (compressibility SMC_TALA): rho_bar on the CGL nodes and its
   // inverse, the coefficients of rho_bar, product matrices of rho_bar and
   // rho_bar^2, Mrho Vi, the L^(rho) Green operators and work buffers
@@ -855,7 +854,6 @@ struct Model {
         dSf2 = mem.alloc<double2>(n); dSf3 = mem.alloc<double2>(n); dSf4 = mem.alloc<double2>(n);
         for (auto& p : dSt) p = mem.alloc<double2>(n);
         dSolveWork = mem.alloc<double2>(n);
-        dBfbtHw = mem.alloc<double>(2 * N);
         // pseudo-spectral plan: L >= 3 Nk - 2 x-points, Mz = 2N - 1 CGL points
         // L: the first power of two >= 3 Nk - 2 (alias-free products of two
         // Nk-mode fields; a power of two for the radix-2 FFTs)
@@ -1375,17 +1373,18 @@ struct Model {
   void eta_of(const double2* th) {
     ProfScope ps(ctx, "eta_of");
     synth(th, dV, KFactor(), gr[0], Np, sp[0]);              // theta on 2 Nx points
-    eta_law(ctx, gr[0], dz, N, (long long)Np * N, law, dEtaP, dScal, dRed);
+    eta_law(ctx, gr[0], dz, N, (long long)Np * N, law, dEtaP, nullptr, dRed);
     // the T / eta counters and the hard window of the padded field (applied
     // iff some point lies outside its dead band), decided on the device
-    eta_stats_apply(ctx, dScal, dEtaP, (long long)Np * N, law, dEtaCtr);
+    eta_stats_apply(ctx, dRed, dEtaP, (long long)Np * N, law, dEtaCtr);
     AnaJob a{dEtaP, sp[1]};
     analysis_x(ctx, &a, 1, Nk, N, Np, dtwNp, 1.0 / Np);
     SynthJob s{sp[1], dEta};
     synth_x(ctx, &s, 1, Nk, N, Nx, dtwNx);
-    min_and_drift(ctx, dEta, nullptr, (long long)Nx * N, dScal, dRed);
+    min_and_drift(ctx, dEta, nullptr, (long long)Nx * N, nullptr, dRed);
     // positivity guard (coupled_model.py:451-496), gated on min(eta) <= 0
-    eta_guard(ctx, dScal, dEta, (long long)Nx * N, law, dEtaCtr, dRed);
+    // (its count partials after the min/drift partials: at most 2 x 120)
+    eta_guard(ctx, dRed, dEta, (long long)Nx * N, law, dEtaCtr, dRed + 256);
   }
 
   // Md (dense blocks, for the Schur assembly) and the pseudo-spectral eta
@@ -1608,8 +1607,7 @@ struct Model {
   // and a skipped rebuild launches none of its kernels.
   void bfbt_build() {
     ProfScope psp(ctx, "bfbt_profile");
-    harm_profile_rhs(ctx, dEta, Nx, N, dwq, dBfbtHw);
-    to_complex(dBfbtHw, dBfbtRhs, N);
+    harm_profile_rhs(ctx, dEta, Nx, N, dwq, dBfbtRhs);
     ZJob j; j.Z = dVT; j.X = dBfbtRhs; j.Y = dBfbtProfC;     // V^T (w g)
     zmat_apply(ctx, &j, 1, 1, N, dkx);
     if (fast) kgemv(ctx, dMpInv, dBfbtProfC, dBfbtRhs, 1, N, 1.0);
@@ -1678,7 +1676,6 @@ struct Model {
   void bfbt_invalidate() {
     if (dBfbtHold) SMC_CUDA(cudaMemsetAsync(&dBfbtHold->valid, 0, sizeof(int), stream));
   }
-  void to_complex(const double* in, double2* out, int count);
 
   double schur_true_res(const double2* b, const double2* x) {
     schur_matvec(x, dSAx);
@@ -2404,10 +2401,6 @@ __global__ void smc_realpart_kernel(const double2* in, double* out, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = in[i].x;
 }
-__global__ void smc_tocomplex_kernel(const double* in, double2* out, int n) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = make_double2(in[i], 0.0);
-}
 __global__ void smc_comm_kernel(const double* a, const double* b, const double* c, double* out,
                                 long long n) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2415,10 +2408,6 @@ __global__ void smc_comm_kernel(const double* a, const double* b, const double* 
 }
 void Model::realpart(const double2* in, double* out, int count) {
   smc_realpart_kernel<<<ceil_div(count, 128), 128, 0, stream>>>(in, out, count);
-  SMC_LAUNCH_CHECK(ctx);
-}
-void Model::to_complex(const double* in, double2* out, int count) {
-  smc_tocomplex_kernel<<<ceil_div(count, 128), 128, 0, stream>>>(in, out, count);
   SMC_LAUNCH_CHECK(ctx);
 }
 void Model::comm_combine(const double* a, const double* b, const double* c, double* out,

@@ -327,9 +327,8 @@ __global__ void smc_eta_law_kernel(const double* __restrict__ th, const double* 
 
 // one warp: lanes stride over the per-CTA partials (maxima, and counts that
 // are exact in any summation order)
-__global__ void smc_eta_stats_final_kernel(const double* part, int np, double* dst) {
+__device__ __forceinline__ void eta_stats_reduce(const double* part, int np, double* dst) {
   const int lane = threadIdx.x & 31;
-  if (threadIdx.x >= 32) return;
   double a0 = -INFINITY, a1 = -INFINITY, a[4] = {0, 0, 0, 0};
   for (int b = lane; b < np; b += 32) {
     const double* o = part + 6LL * b;
@@ -346,6 +345,9 @@ __global__ void smc_eta_stats_final_kernel(const double* part, int np, double* d
     for (int t = 0; t < 4; ++t) dst[2 + t] = a[t];
   }
 }
+__global__ void smc_eta_stats_final_kernel(const double* part, int np, double* dst) {
+  if (threadIdx.x < 32) eta_stats_reduce(part, np, dst);
+}
 
 void eta_law(const Ctx& c, const double* th, const double* z, int N, long long npts,
              const EtaLaw& law, double* eta, double* stats, double* scratch) {
@@ -353,6 +355,7 @@ void eta_law(const Ctx& c, const double* th, const double* z, int N, long long n
   if (nb < 1) nb = 1;
   smc_eta_law_kernel<<<nb, 256, 0, c.s>>>(th, z, N, npts, law, eta, scratch);
   SMC_LAUNCH_CHECK(c);
+  if (!stats) return;
   smc_eta_stats_final_kernel<<<1, 32, 0, c.s>>>(scratch, nb, stats);
   SMC_LAUNCH_CHECK(c);
 }
@@ -480,6 +483,7 @@ void min_and_drift(const Ctx& c, const double* eta, const double* lag, long long
   if (nb < 1) nb = 1;
   smc_min_drift_kernel<<<nb, 256, 0, c.s>>>(eta, lag, n, scratch);
   SMC_LAUNCH_CHECK(c);
+  if (!dst) return;
   smc_min_drift_final_kernel<<<1, 32, 0, c.s>>>(scratch, nb, dst);
   SMC_LAUNCH_CHECK(c);
 }
@@ -499,8 +503,13 @@ __device__ __forceinline__ double block_sum256(double v, double* ws) {
   return s;
 }
 
-__global__ void smc_eta_stats_apply_kernel(const double* __restrict__ st, double* __restrict__ eta,
-                                           long long npts, EtaLaw law, EtaCtrDev* __restrict__ ctr) {
+__global__ void smc_eta_stats_apply_kernel(const double* __restrict__ part, int np,
+                                           double* __restrict__ eta, long long npts, EtaLaw law,
+                                           EtaCtrDev* __restrict__ ctr) {
+  // every CTA reduces the law kernel's partials itself (the same values)
+  __shared__ double st[6];
+  if (threadIdx.x < 32) eta_stats_reduce(part, np, st);
+  __syncthreads();
   const double clip = st[4];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     const double tmin = st[0], tmax = st[1];
@@ -521,18 +530,40 @@ __global__ void smc_eta_stats_apply_kernel(const double* __restrict__ st, double
     eta[idx] = fmin(fmax(eta[idx], law.lo), law.hi);
 }
 
-void eta_stats_apply(const Ctx& c, const double* stats, double* eta, long long npts,
+void eta_stats_apply(const Ctx& c, const double* part, double* eta, long long npts,
                      const EtaLaw& law, EtaCtrDev* ctr) {
   int nb = (int)std::min<long long>(120, (npts + 255) / 256);
   if (nb < 1) nb = 1;
-  smc_eta_stats_apply_kernel<<<nb, 256, 0, c.s>>>(stats, eta, npts, law, ctr);
+  smc_eta_stats_apply_kernel<<<nb, 256, 0, c.s>>>(part, nb, eta, npts, law, ctr);
   SMC_LAUNCH_CHECK(c);
 }
 
+// whether the guard runs: min(eta) not > 0 (or a NaN), from the min/drift
+// kernel's per-CTA partials (as its final reduction decides: any NaN partial
+// makes the minimum NaN); every CTA takes the same decision
+__device__ __forceinline__ bool eta_guard_active(const double* __restrict__ mpart, int mnp) {
+  __shared__ int s_act;
+  if (threadIdx.x < 32) {
+    double a = INFINITY;
+    bool nan_seen = false;
+    for (int i = threadIdx.x; i < mnp; i += 32) {
+      const double x = mpart[2 * i], y = mpart[2 * i + 1];
+      if (x != x || y != y) nan_seen = true;
+      a = fmin(a, x);
+    }
+    for (int d = 16; d > 0; d >>= 1) a = fmin(a, __shfl_xor_sync(0xffffffffu, a, d));
+    nan_seen = __any_sync(0xffffffffu, nan_seen);
+    if (threadIdx.x == 0) s_act = nan_seen || !(a > 0.0);
+  }
+  __syncthreads();
+  return s_act != 0;
+}
+
 // guard, pass 1: per-CTA counts of the points outside the dead-band window
-__global__ void smc_eta_guard_count_kernel(const double* __restrict__ mn, const double* __restrict__ eta,
-                                           long long npts, EtaLaw law, double* __restrict__ part) {
-  if (mn[0] > 0.0) return;
+__global__ void smc_eta_guard_count_kernel(const double* __restrict__ mpart, int mnp,
+                                           const double* __restrict__ eta, long long npts, EtaLaw law,
+                                           double* __restrict__ part) {
+  if (!eta_guard_active(mpart, mnp)) return;
   __shared__ double ws[8];
   double cnt = 0.0;
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < npts;
@@ -547,10 +578,11 @@ __global__ void smc_eta_guard_count_kernel(const double* __restrict__ mn, const 
 // guard, pass 2: every CTA sums the pass-1 counts (integers: exact in any
 // order), CTA 0 adds them to the counters, and the window is applied when it
 // is smooth or some point lies outside the dead band
-__global__ void smc_eta_guard_apply_kernel(const double* __restrict__ mn, double* __restrict__ eta,
-                                           long long npts, EtaLaw law, const double* __restrict__ part,
-                                           int np, EtaCtrDev* __restrict__ ctr) {
-  if (mn[0] > 0.0) return;
+__global__ void smc_eta_guard_apply_kernel(const double* __restrict__ mpart, int mnp,
+                                           double* __restrict__ eta, long long npts, EtaLaw law,
+                                           const double* __restrict__ part, int np,
+                                           EtaCtrDev* __restrict__ ctr) {
+  if (!eta_guard_active(mpart, mnp)) return;
   __shared__ double ws[8];
   __shared__ double s_c;
   if (threadIdx.x < 32) {
@@ -574,13 +606,13 @@ __global__ void smc_eta_guard_apply_kernel(const double* __restrict__ mn, double
               (unsigned long long)(long long)band);
 }
 
-void eta_guard(const Ctx& c, const double* mn, double* eta, long long npts, const EtaLaw& law,
+void eta_guard(const Ctx& c, const double* mpart, double* eta, long long npts, const EtaLaw& law,
                EtaCtrDev* ctr, double* scratch) {
   int nb = (int)std::min<long long>(120, (npts + 255) / 256);
   if (nb < 1) nb = 1;
-  smc_eta_guard_count_kernel<<<nb, 256, 0, c.s>>>(mn, eta, npts, law, scratch);
+  smc_eta_guard_count_kernel<<<nb, 256, 0, c.s>>>(mpart, nb, eta, npts, law, scratch);
   SMC_LAUNCH_CHECK(c);
-  smc_eta_guard_apply_kernel<<<nb, 256, 0, c.s>>>(mn, eta, npts, law, scratch, nb, ctr);
+  smc_eta_guard_apply_kernel<<<nb, 256, 0, c.s>>>(mpart, nb, eta, npts, law, scratch, nb, ctr);
   SMC_LAUNCH_CHECK(c);
 }
 
@@ -636,7 +668,7 @@ void bfbt_decide(const Ctx& c, const double2* prof, double2* held, int N, int ma
 // shape, and the FP64 divisions are spread over N SMs instead of one.
 static constexpr int HP_CHUNK = 1024;
 __global__ void smc_harm_profile_kernel(const double* __restrict__ eta, int Nx, int N,
-                                        const double* __restrict__ wq, double* __restrict__ out) {
+                                        const double* __restrict__ wq, double2* __restrict__ out) {
   __shared__ double rcp[HP_CHUNK];
   const int j = blockIdx.x;
   double s = 0.0;
@@ -648,11 +680,11 @@ __global__ void smc_harm_profile_kernel(const double* __restrict__ eta, int Nx, 
       for (int i = 0; i < cnt; ++i) s += rcp[i];
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[j] = wq[j] * (1.0 / (s / Nx));
+  if (threadIdx.x == 0) out[j] = make_double2(wq[j] * (1.0 / (s / Nx)), 0.0);
 }
 
 void harm_profile_rhs(const Ctx& c, const double* eta, int Nx, int N, const double* wq,
-                      double* out) {
+                      double2* out) {
   smc_harm_profile_kernel<<<N, 128, 0, c.s>>>(eta, Nx, N, wq, out);
   SMC_LAUNCH_CHECK(c);
 }

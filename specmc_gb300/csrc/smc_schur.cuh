@@ -21,18 +21,21 @@ struct EtaLaw {
 void bgemm(const Ctx& c, bool a_cplx, const void* A, long long sa, bool b_cplx, const void* B,
            long long sb, void* C, long long sc, int N, int batch, double alpha);
 // stats = {min T, max T, #T outside [0,1], #T outside [0,2], #eta outside the
-//          dead-band window, #ln(eta) strictly inside a smooth band}
+//          dead-band window, #ln(eta) strictly inside a smooth band}; null:
+// only the per-CTA partials in scratch (for eta_stats_apply)
 void eta_law(const Ctx& c, const double* th, const double* z, int N, long long npts,
              const EtaLaw& law, double* eta, double* stats, double* scratch);
 // counts = {#outside dead-band window, #inside smooth band}; applies the
 // clamp unless count_only
 void eta_window(const Ctx& c, double* eta, long long npts, const EtaLaw& law, int count_only,
                 double* counts, double* scratch);
-// dst = {min eta, max pointwise relative drift vs lag (0 when lag null)}
+// dst = {min eta, max pointwise relative drift vs lag (0 when lag null)}; null
+// dst: only the per-CTA partials in scratch (for eta_guard)
 void min_and_drift(const Ctx& c, const double* eta, const double* lag, long long n, double* dst,
                    double* scratch);
+// out_j = w_j / mean_i(1 / eta[i][j]) as a complex vector (imaginary part 0)
 void harm_profile_rhs(const Ctx& c, const double* eta, int Nx, int N, const double* wq,
-                      double* out);
+                      double2* out);
 void cheb_mult_real(const Ctx& c, const double* a, double* M, int N);
 void reduced_blocks(const Ctx& c, const double* DM, const double* M, const double* CommG,
                     const double* V, const double* kx, double* Pcm, int N, int Nk);
@@ -48,15 +51,17 @@ struct EtaCtrDev {
       n_smooth_eta_proj;
   double max_T_excursion;
 };
-// after eta_law on the padded grid: adds its statistics to ctr and applies the
-// hard clamp iff the window is hard and some point lies outside its dead band
-void eta_stats_apply(const Ctx& c, const double* stats, double* eta, long long npts,
+// after eta_law (stats null) on the padded grid, from its per-CTA partials:
+// adds its statistics to ctr and applies the hard clamp iff the window is hard
+// and some point lies outside its dead band
+void eta_stats_apply(const Ctx& c, const double* part, double* eta, long long npts,
                      const EtaLaw& law, EtaCtrDev* ctr);
 // positivity guard of a truncated field (coupled_model.py:451-496), decided on
-// the device: when min(eta) = mn[0] is not > 0, counts the points outside the
-// dead-band window into ctr and applies the window (smooth: always, counting
-// the points inside its bands; hard: iff any point is outside)
-void eta_guard(const Ctx& c, const double* mn, double* eta, long long npts, const EtaLaw& law,
+// the device from min_and_drift's partials (dst null) of the same field: when
+// min(eta) is not > 0, counts the points outside the dead-band window into ctr
+// and applies the window (smooth: always, counting the points inside its bands;
+// hard: iff any point is outside).  scratch must not overlap mpart.
+void eta_guard(const Ctx& c, const double* mpart, double* eta, long long npts, const EtaLaw& law,
                EtaCtrDev* ctr, double* scratch);
 
 // reuse of the spectral BFBT blocks, decided on the device: whether the held

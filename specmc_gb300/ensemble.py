@@ -118,9 +118,23 @@ def _march_one(run, nsteps, form, device, cap, safety, dtmax, chunk, max_wall, o
         model.close()
 
 
+def run_cost(cfg):
+    """A rough relative cost of marching ``cfg`` (for ordering only): grid
+    size times a factor of the viscosity model, which for eta_T grows with the
+    viscosity contrast and the Rayleigh number (the BFBT iteration counts and
+    the dense rescues of the hard runs)."""
+    cells = (cfg.Nx // 2 + 1) * cfg.Nz
+    vm = cfg.viscosity_model
+    if vm == "const":
+        return cells
+    if vm == "eta_z":
+        return 4.0 * cells
+    return 16.0 * cells * (1.0 + np.log10(max(cfg.deta_T, 1.0))) * np.sqrt(cfg.Ra / 1e4)
+
+
 def march_ensemble_native(runs, nsteps=100, form="mixed", concurrency=16, safety=None,
                           dtmax=None, device=0, batched=True, check_every=5, overrides=None,
-                          batch_ctas=None, keep_states=True):
+                          batch_ctas=None, keep_states=True, longest_first=True):
     """March every run of ``runs`` for ``nsteps`` CFL-limited steps in one
     native call (``smc_march_many``: ``concurrency`` C++ threads; with
     ``batched`` the mixed form's refinement solves of all runs go through the
@@ -128,9 +142,12 @@ def march_ensemble_native(runs, nsteps=100, form="mixed", concurrency=16, safety
     non-finite state stops it ('non-finite'); max|theta| above AMP_LIMIT x its
     initial value flags it ('amplitude', the reference driver's abort
     threshold, specmc/_numerics.py:139-140) and it marches on.  No run is cut
-    short for time.  Returns one result dict per run (as march_ensemble) and,
-    under the key ``"_timing"`` of the first, the march's wall time and the
-    batcher's launch statistics."""
+    short for time.  With ``longest_first`` the worker threads take the runs in
+    decreasing ``run_cost`` (a long run drawn last would stretch the wall time;
+    every run's result is the same in any order).  Returns one result dict per
+    run, in the order of ``runs`` (as march_ensemble), and, under the key
+    ``"_timing"`` of the first, the march's wall time and the batcher's launch
+    statistics."""
     safety = NUM.CFL_SAFETY if safety is None else float(safety)
     dtmax = NUM.DTMAX if dtmax is None else float(dtmax)
     lib = _lib.load()
@@ -154,17 +171,23 @@ def march_ensemble_native(runs, nsteps=100, form="mixed", concurrency=16, safety
             _lib.check(lib.smc_set_state(model._h, th.ctypes.data_as(ctypes.c_void_p),
                                          _lib.SMC_HOST))
             t_build.append(time.perf_counter() - t0)
-        hs = (ctypes.c_void_p * len(models))(*[m._h for m in models])
-        res = (_lib.SmcRunResult * len(models))()
+        order = list(range(len(models)))
+        if longest_first:
+            order.sort(key=lambda i: -run_cost(runs[i]["cfg"]))
+        hs = (ctypes.c_void_p * len(models))(*[models[i]._h for i in order])
+        res_ord = (_lib.SmcRunResult * len(models))()
         b0 = [ctypes.c_longlong() for _ in range(3)]
         _lib.check(lib.smc_batch_stats(int(device), *[ctypes.byref(x) for x in b0]))
         t0 = time.perf_counter()
         _lib.check(lib.smc_march_many(hs, len(models), int(nsteps), safety, dtmax,
                                       float(NUM.AMP_LIMIT), int(check_every), int(concurrency),
-                                      1 if batched else 0, res))
+                                      1 if batched else 0, res_ord))
         wall = time.perf_counter() - t0
         b1 = [ctypes.c_longlong() for _ in range(3)]
         _lib.check(lib.smc_batch_stats(int(device), *[ctypes.byref(x) for x in b1]))
+        res = [None] * len(models)
+        for j, i in enumerate(order):
+            res[i] = res_ord[j]
         out = []
         for i, (model, r) in enumerate(zip(models, res)):
             s = np.empty((model.Nk, model.Nz), dtype=np.complex128)
@@ -293,6 +316,8 @@ def _main(argv=None):
                     help="native: smc_march_many (C++ threads, batched engine); "
                          "python: Python threads, one engine launch per solve")
     ap.add_argument("--no-batch", action="store_true", help="native driver without the batcher")
+    ap.add_argument("--given-order", action="store_true",
+                    help="native driver: start the runs in list order (default: longest first)")
     a = ap.parse_args(argv)
     import os
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -308,7 +333,8 @@ def _main(argv=None):
     if a.driver == "native":
         res = march_ensemble_sharded(runs, nsteps=a.steps, rank=rank, world=world, form=a.form,
                                      concurrency=a.concurrency, device=local,
-                                     batched=not a.no_batch, march=march_ensemble_native)
+                                     batched=not a.no_batch, march=march_ensemble_native,
+                                     longest_first=not a.given_order)
     else:
         res = march_ensemble_sharded(runs, nsteps=a.steps, rank=rank, world=world, form=a.form,
                                      concurrency=a.concurrency, engine_ctas=a.engine_ctas,

@@ -100,3 +100,19 @@ def test_bench_times_the_slowest_replica():
         p.join(timeout=60)
         assert p.exitcode == 0
     assert got == {0: 2.5, 1: 2.5}
+
+
+def test_run_cost_orders_the_hard_runs_first():
+    """The native driver starts the runs in decreasing estimated cost: the
+    eta_T runs at high viscosity contrast and Rayleigh number before the
+    isoviscous ones of the same grid, larger grids before smaller."""
+    from specmc_gb300.config import ConvectionConfig
+    from specmc_gb300.ensemble import ensemble_configs, run_cost
+    c = lambda **kw: ConvectionConfig(**kw)
+    assert run_cost(c(viscosity_model="eta_T", deta_T=1e4, Ra=1e6, Nx=64, Nz=48)) > \
+        run_cost(c(viscosity_model="eta_T", deta_T=10.0, Ra=1e4, Nx=64, Nz=48)) > \
+        run_cost(c(viscosity_model="eta_z", Nx=64, Nz=48)) > run_cost(c(viscosity_model="const", Nx=64, Nz=48))
+    assert run_cost(c(viscosity_model="const", Nx=128, Nz=96)) > run_cost(c(viscosity_model="const", Nx=32, Nz=24))
+    runs = ensemble_configs(256, seed=0)
+    costs = sorted((run_cost(r["cfg"]) for r in runs), reverse=True)
+    assert len(costs) == 256 and costs[0] > 100 * costs[-1]

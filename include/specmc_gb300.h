@@ -233,6 +233,10 @@ int smc_schur_matvec(smc_handle* h, const double* eta, const double* v,
  * "theta_precond_lag" (0 <= f < 1, default 0.3): the mixed form reuses the
  * temperature preconditioner while a0 stays within this relative distance
  * of the a0 it was built for (0: rebuild for every new a0, as the reference).
+ * "bfbt_reuse_rel" (0 <= f < 1, default 0.02), "bfbt_reuse_age" (>= 1,
+ * default 32): the mixed form keeps its BFBT blocks while the harmonic-mean
+ * profile stays within this max-norm relative distance of the one they were
+ * built from, for at most this many solves (set before the first Stokes solve).
  * "engine_ctas" (>= 0): the CTAs of the persistent Krylov engine, for handles
  * that share the GPU concurrently; default 0 = Nk R CTAs, R the smallest
  * count that leaves at most two z-points of the x-direction phase to a CTA,

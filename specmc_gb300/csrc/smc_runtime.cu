@@ -1600,7 +1600,7 @@ struct Model {
   // spectral BFBT blocks from the harmonic-mean profile (stokes/bfbt.py:111-191).
   // The fast form keeps the blocks while the Galerkin profile stays within
   // 2% (max-norm, relative) of the one they were built from and for at most
-  // 16 solves: the blocks only precondition, so the solution is unchanged.
+  // 32 solves: the blocks only precondition, so the solution is unchanged.
   // The decision is taken on the device (bfbt_decide) inside a CUDA graph
   // whose rebuild runs under a conditional node the decision sets: one graph
   // launch per solve, the host enqueues the solve without waiting for it,
@@ -1655,7 +1655,9 @@ struct Model {
     SMC_CUDA(cudaGraphCreate(&bfbt_graph, 0));
     cudaGraphConditionalHandle cond;
     SMC_CUDA(cudaGraphConditionalHandleCreate(&cond, bfbt_graph, 0, cudaGraphCondAssignDefault));
-    capture_into(bfbt_graph, [&] { bfbt_decide(ctx, dBfbtRhs, dBfbtHeld, N, 16, 0.02, dBfbtHold, cond); });
+    capture_into(bfbt_graph, [&] {
+      bfbt_decide(ctx, dBfbtRhs, dBfbtHeld, N, bfbt_reuse_age, bfbt_reuse_rel, dBfbtHold, cond);
+    });
     cudaGraphNode_t decide = nullptr;
     size_t nn = 1;
     SMC_CUDA(cudaGraphGetNodes(bfbt_graph, &decide, &nn));
@@ -1672,6 +1674,11 @@ struct Model {
     capture_into(p.conditional.phGraph_out[0], [&] { bfbt_rebuild_launches(); });
     SMC_CUDA(cudaGraphInstantiate(&bfbt_exec, bfbt_graph, 0));
   }
+  // reuse of the BFBT blocks: profile within bfbt_reuse_rel (max-norm,
+  // relative) of the one they were built from, at most bfbt_reuse_age solves
+  // (captured into the rebuild graph at the handle's first fast BFBT solve)
+  int bfbt_reuse_age = 32;
+  double bfbt_reuse_rel = 0.02;
   // the next build runs whatever the profile (held profile invalid)
   void bfbt_invalidate() {
     if (dBfbtHold) SMC_CUDA(cudaMemsetAsync(&dBfbtHold->valid, 0, sizeof(int), stream));
@@ -2819,6 +2826,15 @@ int smc_set_option(smc_handle* h, const char* key, double value) {
       h->m.inner_fp32 = value != 0.0;
     } else if (k == "krylov_engine") {
       h->m.use_engine = value != 0.0;
+    } else if (k == "bfbt_reuse_rel" || k == "bfbt_reuse_age") {
+      if (h->m.bfbt_exec) throw std::runtime_error(k + ": set it before the first Stokes solve");
+      if (k == "bfbt_reuse_rel") {
+        if (!(value >= 0.0 && value < 1.0)) throw std::runtime_error("bfbt_reuse_rel must be in [0, 1)");
+        h->m.bfbt_reuse_rel = value;
+      } else {
+        if (!(value >= 1.0 && value <= 1e6)) throw std::runtime_error("bfbt_reuse_age must be in [1, 1e6]");
+        h->m.bfbt_reuse_age = (int)value;
+      }
     } else if (k == "theta_precond_lag") {
       if (!(value >= 0.0 && value < 1.0)) throw std::runtime_error("theta_precond_lag must be in [0, 1)");
       h->m.theta_lag = value;

@@ -69,3 +69,40 @@ def test_deferred_march_equals_stepwise(gb, Nx, Nz, deta):
     for key in KEYS:
         assert ca[key] == cc[key] == cb[key], (key, ca[key], cb[key], cc[key])
     assert ca["n_stokes"] >= STEPS and ca["n_theta_solves"] == STEPS
+
+
+def test_deferred_failed_solves_equal_stepwise(gb):
+    """The same comparison when every BFBT solve fails (a one-iteration
+    budget): the deferred Stokes result is read after the CFL reduction and
+    turns into the FP64 fallback and the dense rescue there, and what was
+    computed from the failed solve (psi, omega, the velocity, the CFL
+    reduction) is computed again; the later solves take the lagged-factor
+    route.  The resident march and the stepwise host loop give the same bits
+    and counters."""
+    from specmc_gb300.solver import RBCCoupled
+    api, CC, lib = gb
+    kw = dict(Nx=32, Nz=24, deta_T=1000.0, stokes_maxiter=1, form="mixed")
+    m0 = RBCCoupled(**kw)
+    th0 = np.ascontiguousarray(m0.seed(amp=3e-2, m=1, n=1))
+    m0.close()
+    steps = 12
+    ma = RBCCoupled(**kw)
+    _lib = ma._lib
+    lib.check(_lib.smc_set_state(ma._h, th0.ctypes.data_as(ctypes.c_void_p), lib.SMC_HOST))
+    info = lib.SmcMarchInfo()
+    for _ in range(steps):
+        lib.check(_lib.smc_advance(ma._h, 1e30, 1, 40.0, 4e-5, ctypes.byref(info)))
+    sa = np.empty_like(th0)
+    lib.check(_lib.smc_get_state(ma._h, sa.ctypes.data_as(ctypes.c_void_p), lib.SMC_HOST))
+    ca = ma.counters()
+    ma.close()
+    mc = RBCCoupled(**kw)
+    sc = np.array(th0, copy=True)
+    for _ in range(steps):
+        sc = mc.step(sc, mc.production_dt(sc, safety=40.0, dtmax=4e-5))
+    cc = mc.counters()
+    mc.close()
+    assert ca["n_bfbt_rescue"] >= 1
+    assert np.array_equal(sa, sc)
+    for key in KEYS + ("n_refresh", "n_defect"):
+        assert ca[key] == cc[key], (key, ca[key], cc[key])

@@ -1928,8 +1928,12 @@ struct Model {
     return redo;
   }
   // completes deferred work before an entry point other than the march's
-  void settle() {
-    mpf.valid = false;
+  // keep_prefetch: smc_step on the host input smc_production_dt just saw
+  void settle(bool keep_prefetch = false) {
+    if (!keep_prefetch) {
+      mpf.valid = false;
+      mpf_host.clear();
+    }
     if (stokes_pend_x) {           // left by an exception inside cfl_dt
       eng_pending[0] = false;
       stokes_pend_x = nullptr;
@@ -1939,6 +1943,9 @@ struct Model {
   // the step's memo test, prefetched by cfl_dt inside a march: the values of
   // memo_compare for the step's projected temperature
   bool want_memo_prefetch = false;
+  // the host input of the smc_production_dt call that made the prefetch
+  // (smc_step on the same bytes uses it: the device copy is then identical)
+  std::vector<unsigned char> mpf_host;
   struct MemoPrefetch {
     bool valid = false;
     const double2* src = nullptr;
@@ -2535,8 +2542,15 @@ int smc_destroy(smc_handle* h) {
 #define SMC_GUARD(h, ...) SMC_GUARD_IMPL(h, true, __VA_ARGS__)
 
 int smc_step(smc_handle* h, const double* in, double* out, int mem, double dt) {
-  SMC_GUARD(h, {
+  SMC_GUARD_IMPL(h, false, {
     Model& m = h->m;
+    // the input smc_production_dt just took: its prefetched projections and
+    // memo test hold for it (bytes compared on the host)
+    const bool same = mem == SMC_HOST && !m.mpf_host.empty() &&
+                      m.mpf_host.size() == (size_t)m.n * sizeof(double2) &&
+                      std::memcmp(m.mpf_host.data(), in, m.mpf_host.size()) == 0;
+    m.settle(same);
+    m.mpf_host.clear();
     smc::BatchScope bs(m.device, m.batch_mode);
     copy_in(m, m.dIn, in, mem, m.n);
     {
@@ -2566,7 +2580,16 @@ int smc_production_dt(smc_handle* h, const double* in, int mem, double safety, d
     Model& m = h->m;
     smc::BatchScope bs(m.device, m.batch_mode);
     copy_in(m, m.dIn, in, mem, m.n);
-    *dt_out = m.production_dt(m.dIn, safety, dtmax);
+    {
+      // prefetch the step's projections and memo test too (host input: a
+      // following smc_step on the same bytes uses them, as a march does)
+      Model::FlagScope pf(m.want_memo_prefetch, mem == SMC_HOST);
+      *dt_out = m.production_dt(m.dIn, safety, dtmax);
+    }
+    if (mem == SMC_HOST && m.mpf.valid) {
+      const unsigned char* p = reinterpret_cast<const unsigned char*>(in);
+      m.mpf_host.assign(p, p + m.n * sizeof(double2));
+    }
   })
 }
 

@@ -116,3 +116,18 @@ def test_run_cost_orders_the_hard_runs_first():
     runs = ensemble_configs(256, seed=0)
     costs = sorted((run_cost(r["cfg"]) for r in runs), reverse=True)
     assert len(costs) == 256 and costs[0] > 100 * costs[-1]
+
+
+def test_tuned_table_covers_the_ensemble_grids(tmp_path):
+    """The autotuner's committed table gives every grid class of the seeded
+    ensemble a CTA count among that grid's candidates; a missing table (or
+    grid) gives None, so the driver falls back to its default."""
+    from specmc_gb300 import ensemble, tune
+    table = tune.load()
+    for Nx, Nz in ensemble.GRIDS:
+        c = tune.batch_ctas_for(Nx, Nz, table)
+        assert c in tune.candidates(Nx), (Nx, Nz, c)
+    assert tune.candidates(64) == sorted(set(tune.candidates(64)))
+    assert all(16 <= c <= 304 for c in tune.candidates(128))
+    assert tune.load(str(tmp_path / "none.json")) == {}
+    assert tune.batch_ctas_for(64, 96, {}) is None

@@ -4,9 +4,10 @@ workload (Ra = 1e4, deta_T = 1000, 1x1 box, Nx = 64 x Nz = 96, seeded
 conductive perturbation amp = 3e-2 m = n = 1; the 200-step adaptive march).
 
 One bench "step" is one CFL-limited time step of that march (production_dt +
-step: eta(T), coupled Stokes solve with lagged LU + defect correction, BDF2
-temperature FGMRES).  W warm-up steps run first; the K timed steps are the
-steps W+1 .. W+K of the march.
+step: eta(T), the coupled Stokes solve, the BDF2 temperature solve) in the
+mixed form (BFBT-preconditioned FGMRES as FP32 iterative refinement of the
+FP64 system, one persistent launch per solve).  W warm-up steps run first; the
+K timed steps are the steps W+1 .. W+K of the march.
 
   value  steps/s with the state resident in HBM (device-resident march,
          CUDA events on the handle's stream around each step; an L2 flush
@@ -14,6 +15,11 @@ steps W+1 .. W+K of the march.
   e2e    the same steps through the public API with host (pinned) buffers:
          dt = api.production_dt(model, s); s = model.step(s, dt) -- the
          state crosses host<->device every step.
+  plain_fp64   the same march in the FP64 plain form (the reference's route:
+               lagged dense LU + defect correction), timed as `value`.
+  batched      a bounded sample of the many-run ensemble (the first 64 runs
+               of the seeded 256-run list, 20 steps each) through the batched
+               engine, against the plain form on the same sample.
 
 ``--impl reference`` times the CPU oracle (the restatement of the reference
 NumPy/SciPy path, all host threads) on the same workload and prints the same

@@ -280,20 +280,32 @@ __global__ void __launch_bounds__(DIAG_THREADS) smc_diag_kernel(
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double v1 = 0, v2 = 0, m = 0, t = 0, ntop = 0, nbot = 0;
-    for (int jc = 0; jc < DIAG_COLS && c0 + jc < N; ++jc) {
-      double a = 0, b = 0, mm = 0, tt = 0;
+  // one thread per column sums its slices (dependent FP64 chains stay short)
+  __shared__ double cs[4][DIAG_COLS];
+  if (threadIdx.x < DIAG_COLS) {
+    const int jc = threadIdx.x;
+    double a = 0, b = 0, mm = 0, tt = 0;
+    if (c0 + jc < N) {
       for (int sl = 0; sl < DIAG_SLICES; ++sl) {
         a += ps[0][sl][jc];
         b += ps[1][sl][jc];
         mm = fmax(mm, ps[2][sl][jc]);
         tt = fmax(tt, ps[3][sl][jc]);
       }
-      v1 += wq[c0 + jc] * (a / Nx);
-      v2 += wq[c0 + jc] * (b / Nx);
-      m = fmax(m, mm);
-      t = fmax(t, tt);
+      cs[0][jc] = wq[c0 + jc] * (a / Nx);
+      cs[1][jc] = wq[c0 + jc] * (b / Nx);
+    }
+    cs[2][jc] = mm;
+    cs[3][jc] = tt;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v1 = 0, v2 = 0, m = 0, t = 0, ntop = 0, nbot = 0;
+    for (int jc = 0; jc < DIAG_COLS && c0 + jc < N; ++jc) {
+      v1 += cs[0][jc];
+      v2 += cs[1][jc];
+      m = fmax(m, cs[2][jc]);
+      t = fmax(t, cs[3][jc]);
       ntop += fl[0][jc];
       nbot += fl[1][jc];
     }

@@ -280,7 +280,8 @@ __global__ void __launch_bounds__(DIAG_THREADS) smc_diag_kernel(
     }
   }
   __syncthreads();
-  // one thread per column sums its slices (dependent FP64 chains stay short)
+  // one thread per column sums its slices (dependent FP64 chains stay short);
+  // thread 0 then forms the quadrature-weighted sums in column order
   __shared__ double cs[4][DIAG_COLS];
   if (threadIdx.x < DIAG_COLS) {
     const int jc = threadIdx.x;
@@ -292,8 +293,8 @@ __global__ void __launch_bounds__(DIAG_THREADS) smc_diag_kernel(
         mm = fmax(mm, ps[2][sl][jc]);
         tt = fmax(tt, ps[3][sl][jc]);
       }
-      cs[0][jc] = wq[c0 + jc] * (a / Nx);
-      cs[1][jc] = wq[c0 + jc] * (b / Nx);
+      cs[0][jc] = a / Nx;
+      cs[1][jc] = b / Nx;
     }
     cs[2][jc] = mm;
     cs[3][jc] = tt;
@@ -302,8 +303,8 @@ __global__ void __launch_bounds__(DIAG_THREADS) smc_diag_kernel(
   if (threadIdx.x == 0) {
     double v1 = 0, v2 = 0, m = 0, t = 0, ntop = 0, nbot = 0;
     for (int jc = 0; jc < DIAG_COLS && c0 + jc < N; ++jc) {
-      v1 += cs[0][jc];
-      v2 += cs[1][jc];
+      v1 += wq[c0 + jc] * cs[0][jc];
+      v2 += wq[c0 + jc] * cs[1][jc];
       m = fmax(m, cs[2][jc]);
       t = fmax(t, cs[3][jc]);
       ntop += fl[0][jc];

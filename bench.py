@@ -197,10 +197,13 @@ def run_ours(args, rank, world):
     # CPU baseline first (rank 0, N = 1 only): a fresh interpreter
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, d = cpu_oracle_rate(args.cpu_steps, 0)
+        # the steps this arm times (at most 20 of them), after the same warm-up
+        k = args.cpu_steps if args.cpu_steps else min(args.steps, 20)
+        rate, d = cpu_oracle_rate(k, args.warmup, threads=os.cpu_count())
         cpu = {"value": rate, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "oracle restatement (NumPy/SciPy, default BLAS threads) on the first "
-                         "%d steps of the same march (%.1f s)" % (d["steps"], d["seconds"])}
+               "sample": "oracle restatement (NumPy/SciPy, LAPACK on all host threads), steps "
+                         "%d..%d of the same march (%.1f s timed)"
+                         % (args.warmup + 1, args.warmup + k, d["seconds"])}
 
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
 
@@ -403,7 +406,8 @@ def main():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
-    ap.add_argument("--cpu-steps", type=int, default=6)
+    ap.add_argument("--cpu-steps", type=int, default=None,
+                    help="CPU baseline: timed steps after the warm-up (default: --steps, at most 20)")
     ap.add_argument("--ref-steps", type=int, default=None,
                     help="reference arm: timed steps (default: --steps)")
     ap.add_argument("--ref-warmup", type=int, default=None,

@@ -5,7 +5,6 @@ reference, every GPU parity test downstream would be measuring against the
 wrong thing.
 """
 import os
-import types
 
 import numpy as np
 import pytest

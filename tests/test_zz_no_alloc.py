@@ -13,7 +13,6 @@ and passes alone in a fresh process as well as after the other tests.
 """
 import ctypes
 
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
